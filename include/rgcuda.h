@@ -1,0 +1,206 @@
+/* rgcuda.h -- C ABI of the GB300 ray-tracing core that replaces Raygun's Vulkan RT path.
+ *
+ * Every entry point returns rg_status (0 = RG_OK, negative = error; rg_last_error() gives text).
+ * The library owns all device memory; inputs are copied; work is ordered on the context's stream
+ * and rg_render() is asynchronous until rg_download()/rg_synchronize().  One context per host
+ * thread, calls serialized per context (Raygun calls the renderer from its main loop only,
+ * raygun/raygun.cpp:91-133).
+ *
+ * Data layouts are byte-identical to Raygun's shared GLSL/C++ structs.
+ */
+#ifndef RGCUDA_H
+#define RGCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t rg_status;
+enum {
+    RG_OK = 0,
+    RG_ERR_INVALID_ARG = -1,
+    RG_ERR_CUDA = -2,
+    RG_ERR_OUT_OF_MEMORY = -3,
+    RG_ERR_NOT_READY = -4,     /* e.g. render before geometry/TLAS */
+    RG_ERR_STACK_OVERFLOW = -5,
+    RG_ERR_BUDGET = -6,        /* HBM budget of rg_device_opts exceeded */
+    RG_ERR_NO_DEVICE = -7
+};
+
+typedef struct rg_ctx rg_ctx;
+
+typedef struct {
+    int32_t device;            /* CUDA ordinal */
+    uint32_t flags;            /* RG_FLAG_* */
+    uint64_t hbm_budget_bytes; /* 0 = unlimited */
+} rg_device_opts;
+#define RG_FLAG_DEBUG_IMAGES 1u /* keep roughTransitions / roughColorsA/B for rg_download_image */
+#define RG_FLAG_COUNT_VISITS 2u /* count BVH node / triangle visits (roofline accounting) */
+
+/* resources/shaders/vertex.def:3-7 (render/vertex.hpp:27-29): 32 B */
+typedef struct {
+    float position[3];
+    uint32_t matIndex;
+    float normal[3];
+    float pad1;
+} rg_vertex;
+
+/* resources/shaders/gpu_material.def:11-26 (gpu/gpu_material.hpp:27-31): 64 B */
+typedef struct {
+    float diffuse[3];
+    float transparency;
+    float specular[3];
+    float reflectivity;
+    float roughness;
+    float ior;
+    uint32_t effectId;
+    uint32_t rayConsumption;
+    float emission;
+    float pad0, pad1, pad2;
+} rg_material;
+
+/* resources/shaders/uniform_buffer_object.def:3-17 (gpu/uniform_buffer.hpp:29-31), std140: 192 B.
+ * Matrices are column-major (glm).  showAlpha is a 32-bit bool as in std140. */
+typedef struct {
+    float viewInverse[16];
+    float projInverse[16];
+    float clearColor[3];
+    int32_t numSamples;
+    float lightDir[3];
+    int32_t maxRecursions;
+    float time;
+    uint32_t showAlpha;
+    float pad0, pad1;
+    float fadeColor[4];
+} rg_ubo;
+
+/* One TLAS instance: the 3x4 row-major object-to-world transform of
+ * VkAccelerationStructureInstanceKHR (render/acceleration_structure.cpp:34-51), the BLAS handle,
+ * the cull mask (0xFF in Raygun) and the InstanceOffsetTableEntry
+ * (resources/shaders/instance_offset_table.def:1-3).  customIndex = position in the array. 72 B. */
+typedef struct {
+    float transform[3][4];
+    uint32_t blas;
+    uint32_t mask;
+    uint32_t vertexBufferOffset;
+    uint32_t indexBufferOffset;
+    uint32_t materialBufferOffset;
+    uint32_t pad;
+} rg_instance;
+
+/* GPU time of the profiler ranges of raygun/profiler.def:6-10, milliseconds of the last frame. */
+typedef struct {
+    float asBuild;   /* TLAS build (raytracer.cpp:78,84) */
+    float rtTotal;   /* trace + post (raytracer.cpp:93,144) */
+    float rtOnly;    /* trace (raytracer.cpp:95,104) */
+    float postproc;  /* roughness + composite + FXAA (raytracer.cpp:106,142) */
+    float rough;     /* roughness approximation (raytracer.cpp:111,123) */
+    float refit;     /* BLAS refits issued since the previous frame (not in the reference) */
+} rg_timings;
+
+/* Ray statistics of the last frame. */
+typedef struct {
+    uint64_t primary;    /* camera rays */
+    uint64_t shadow;     /* SHADOW_TRACE / SHADOW_INTERNAL rays that traversed */
+    uint64_t secondary;  /* reflection + refraction rays */
+    uint64_t masked;     /* mask-0 traces (closesthit.rchit:144): miss shader only, no traversal */
+    uint64_t nodes;      /* BVH node visits (RG_FLAG_COUNT_VISITS) */
+    uint64_t tris;       /* triangle tests (RG_FLAG_COUNT_VISITS) */
+    uint64_t stack_overflows;
+    uint64_t pad;
+} rg_stats;
+
+/* Debug images of Raytracer::selectResultImage (raytracer.cpp:379-392). */
+enum {
+    RG_IMAGE_FINAL = 0,
+    RG_IMAGE_BASE = 1,
+    RG_IMAGE_NORMAL = 2,
+    RG_IMAGE_ROUGH = 3,
+    RG_IMAGE_ROUGH_TRANSITION = 4,
+    RG_IMAGE_ROUGH_COLORS_A = 5,
+    RG_IMAGE_ROUGH_COLORS_B = 6,
+    RG_IMAGE_PRE_FXAA = 7
+};
+
+/* Replaces Raytracer::Raytracer (render/raytracer.cpp:38-52) and the device parts of
+ * VulkanContext (raygun/vulkan_context.cpp). */
+rg_status rg_create(rg_ctx** out, const rg_device_opts* opts);
+rg_status rg_destroy(rg_ctx* ctx);
+const char* rg_last_error(const rg_ctx* ctx);
+
+/* Replaces RenderSystem::setupModelBuffers (render/render_system.cpp:192-223): copies the packed
+ * vertex / index / material buffers to device memory. */
+rg_status rg_upload_geometry(rg_ctx* ctx, const rg_vertex* vertices, uint32_t nv, const uint32_t* indices, uint32_t ni,
+                             const rg_material* materials, uint32_t nm);
+/* Replaces RenderSystem::updateModelBuffers (render/render_system.cpp:225-233) for a range:
+ * changed vertices (the caller then refits) / materials (live material edit,
+ * gpu/gpu_material.cpp:52-94). */
+rg_status rg_update_vertices(rg_ctx* ctx, uint32_t first, const rg_vertex* vertices, uint32_t n);
+rg_status rg_update_materials(rg_ctx* ctx, uint32_t first, const rg_material* materials, uint32_t n);
+
+/* Replaces BottomLevelAS::BottomLevelAS (render/acceleration_structure.cpp:140-194) as driven by
+ * Raytracer::setupBottomLevelAS (render/raytracer.cpp:54-74): triangles
+ * indices[indexOffset + 3k + 0..2] + vertexOffset, k < triCount.  *out_blas receives the handle. */
+rg_status rg_build_blas(rg_ctx* ctx, uint32_t vertexOffset, uint32_t indexOffset, uint32_t triCount, uint32_t* out_blas);
+/* Refit of a BLAS after its vertices moved (same topology).  No reference counterpart: Raygun
+ * never refits. */
+rg_status rg_refit_blas(rg_ctx* ctx, uint32_t blas);
+
+/* Replaces TopLevelAS::TopLevelAS + Raytracer::setupTopLevelAS (render/acceleration_structure.cpp:55-138,
+ * render/raytracer.cpp:76-85): rebuilds the TLAS from scratch from host instances. */
+rg_status rg_build_tlas(rg_ctx* ctx, const rg_instance* instances, uint32_t n);
+/* Same, from instances already in device memory (device pointer). */
+rg_status rg_build_tlas_device(rg_ctx* ctx, const rg_instance* d_instances, uint32_t n);
+
+/* Replaces the resize path RenderSystem::reload -> Raytracer::setupRaytracingImages
+ * (render/render_system.cpp:66-81, render/raytracer.cpp:173-195). */
+rg_status rg_set_resolution(rg_ctx* ctx, uint32_t width, uint32_t height);
+
+/* Replaces RenderSystem::render's trace part: updateRenderTarget + doRaytracing
+ * (render/render_system.cpp:88-100, render/raytracer.cpp:87-171): trace, roughness passes,
+ * postprocess and FXAA into the RGBA32F framebuffer.  fxaa = 0 skips FXAA (ImGui checkbox,
+ * raytracer.cpp:136). */
+rg_status rg_render(rg_ctx* ctx, const rg_ubo* ubo, int32_t fxaa);
+
+/* Framebuffer (width*height*4 floats) to host memory; waits for the frame. */
+rg_status rg_download(rg_ctx* ctx, float* host_rgba);
+/* Device pointer of the RGBA32F framebuffer (valid until the next rg_set_resolution). */
+rg_status rg_framebuffer_device(rg_ctx* ctx, float** d_rgba);
+/* Any of the RG_IMAGE_* images as RGBA32F (roughTransition: value in .r). */
+rg_status rg_download_image(rg_ctx* ctx, int32_t which, float* host_rgba);
+
+rg_status rg_synchronize(rg_ctx* ctx);
+/* Replaces Profiler (raygun/profiler.cpp:55-105): GPU ranges of the last frame. */
+rg_status rg_get_timings(rg_ctx* ctx, rg_timings* out);
+rg_status rg_get_stats(rg_ctx* ctx, rg_stats* out);
+/* The CUDA stream the context orders its work on (cudaStream_t). */
+rg_status rg_get_stream(rg_ctx* ctx, void** stream);
+
+/* ---- parity / inspection entry points (no reference counterpart: the Vulkan driver's BVHs are
+ * opaque) ---- */
+/* LBVH of a BLAS (blas) or of the TLAS (blas = 0xFFFFFFFF): Morton codes per primitive, sorted
+ * order, children of the n-1 internal nodes (bit 31 = leaf, payload = sorted position) and the
+ * internal node boxes (6 floats: lo xyz, hi xyz).  Pointers may be NULL.  *n_out = primitive count. */
+rg_status rg_bvh_info(rg_ctx* ctx, uint32_t blas, uint32_t* n_out, uint32_t* morton, uint32_t* order, uint32_t* left,
+                      uint32_t* right, float* nodeboxes);
+/* World-to-object transforms the TLAS build computed (12 floats per instance). */
+rg_status rg_instance_inverse(rg_ctx* ctx, float* out);
+/* Closest hit of n rays (8 floats: origin.xyz, tmin, dir.xyz, tmax) through the current TLAS:
+ * hit_tuv n x 3 (t, u, v), hit_ids n x 2 (instance, primitive; 0xFFFFFFFF = miss). */
+rg_status rg_trace_rays(rg_ctx* ctx, const float* rays, uint32_t n, float* hit_tuv, uint32_t* hit_ids);
+/* Post passes alone on host G-buffers (width*height*4 floats each, current resolution):
+ * writes the framebuffer; used to check the post kernels on identical inputs. */
+rg_status rg_post_only(rg_ctx* ctx, const rg_ubo* ubo, const float* base, const float* normal, const float* rough,
+                       int32_t fxaa);
+
+/* Raw LBVH build over host boxes (n x 6 floats), for the builder's parity tests. */
+rg_status rg_lbvh_build_host(rg_ctx* ctx, const float* boxes, uint32_t n, uint32_t* morton, uint32_t* order,
+                             uint32_t* left, uint32_t* right, float* nodeboxes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RGCUDA_H */

@@ -1196,7 +1196,7 @@ orc_scene* orc_scene_create(const void* vertices, uint32_t nv, const uint32_t* i
     for (uint32_t i = 0; i < ninst; ++i) {
         Inst& d = s->inst[i];
         std::memcpy(d.m, in[i].transform, 48);
-        d.valid = affine_inverse(d.m, d.inv) && in[i].blas < nmesh;
+        d.valid = affine_inverse(d.m, d.inv) && in[i].blas < nmesh && (in[i].mask & 0xFFu) != 0u;
         d.blas = in[i].blas < nmesh ? in[i].blas : 0;
         d.vOff = in[i].vertexBufferOffset;
         d.iOff = in[i].indexBufferOffset;
@@ -1225,7 +1225,7 @@ int orc_scene_set_instances(orc_scene* sc, const void* instances, uint32_t ninst
     for (uint32_t i = 0; i < ninst; ++i) {
         Inst& d = s->inst[i];
         std::memcpy(d.m, in[i].transform, 48);
-        d.valid = affine_inverse(d.m, d.inv) && in[i].blas < s->blas.size();
+        d.valid = affine_inverse(d.m, d.inv) && in[i].blas < s->blas.size() && (in[i].mask & 0xFFu) != 0u;
         d.blas = in[i].blas < s->blas.size() ? in[i].blas : 0;
         d.vOff = in[i].vertexBufferOffset;
         d.iOff = in[i].indexBufferOffset;

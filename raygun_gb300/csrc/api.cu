@@ -1,0 +1,669 @@
+// api.cu -- the rgcuda C ABI: context, device memory, BLAS/TLAS management, frame pipeline.
+//
+// Replaces the Vulkan objects the reference's renderer owns (render/raytracer.cpp,
+// render/render_system.cpp, render/acceleration_structure.cpp): buffers become device
+// allocations, the pipeline and descriptor sets become kernel parameters, image barriers become
+// stream order, and the profiler's timestamp queries (raygun/profiler.cpp:55-105) become CUDA
+// events around the same five ranges.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rg_internal.cuh"
+
+using namespace rg;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct BvhSet {  // buffers of one LBVH (BLAS or TLAS)
+    uint32_t n = 0;
+    DevBuf primBoxes, morton, order, left, right, nodeBoxes, nodes, parents, flags;
+};
+
+struct BlasRec {
+    uint32_t vOff = 0, iOff = 0;
+    BvhSet bvh;
+    DevBuf tris;
+};
+
+}  // namespace
+
+struct rg_ctx {
+    int device = 0;
+    uint32_t flags = 0;
+    uint64_t budget = 0, allocated = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // geometry (render_system.cpp:192-223)
+    DevBuf vertices, indices, materials;
+    uint32_t nv = 0, ni = 0, nm = 0;
+    std::vector<BlasRec> blas;
+    DevBuf blasTable;
+    // TLAS
+    DevBuf instIn, instDev;
+    BvhSet tlas;
+    uint32_t nInst = 0;
+    bool tlasReady = false;
+    // shared sort scratch
+    DevBuf keysA, keysB, valsA, valsB, blockHist, bounds;
+    // images (raytracer.cpp:173-195)
+    uint32_t W = 0, H = 0;
+    DevBuf base, normal, rough, finalImg, fxaaOut, fb, dbgT, dbgA, dbgB;
+    bool lastFxaa = true;
+    // misc
+    DevBuf counters, tmpA, tmpB, tmpC, tmpD;
+    cudaEvent_t ev[8] = {};
+    bool refitPending = false;
+    bool haveFrame = false;
+};
+
+namespace {
+
+rg_status fail(rg_ctx* c, rg_status code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            return fail(c, e_ == cudaErrorMemoryAllocation ? RG_ERR_OUT_OF_MEMORY : RG_ERR_CUDA,        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+        }                                                                                               \
+    } while (0)
+
+#define TRY(expr)                    \
+    do {                             \
+        rg_status s_ = (expr);       \
+        if (s_ != RG_OK) return s_;  \
+    } while (0)
+
+rg_status ensure(rg_ctx* c, DevBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.cap >= bytes) return RG_OK;
+    size_t grow = bytes;
+    if (c->budget && c->allocated - b.cap + grow > c->budget)
+        return fail(c, RG_ERR_BUDGET, "device memory budget exceeded (" + std::to_string(c->allocated - b.cap + grow) + " > " +
+                                          std::to_string(c->budget) + " bytes)");
+    if (b.p) {
+        cudaFree(b.p);
+        c->allocated -= b.cap;
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    cudaError_t e = cudaMalloc(&b.p, grow);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return fail(c, RG_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    b.cap = grow;
+    c->allocated += grow;
+    return RG_OK;
+}
+
+void release(rg_ctx* c, DevBuf& b) {
+    if (b.p) {
+        cudaFree(b.p);
+        c->allocated -= b.cap;
+    }
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+rg_status ensure_sort_scratch(rg_ctx* c, uint32_t n) {
+    TRY(ensure(c, c->keysA, 4ull * n));
+    TRY(ensure(c, c->keysB, 4ull * n));
+    TRY(ensure(c, c->valsA, 4ull * n));
+    TRY(ensure(c, c->valsB, 4ull * n));
+    TRY(ensure(c, c->blockHist, 4ull * 256 * sort_block_count(n)));
+    TRY(ensure(c, c->bounds, 64));
+    return RG_OK;
+}
+
+rg_status ensure_bvh(rg_ctx* c, BvhSet& s, uint32_t n) {
+    s.n = n;
+    uint64_t m = n > 1 ? n - 1 : 1;
+    TRY(ensure(c, s.primBoxes, 24ull * n));
+    TRY(ensure(c, s.morton, 4ull * n));
+    TRY(ensure(c, s.order, 4ull * n));
+    TRY(ensure(c, s.left, 4ull * m));
+    TRY(ensure(c, s.right, 4ull * m));
+    TRY(ensure(c, s.nodeBoxes, 24ull * m));
+    TRY(ensure(c, s.nodes, sizeof(BvhNode) * m));
+    TRY(ensure(c, s.parents, 8ull * n));
+    TRY(ensure(c, s.flags, 4ull * m));
+    return ensure_sort_scratch(c, n);
+}
+
+LbvhBuffers buffers(rg_ctx* c, const BvhSet& s) {
+    LbvhBuffers b;
+    b.n = s.n;
+    b.primBoxes = s.primBoxes.as<float>();
+    b.morton = s.morton.as<uint32_t>();
+    b.order = s.order.as<uint32_t>();
+    b.left = s.left.as<uint32_t>();
+    b.right = s.right.as<uint32_t>();
+    b.nodeBoxes = s.nodeBoxes.as<float>();
+    b.nodes = s.nodes.as<BvhNode>();
+    b.keysA = c->keysA.as<uint32_t>();
+    b.keysB = c->keysB.as<uint32_t>();
+    b.valsA = c->valsA.as<uint32_t>();
+    b.valsB = c->valsB.as<uint32_t>();
+    b.blockHist = c->blockHist.as<uint32_t>();
+    b.parents = s.parents.as<uint32_t>();
+    b.flags = s.flags.as<uint32_t>();
+    b.bounds = c->bounds.as<uint32_t>();
+    return b;
+}
+
+// root box of an LBVH: internal node 0, or the single primitive's box
+const float* root_box(const BvhSet& s) { return s.n > 1 ? s.nodeBoxes.as<float>() : s.primBoxes.as<float>(); }
+
+rg_status upload_blas_entry(rg_ctx* c, uint32_t b) {
+    BlasRec& r = c->blas[b];
+    DevBlas e;
+    std::memset(&e, 0, sizeof(e));
+    e.nodes = r.bvh.nodes.as<BvhNode>();
+    e.tris = r.tris.as<float4>();
+    e.n = r.bvh.n;
+    DevBlas* d = c->blasTable.as<DevBlas>() + b;
+    CK(cudaMemcpyAsync(d, &e, sizeof(DevBlas), cudaMemcpyHostToDevice, c->stream));
+    if (r.bvh.n > 0) CK(cudaMemcpyAsync(d->root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
+    return RG_OK;
+}
+
+rg_status set_device(rg_ctx* c) {
+    CK(cudaSetDevice(c->device));
+    return RG_OK;
+}
+
+DevScene scene_of(rg_ctx* c) {
+    DevScene s;
+    s.blas = c->blasTable.as<DevBlas>();
+    s.inst = c->instDev.as<DevInstance>();
+    s.tlasNodes = c->tlas.nodes.as<BvhNode>();
+    s.tlasOrder = c->tlas.order.as<uint32_t>();
+    s.tlasN = c->nInst;
+    s.pad = 0;
+    s.tlasRoot = root_box(c->tlas);
+    s.vertices = c->vertices.as<rg_vertex>();
+    s.indices = c->indices.as<uint32_t>();
+    s.materials = c->materials.as<rg_material>();
+    return s;
+}
+
+rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
+    c->nInst = n;
+    c->tlasReady = false;
+    TRY(ensure(c, c->instDev, sizeof(DevInstance) * (size_t)(n ? n : 1)));
+    TRY(ensure_bvh(c, c->tlas, n));
+    CK(cudaEventRecord(c->ev[0], c->stream));
+    CK(setup_instances(c->instIn.as<rg_instance>(), n, c->blasTable.as<DevBlas>(), (uint32_t)c->blas.size(),
+                       c->instDev.as<DevInstance>(), c->tlas.primBoxes.as<float>(), c->stream));
+    CK(lbvh_build(buffers(c, c->tlas), c->stream));
+    CK(cudaEventRecord(c->ev[1], c->stream));
+    c->tlasReady = true;
+    return RG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rg_status rg_create(rg_ctx** out, const rg_device_opts* opts) {
+    if (!out) return RG_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return RG_ERR_NO_DEVICE;
+    rg_ctx* c = new rg_ctx();
+    if (opts) {
+        c->device = opts->device;
+        c->flags = opts->flags;
+        c->budget = opts->hbm_budget_bytes;
+    }
+    if (c->device < 0 || c->device >= count) {
+        delete c;
+        return RG_ERR_INVALID_ARG;
+    }
+    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return RG_ERR_CUDA;
+    }
+    for (auto& e : c->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            delete c;
+            return RG_ERR_CUDA;
+        }
+    if (ensure(c, c->counters, 8 * sizeof(unsigned long long)) != RG_OK) {
+        delete c;
+        return RG_ERR_OUT_OF_MEMORY;
+    }
+    cudaMemsetAsync(c->counters.p, 0, 64, c->stream);
+    *out = c;
+    return RG_OK;
+}
+
+rg_status rg_destroy(rg_ctx* c) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    DevBuf* bufs[] = {&c->vertices, &c->indices, &c->materials, &c->blasTable, &c->instIn, &c->instDev, &c->keysA, &c->keysB,
+                      &c->valsA, &c->valsB, &c->blockHist, &c->bounds, &c->base, &c->normal, &c->rough, &c->finalImg,
+                      &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC, &c->tmpD};
+    for (DevBuf* b : bufs) release(c, *b);
+    auto relBvh = [&](BvhSet& s) {
+        DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags};
+        for (DevBuf* b : bb) release(c, *b);
+    };
+    relBvh(c->tlas);
+    for (auto& r : c->blas) {
+        relBvh(r.bvh);
+        release(c, r.tris);
+    }
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return RG_OK;
+}
+
+const char* rg_last_error(const rg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+rg_status rg_upload_geometry(rg_ctx* c, const rg_vertex* v, uint32_t nv, const uint32_t* idx, uint32_t ni, const rg_material* m,
+                             uint32_t nm) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    if ((nv && !v) || (ni && !idx) || (nm && !m) || ni % 3 != 0) return fail(c, RG_ERR_INVALID_ARG, "bad geometry arrays");
+    for (uint32_t k = 0; k < nm; ++k)
+        if (m[k].rayConsumption < 1 || m[k].rayConsumption > 5)
+            return fail(c, RG_ERR_INVALID_ARG, "material rayConsumption outside 1..5 (gpu_material.def:21)");
+    for (uint32_t k = 0; k < ni; ++k)
+        if (idx[k] >= nv) return fail(c, RG_ERR_INVALID_ARG, "index " + std::to_string(k) + " out of range");
+    TRY(set_device(c));
+    TRY(ensure(c, c->vertices, sizeof(rg_vertex) * (size_t)nv));
+    TRY(ensure(c, c->indices, 4ull * ni));
+    TRY(ensure(c, c->materials, sizeof(rg_material) * (size_t)nm));
+    if (nv) CK(cudaMemcpyAsync(c->vertices.p, v, sizeof(rg_vertex) * (size_t)nv, cudaMemcpyHostToDevice, c->stream));
+    if (ni) CK(cudaMemcpyAsync(c->indices.p, idx, 4ull * ni, cudaMemcpyHostToDevice, c->stream));
+    if (nm) CK(cudaMemcpyAsync(c->materials.p, m, sizeof(rg_material) * (size_t)nm, cudaMemcpyHostToDevice, c->stream));
+    c->nv = nv;
+    c->ni = ni;
+    c->nm = nm;
+    return RG_OK;
+}
+
+rg_status rg_update_vertices(rg_ctx* c, uint32_t first, const rg_vertex* v, uint32_t n) {
+    if (!c || (n && !v) || (uint64_t)first + n > c->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
+    TRY(set_device(c));
+    if (n) CK(cudaMemcpyAsync(c->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    return RG_OK;
+}
+
+rg_status rg_update_materials(rg_ctx* c, uint32_t first, const rg_material* m, uint32_t n) {
+    if (!c || (n && !m) || (uint64_t)first + n > c->nm) return fail(c, RG_ERR_INVALID_ARG, "material range outside the uploaded buffer");
+    for (uint32_t k = 0; k < n; ++k)
+        if (m[k].rayConsumption < 1 || m[k].rayConsumption > 5) return fail(c, RG_ERR_INVALID_ARG, "material rayConsumption outside 1..5");
+    TRY(set_device(c));
+    if (n) CK(cudaMemcpyAsync(c->materials.as<rg_material>() + first, m, sizeof(rg_material) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    return RG_OK;
+}
+
+rg_status rg_build_blas(rg_ctx* c, uint32_t vOff, uint32_t iOff, uint32_t triCount, uint32_t* out) {
+    if (!c || !out) return RG_ERR_INVALID_ARG;
+    if ((uint64_t)iOff + 3ull * triCount > c->ni) return fail(c, RG_ERR_INVALID_ARG, "triangle range outside the index buffer");
+    if (triCount >= 0x7FFFFFFFu) return fail(c, RG_ERR_INVALID_ARG, "too many triangles");
+    TRY(set_device(c));
+    // vertex references of this range must stay inside the vertex buffer (checked on the host copy
+    // the caller passed at upload time would be cheaper, but the index buffer lives on the device)
+    uint32_t b = (uint32_t)c->blas.size();
+    c->blas.emplace_back();
+    BlasRec& r = c->blas.back();
+    r.vOff = vOff;
+    r.iOff = iOff;
+    TRY(ensure_bvh(c, r.bvh, triCount));
+    TRY(ensure(c, r.tris, 48ull * (triCount ? triCount : 1)));
+    if (triCount) {
+        CK(tri_boxes(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), vOff, iOff, triCount, r.bvh.primBoxes.as<float>(), c->stream));
+        CK(lbvh_build(buffers(c, r.bvh), c->stream));
+        CK(tri_records(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), vOff, iOff, r.bvh.order.as<uint32_t>(), triCount,
+                       r.tris.as<float4>(), c->stream));
+    }
+    // the BLAS table grows; copy the existing entries over
+    DevBuf old = c->blasTable;
+    c->blasTable = DevBuf{};
+    TRY(ensure(c, c->blasTable, sizeof(DevBlas) * c->blas.size()));
+    if (old.p) {
+        CK(cudaMemcpyAsync(c->blasTable.p, old.p, sizeof(DevBlas) * b, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        release(c, old);
+    }
+    TRY(upload_blas_entry(c, b));
+    *out = b;
+    c->tlasReady = false;  // instances point at the BLAS table, which moved
+    return RG_OK;
+}
+
+rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
+    if (!c || b >= c->blas.size()) return fail(c, RG_ERR_INVALID_ARG, "unknown BLAS");
+    TRY(set_device(c));
+    BlasRec& r = c->blas[b];
+    uint32_t n = r.bvh.n;
+    if (!n) return RG_OK;
+    if (!c->refitPending) CK(cudaEventRecord(c->ev[6], c->stream));
+    CK(tri_boxes(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, n, r.bvh.primBoxes.as<float>(), c->stream));
+    CK(lbvh_refit(buffers(c, r.bvh), c->stream));
+    CK(tri_records(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, r.bvh.order.as<uint32_t>(), n,
+                   r.tris.as<float4>(), c->stream));
+    CK(cudaMemcpyAsync(c->blasTable.as<DevBlas>()[b].root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaEventRecord(c->ev[7], c->stream));
+    c->refitPending = true;
+    return RG_OK;
+}
+
+rg_status rg_build_tlas(rg_ctx* c, const rg_instance* inst, uint32_t n) {
+    if (!c || (n && !inst)) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    TRY(ensure(c, c->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
+    if (n) CK(cudaMemcpyAsync(c->instIn.p, inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    return build_tlas_from_device_instances(c, n);
+}
+
+rg_status rg_build_tlas_device(rg_ctx* c, const rg_instance* d_inst, uint32_t n) {
+    if (!c || (n && !d_inst)) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    TRY(ensure(c, c->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
+    if (n) CK(cudaMemcpyAsync(c->instIn.p, d_inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+    return build_tlas_from_device_instances(c, n);
+}
+
+rg_status rg_set_resolution(rg_ctx* c, uint32_t w, uint32_t h) {
+    if (!c || w == 0 || h == 0 || w > 16384 || h > 16384) return fail(c, RG_ERR_INVALID_ARG, "resolution must be 1..16384");
+    TRY(set_device(c));
+    size_t px = (size_t)w * h;
+    TRY(ensure(c, c->base, 8 * px));
+    TRY(ensure(c, c->normal, 8 * px));
+    TRY(ensure(c, c->rough, 8 * px));
+    TRY(ensure(c, c->finalImg, 8 * px));
+    TRY(ensure(c, c->fxaaOut, 8 * px));
+    TRY(ensure(c, c->fb, 16 * px));
+    if (c->flags & RG_FLAG_DEBUG_IMAGES) {
+        TRY(ensure(c, c->dbgT, 4 * px));
+        TRY(ensure(c, c->dbgA, 8 * px));
+        TRY(ensure(c, c->dbgB, 8 * px));
+    }
+    c->W = w;
+    c->H = h;
+    c->haveFrame = false;
+    return RG_OK;
+}
+
+static rg_status run_post(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
+    PostParams pp;
+    std::memset(&pp, 0, sizeof(pp));
+    pp.W = c->W;
+    pp.H = c->H;
+    pp.base = c->base.as<uint2>();
+    pp.normal = c->normal.as<uint2>();
+    pp.rough = c->rough.as<uint2>();
+    pp.finalImg = c->finalImg.as<uint2>();
+    pp.fxaaOut = c->fxaaOut.as<uint2>();
+    pp.framebuffer = c->fb.as<float4>();
+    if (c->flags & RG_FLAG_DEBUG_IMAGES) {
+        pp.dbgTransition = c->dbgT.as<float>();
+        pp.dbgA = c->dbgA.as<uint2>();
+        pp.dbgB = c->dbgB.as<uint2>();
+    }
+    for (int k = 0; k < 4; ++k) pp.fade[k] = ubo->fadeColor[k];
+    pp.showAlpha = ubo->showAlpha ? 1 : 0;
+    pp.fxaa = fxaa ? 1 : 0;
+    CK(cudaEventRecord(c->ev[3], c->stream));
+    CK(launch_rough_post(pp, c->stream));
+    CK(cudaEventRecord(c->ev[4], c->stream));
+    CK(launch_fxaa(pp, c->stream));
+    CK(cudaEventRecord(c->ev[5], c->stream));
+    c->lastFxaa = fxaa != 0;
+    c->haveFrame = true;
+    return RG_OK;
+}
+
+static rg_status check_ubo(rg_ctx* c, const rg_ubo* ubo) {
+    if (!ubo) return fail(c, RG_ERR_INVALID_ARG, "null ubo");
+    if (ubo->numSamples < 1 || ubo->numSamples > 32) return fail(c, RG_ERR_INVALID_ARG, "numSamples outside 1..32 (render_system.cpp:263)");
+    if (ubo->maxRecursions < 0 || ubo->maxRecursions > 8) return fail(c, RG_ERR_INVALID_ARG, "maxRecursions outside 0..8");
+    return RG_OK;
+}
+
+rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    TRY(check_ubo(c, ubo));
+    if (!c->W) return fail(c, RG_ERR_NOT_READY, "rg_set_resolution was not called");
+    if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS (call rg_build_tlas after the last rg_build_blas)");
+    TRY(set_device(c));
+    TraceParams tp;
+    std::memset(&tp, 0, sizeof(tp));
+    tp.scene = scene_of(c);
+    tp.ubo = *ubo;
+    tp.W = c->W;
+    tp.H = c->H;
+    tp.base = c->base.as<uint2>();
+    tp.normal = c->normal.as<uint2>();
+    tp.rough = c->rough.as<uint2>();
+    tp.counters = c->counters.as<unsigned long long>();
+    tp.countVisits = (c->flags & RG_FLAG_COUNT_VISITS) ? 1 : 0;
+    CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+    CK(cudaEventRecord(c->ev[2], c->stream));
+    CK(launch_trace(tp, c->stream));
+    return run_post(c, ubo, fxaa);
+}
+
+rg_status rg_post_only(rg_ctx* c, const rg_ubo* ubo, const float* base, const float* normal, const float* rough, int32_t fxaa) {
+    if (!c || !base || !normal || !rough) return RG_ERR_INVALID_ARG;
+    if (!ubo) return fail(c, RG_ERR_INVALID_ARG, "null ubo");
+    if (!c->W) return fail(c, RG_ERR_NOT_READY, "rg_set_resolution was not called");
+    TRY(set_device(c));
+    size_t px = (size_t)c->W * c->H;
+    TRY(ensure(c, c->tmpA, 16 * px));
+    const float* src[3] = {base, normal, rough};
+    DevBuf* dst[3] = {&c->base, &c->normal, &c->rough};
+    for (int k = 0; k < 3; ++k) {
+        CK(cudaMemcpyAsync(c->tmpA.p, src[k], 16 * px, cudaMemcpyHostToDevice, c->stream));
+        CK(f32_to_h16(c->tmpA.as<float4>(), dst[k]->as<uint2>(), px, c->stream));
+    }
+    CK(cudaEventRecord(c->ev[2], c->stream));
+    return run_post(c, ubo, fxaa);
+}
+
+rg_status rg_download(rg_ctx* c, float* host) {
+    if (!c || !host) return RG_ERR_INVALID_ARG;
+    if (!c->haveFrame) return fail(c, RG_ERR_NOT_READY, "no frame rendered");
+    TRY(set_device(c));
+    CK(cudaMemcpyAsync(host, c->fb.p, 16ull * c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
+}
+
+rg_status rg_framebuffer_device(rg_ctx* c, float** d) {
+    if (!c || !d) return RG_ERR_INVALID_ARG;
+    if (!c->W) return fail(c, RG_ERR_NOT_READY, "rg_set_resolution was not called");
+    *d = c->fb.as<float>();
+    return RG_OK;
+}
+
+rg_status rg_download_image(rg_ctx* c, int32_t which, float* host) {
+    if (!c || !host) return RG_ERR_INVALID_ARG;
+    if (!c->haveFrame) return fail(c, RG_ERR_NOT_READY, "no frame rendered");
+    TRY(set_device(c));
+    size_t px = (size_t)c->W * c->H;
+    TRY(ensure(c, c->tmpB, 16 * px));
+    const uint2* h16 = nullptr;
+    switch (which) {
+        case RG_IMAGE_FINAL: h16 = c->lastFxaa ? c->fxaaOut.as<uint2>() : c->finalImg.as<uint2>(); break;
+        case RG_IMAGE_BASE: h16 = c->lastFxaa ? c->finalImg.as<uint2>() : c->base.as<uint2>(); break;  // swapped by FXAA (raytracer.cpp:139)
+        case RG_IMAGE_NORMAL: h16 = c->normal.as<uint2>(); break;
+        case RG_IMAGE_ROUGH: h16 = c->rough.as<uint2>(); break;
+        case RG_IMAGE_PRE_FXAA: h16 = c->finalImg.as<uint2>(); break;
+        case RG_IMAGE_ROUGH_COLORS_A:
+        case RG_IMAGE_ROUGH_COLORS_B:
+        case RG_IMAGE_ROUGH_TRANSITION:
+            if (!(c->flags & RG_FLAG_DEBUG_IMAGES)) return fail(c, RG_ERR_NOT_READY, "context created without RG_FLAG_DEBUG_IMAGES");
+            if (which == RG_IMAGE_ROUGH_TRANSITION) {
+                CK(r32_to_rgba(c->dbgT.as<float>(), c->tmpB.as<float4>(), px, c->stream));
+            } else {
+                h16 = which == RG_IMAGE_ROUGH_COLORS_A ? c->dbgA.as<uint2>() : c->dbgB.as<uint2>();
+            }
+            break;
+        default: return fail(c, RG_ERR_INVALID_ARG, "unknown image");
+    }
+    if (h16) CK(h16_to_f32(h16, c->tmpB.as<float4>(), px, c->stream));
+    CK(cudaMemcpyAsync(host, c->tmpB.p, 16 * px, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
+}
+
+rg_status rg_synchronize(rg_ctx* c) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
+}
+
+rg_status rg_get_timings(rg_ctx* c, rg_timings* t) {
+    if (!c || !t) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    CK(cudaStreamSynchronize(c->stream));
+    std::memset(t, 0, sizeof(*t));
+    auto el = [&](int a, int b) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) {
+            cudaGetLastError();
+            ms = 0.0f;
+        }
+        return ms;
+    };
+    if (c->tlasReady) t->asBuild = el(0, 1);
+    if (c->haveFrame) {
+        t->rtOnly = el(2, 3);
+        t->rough = el(3, 4);
+        t->postproc = el(3, 5);
+        t->rtTotal = el(2, 5);
+    }
+    if (c->refitPending) {
+        t->refit = el(6, 7);
+        c->refitPending = false;
+    }
+    return RG_OK;
+}
+
+rg_status rg_get_stats(rg_ctx* c, rg_stats* s) {
+    if (!c || !s) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    unsigned long long v[8];
+    CK(cudaMemcpyAsync(v, c->counters.p, 64, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    s->primary = v[0];
+    s->shadow = v[1];
+    s->secondary = v[2];
+    s->masked = v[3];
+    s->nodes = v[4];
+    s->tris = v[5];
+    s->stack_overflows = v[6];
+    s->pad = 0;
+    return RG_OK;
+}
+
+rg_status rg_get_stream(rg_ctx* c, void** s) {
+    if (!c || !s) return RG_ERR_INVALID_ARG;
+    *s = (void*)c->stream;
+    return RG_OK;
+}
+
+static rg_status download_bvh(rg_ctx* c, const BvhSet& s, uint32_t* morton, uint32_t* order, uint32_t* left, uint32_t* right,
+                              float* nodeboxes) {
+    uint32_t n = s.n;
+    if (morton && n) CK(cudaMemcpyAsync(morton, s.morton.p, 4ull * n, cudaMemcpyDeviceToHost, c->stream));
+    if (order && n) CK(cudaMemcpyAsync(order, s.order.p, 4ull * n, cudaMemcpyDeviceToHost, c->stream));
+    if (n > 1) {
+        if (left) CK(cudaMemcpyAsync(left, s.left.p, 4ull * (n - 1), cudaMemcpyDeviceToHost, c->stream));
+        if (right) CK(cudaMemcpyAsync(right, s.right.p, 4ull * (n - 1), cudaMemcpyDeviceToHost, c->stream));
+        if (nodeboxes) CK(cudaMemcpyAsync(nodeboxes, s.nodeBoxes.p, 24ull * (n - 1), cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
+}
+
+rg_status rg_bvh_info(rg_ctx* c, uint32_t b, uint32_t* n_out, uint32_t* morton, uint32_t* order, uint32_t* left, uint32_t* right,
+                      float* nodeboxes) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    const BvhSet* s = nullptr;
+    if (b == 0xFFFFFFFFu) {
+        if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+        s = &c->tlas;
+    } else if (b < c->blas.size()) {
+        s = &c->blas[b].bvh;
+    } else {
+        return fail(c, RG_ERR_INVALID_ARG, "unknown BLAS");
+    }
+    if (n_out) *n_out = s->n;
+    TRY(set_device(c));
+    return download_bvh(c, *s, morton, order, left, right, nodeboxes);
+}
+
+rg_status rg_instance_inverse(rg_ctx* c, float* out) {
+    if (!c || !out) return RG_ERR_INVALID_ARG;
+    if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+    TRY(set_device(c));
+    std::vector<DevInstance> h(c->nInst);
+    if (c->nInst) CK(cudaMemcpyAsync(h.data(), c->instDev.p, sizeof(DevInstance) * c->nInst, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (uint32_t i = 0; i < c->nInst; ++i)
+        for (int r = 0; r < 3; ++r) {
+            out[12 * i + 4 * r + 0] = h[i].inv[r].x;
+            out[12 * i + 4 * r + 1] = h[i].inv[r].y;
+            out[12 * i + 4 * r + 2] = h[i].inv[r].z;
+            out[12 * i + 4 * r + 3] = h[i].inv[r].w;
+        }
+    return RG_OK;
+}
+
+rg_status rg_trace_rays(rg_ctx* c, const float* rays, uint32_t n, float* tuv, uint32_t* ids) {
+    if (!c || (n && (!rays || !tuv || !ids))) return RG_ERR_INVALID_ARG;
+    if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+    if (!n) return RG_OK;
+    TRY(set_device(c));
+    TRY(ensure(c, c->tmpA, 32ull * n));
+    TRY(ensure(c, c->tmpC, 12ull * n));
+    TRY(ensure(c, c->tmpD, 8ull * n));
+    CK(cudaMemcpyAsync(c->tmpA.p, rays, 32ull * n, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_trace_rays(scene_of(c), c->tmpA.as<float>(), n, c->tmpC.as<float>(), c->tmpD.as<uint32_t>(), c->stream));
+    CK(cudaMemcpyAsync(tuv, c->tmpC.p, 12ull * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(ids, c->tmpD.p, 8ull * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
+}
+
+rg_status rg_lbvh_build_host(rg_ctx* c, const float* boxes, uint32_t n, uint32_t* morton, uint32_t* order, uint32_t* left,
+                             uint32_t* right, float* nodeboxes) {
+    if (!c || (n && !boxes)) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    BvhSet s;
+    rg_status st = ensure_bvh(c, s, n);
+    if (st == RG_OK && n) {
+        cudaError_t e = cudaMemcpyAsync(s.primBoxes.p, boxes, 24ull * n, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = lbvh_build(buffers(c, s), c->stream);
+        if (e != cudaSuccess) st = fail(c, RG_ERR_CUDA, cudaGetErrorString(e));
+        if (st == RG_OK) st = download_bvh(c, s, morton, order, left, right, nodeboxes);
+    }
+    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags};
+    cudaStreamSynchronize(c->stream);
+    for (DevBuf* b : bb) release(c, *b);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,379 @@
+// lbvh.cu -- linear BVH builder (BLAS over triangles, TLAS over instance boxes).
+//
+// Replaces the driver-side builds of BottomLevelAS / TopLevelAS
+// (render/acceleration_structure.cpp:55-194), which the reference leaves opaque:
+//   1. primitive boxes (triangles: min/max of the three vertices)
+//   2. centroid bounds (order-preserving uint atomics: exact, order independent)
+//   3. 30-bit Morton codes of the centroids, normalised to the centroid bounds
+//   4. stable LSD radix sort of (code, primitive) in four 8-bit passes
+//   5. Karras 2012 hierarchy (n-1 internal nodes; equal codes split on the index)
+//   6. bottom-up boxes: one thread per leaf climbs; the second arrival at a node writes its box
+// Refit (topology kept, boxes recomputed) reruns step 6 only.
+#include "rg_internal.cuh"
+
+namespace rg {
+
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortRounds = 8;
+constexpr int kSortTile = kSortWarps * kSortRounds * 32;  // 2048 keys per block
+
+__global__ void k_tri_boxes(const rg_vertex* __restrict__ v, const uint32_t* __restrict__ idx, uint32_t vOff, uint32_t iOff,
+                            uint32_t n, float* __restrict__ boxes) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        const float* pos = v[vOff + idx[iOff + 3 * p + k]].position;
+        for (int a = 0; a < 3; ++a) {
+            float x = pos[a];
+            lo[a] = k == 0 ? x : fminf(lo[a], x);
+            hi[a] = k == 0 ? x : fmaxf(hi[a], x);
+        }
+    }
+    float* o = boxes + 6 * (size_t)p;
+    o[0] = lo[0]; o[1] = lo[1]; o[2] = lo[2]; o[3] = hi[0]; o[4] = hi[1]; o[5] = hi[2];
+}
+
+// triangle records in leaf order: v0 (w = primitive id), v1, v2
+__global__ void k_tri_records(const rg_vertex* __restrict__ v, const uint32_t* __restrict__ idx, uint32_t vOff, uint32_t iOff,
+                              const uint32_t* __restrict__ order, uint32_t n, float4* __restrict__ tris) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t p = order[k];
+    const float* a = v[vOff + idx[iOff + 3 * p + 0]].position;
+    const float* b = v[vOff + idx[iOff + 3 * p + 1]].position;
+    const float* c = v[vOff + idx[iOff + 3 * p + 2]].position;
+    tris[3 * (size_t)k + 0] = make_float4(a[0], a[1], a[2], __uint_as_float(p));
+    tris[3 * (size_t)k + 1] = make_float4(b[0], b[1], b[2], 0.0f);
+    tris[3 * (size_t)k + 2] = make_float4(c[0], c[1], c[2], 0.0f);
+}
+
+__device__ inline void centroid(const float* b, float* c) {
+    if (!(b[0] <= b[3])) {  // empty box (invalid instance): keyed at the origin
+        c[0] = c[1] = c[2] = 0.0f;
+        return;
+    }
+    for (int a = 0; a < 3; ++a) c[a] = __fmul_rn(__fadd_rn(b[a], b[3 + a]), 0.5f);
+}
+
+__global__ void k_bounds_init(uint32_t* bounds) {
+    if (threadIdx.x < 3) bounds[threadIdx.x] = 0xFFFFFFFFu;
+    else if (threadIdx.x < 6) bounds[threadIdx.x] = 0u;
+}
+
+__global__ void k_centroid_bounds(const float* __restrict__ boxes, uint32_t n, uint32_t* bounds) {
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        float c[3];
+        centroid(boxes + 6 * (size_t)p, c);
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = fminf(mn[a], c[a]);
+            mx[a] = fmaxf(mx[a], c[a]);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = fminf(mn[a], __shfl_xor_sync(0xFFFFFFFFu, mn[a], off));
+            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xFFFFFFFFu, mx[a], off));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int a = 0; a < 3; ++a) {
+            if (mn[a] <= mx[a]) {
+                atomicMin(&bounds[a], f2ord(mn[a]));
+                atomicMax(&bounds[3 + a], f2ord(mx[a]));
+            }
+        }
+}
+
+__global__ void k_morton(const float* __restrict__ boxes, uint32_t n, const uint32_t* __restrict__ bounds,
+                         uint32_t* __restrict__ morton, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float lo[3], inv[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = ord2f(bounds[a]);
+        float ext = __fsub_rn(ord2f(bounds[3 + a]), lo[a]);
+        inv[a] = ext > 0.0f ? __fdiv_rn(1.0f, ext) : 0.0f;
+    }
+    float c[3];
+    centroid(boxes + 6 * (size_t)p, c);
+    uint32_t x = quant10(c[0], lo[0], inv[0]), y = quant10(c[1], lo[1], inv[1]), z = quant10(c[2], lo[2], inv[2]);
+    uint32_t m = (expand10(x) << 2) | (expand10(y) << 1) | expand10(z);
+    morton[p] = m;
+    keys[p] = m;
+    vals[p] = p;
+}
+
+// ---- stable LSD radix sort ----------------------------------------------------------------------
+__global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                             uint32_t* __restrict__ blockHist, uint32_t nb) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t base = blockIdx.x * kSortTile;
+    for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
+        uint32_t k = base + i;
+        if (k < n) atomicAdd(&cnt[(keys[k] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    blockHist[(size_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// exclusive scan of blockHist in digit-major order (one block)
+__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* data, uint32_t total) {
+    __shared__ uint32_t part[1024];
+    uint32_t chunk = (total + 1023) / 1024;
+    uint32_t b = threadIdx.x * chunk, e = min(total, b + chunk);
+    uint32_t s = 0;
+    for (uint32_t i = b; i < e; ++i) s += data[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (uint32_t i = b; i < e; ++i) {
+        uint32_t x = data[i];
+        data[i] = run;
+        run += x;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+                                                                uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
+                                                                uint32_t n, int shift, const uint32_t* __restrict__ offsets,
+                                                                uint32_t nb) {
+    __shared__ uint32_t wc[kSortWarps][256];
+    for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&wc[0][0])[i] = 0;
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ltmask = (1u << lane) - 1u;
+    uint32_t base = blockIdx.x * kSortTile + w * (kSortRounds * 32);
+    uint32_t key[kSortRounds], val[kSortRounds], pos[kSortRounds];
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        uint32_t i = base + r * 32 + lane;
+        bool ok = i < n;
+        key[r] = ok ? keysIn[i] : 0u;
+        val[r] = ok ? valsIn[i] : 0u;
+        uint32_t digit = ok ? ((key[r] >> shift) & 0xFFu) : (256u + lane);
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        uint32_t before = ok ? wc[w][digit] : 0u;
+        __syncwarp();
+        pos[r] = before + __popc(peers & ltmask);
+        if (ok && (peers & ltmask) == 0) wc[w][digit] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {  // per digit: prefix over warps, seeded with this block's global offset
+        uint32_t d = threadIdx.x;
+        uint32_t run = offsets[(size_t)d * nb + blockIdx.x];
+        for (int ww = 0; ww < kSortWarps; ++ww) {
+            uint32_t t = wc[ww][d];
+            wc[ww][d] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        uint32_t i = base + r * 32 + lane;
+        if (i < n) {
+            uint32_t dst = wc[w][(key[r] >> shift) & 0xFFu] + pos[r];
+            keysOut[dst] = key[r];
+            valsOut[dst] = val[r];
+        }
+    }
+}
+
+// ---- Karras 2012 hierarchy ----------------------------------------------------------------------
+__device__ inline int delta(const uint32_t* __restrict__ k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint32_t a = k[i], b = k[j];
+    if (a == b) return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    return __clz(a ^ b);
+}
+
+__global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ left, uint32_t* __restrict__ right,
+                         uint32_t* __restrict__ parents) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = (int)n;
+    if (i >= N - 1) return;
+    int d = (delta(keys, N, i, i + 1) - delta(keys, N, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, N, i, i - d);
+    int lmax = 2;
+    while (delta(keys, N, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta(keys, N, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, N, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, N, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    uint32_t L = (lo == gamma) ? (kLeaf | (uint32_t)gamma) : (uint32_t)gamma;
+    uint32_t R = (hi == gamma + 1) ? (kLeaf | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+    left[i] = L;
+    right[i] = R;
+    parents[(L & kLeaf) ? (n - 1) + (L & ~kLeaf) : L] = (uint32_t)i;
+    parents[(R & kLeaf) ? (n - 1) + (R & ~kLeaf) : R] = (uint32_t)i;
+    if (i == 0) parents[0] = 0xFFFFFFFFu;
+}
+
+// ---- bottom-up boxes ----------------------------------------------------------------------------
+__device__ inline void load_box_cg(const float* p, float* b) {
+    for (int a = 0; a < 6; ++a) b[a] = __ldcg(p + a);
+}
+
+__global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t* __restrict__ order, uint32_t n,
+                            const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                            const uint32_t* __restrict__ parents, uint32_t* flags, float* nodeBoxes, BvhNode* nodes) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t node = parents[(n - 1) + k];
+    while (node != 0xFFFFFFFFu) {
+        __threadfence();
+        uint32_t old = atomicAdd(&flags[node], 1u);
+        if (old == 0) return;
+        __threadfence();
+        uint32_t L = left[node], R = right[node];
+        float bl[6], br[6];
+        if (L & kLeaf) load_box_cg(primBoxes + 6 * (size_t)order[L & ~kLeaf], bl);
+        else load_box_cg(nodeBoxes + 6 * (size_t)L, bl);
+        if (R & kLeaf) load_box_cg(primBoxes + 6 * (size_t)order[R & ~kLeaf], br);
+        else load_box_cg(nodeBoxes + 6 * (size_t)R, br);
+        float* o = nodeBoxes + 6 * (size_t)node;
+        for (int a = 0; a < 3; ++a) {
+            __stcg(o + a, fminf(bl[a], br[a]));
+            __stcg(o + 3 + a, fmaxf(bl[3 + a], br[3 + a]));
+        }
+        BvhNode nd;
+        nd.a = make_float4(bl[0], bl[3], bl[1], bl[4]);
+        nd.b = make_float4(bl[2], bl[5], br[0], br[3]);
+        nd.c = make_float4(br[1], br[4], br[2], br[5]);
+        nd.d = make_uint4(L, R, 0u, 0u);
+        nodes[node] = nd;
+        node = parents[node];
+    }
+}
+
+// ---- instances ----------------------------------------------------------------------------------
+__global__ void k_instances(const rg_instance* __restrict__ in, uint32_t n, const DevBlas* __restrict__ blas, uint32_t nblas,
+                            DevInstance* __restrict__ out, float* __restrict__ boxes) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rg_instance I = in[i];
+    const float* m = &I.transform[0][0];
+    float a00 = m[0], a01 = m[1], a02 = m[2], t0 = m[3];
+    float a10 = m[4], a11 = m[5], a12 = m[6], t1 = m[7];
+    float a20 = m[8], a21 = m[9], a22 = m[10], t2 = m[11];
+    float c00 = a11 * a22 - a12 * a21, c01 = a02 * a21 - a01 * a22, c02 = a01 * a12 - a02 * a11;
+    float c10 = a12 * a20 - a10 * a22, c11 = a00 * a22 - a02 * a20, c12 = a02 * a10 - a00 * a12;
+    float c20 = a10 * a21 - a11 * a20, c21 = a01 * a20 - a00 * a21, c22 = a00 * a11 - a01 * a10;
+    float det = (a00 * c00 + a01 * c10) + a02 * c20;
+    bool ok = (det != 0.0f) && isfinite(det) && I.blas < nblas && (I.mask & 0xFFu) != 0u;
+    float id = ok ? 1.0f / det : 0.0f;
+    float r[9] = {c00 * id, c01 * id, c02 * id, c10 * id, c11 * id, c12 * id, c20 * id, c21 * id, c22 * id};
+    DevInstance d;
+    for (int row = 0; row < 3; ++row) {
+        float tr = -((r[3 * row + 0] * t0 + r[3 * row + 1] * t1) + r[3 * row + 2] * t2);
+        d.inv[row] = make_float4(r[3 * row + 0], r[3 * row + 1], r[3 * row + 2], tr);
+        d.m[row] = make_float4(m[4 * row + 0], m[4 * row + 1], m[4 * row + 2], m[4 * row + 3]);
+    }
+    d.blas = ok ? I.blas : 0u;
+    d.valid = ok ? 1u : 0u;
+    d.vOff = I.vertexBufferOffset;
+    d.iOff = I.indexBufferOffset;
+    d.mOff = I.materialBufferOffset;
+    d.mask = I.mask;
+    d.pad0 = d.pad1 = 0;
+    out[i] = d;
+    float* o = boxes + 6 * (size_t)i;
+    if (ok && blas[I.blas].n > 0) {
+        const float* rb = blas[I.blas].root;
+        for (int row = 0; row < 3; ++row) {
+            float lo = m[4 * row + 3], hi = m[4 * row + 3];
+            for (int j = 0; j < 3; ++j) {
+                float e = m[4 * row + j] * rb[j], f = m[4 * row + j] * rb[3 + j];
+                lo = lo + fminf(e, f);
+                hi = hi + fmaxf(e, f);
+            }
+            o[row] = lo;
+            o[3 + row] = hi;
+        }
+    } else {
+        o[0] = o[1] = o[2] = INFINITY;
+        o[3] = o[4] = o[5] = -INFINITY;
+    }
+}
+
+inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
+
+}  // namespace
+
+size_t sort_block_count(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+
+cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_tri_boxes<<<blocks(n, 256), 256, 0, s>>>(v, idx, vOff, iOff, n, boxes);
+    return cudaGetLastError();
+}
+
+cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, const uint32_t* order, uint32_t n,
+                        float4* tris, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_tri_records<<<blocks(n, 256), 256, 0, s>>>(v, idx, vOff, iOff, order, n, tris);
+    return cudaGetLastError();
+}
+
+cudaError_t setup_instances(const rg_instance* in, uint32_t n, const DevBlas* blas, uint32_t nblas, DevInstance* out, float* boxes,
+                            cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_instances<<<blocks(n, 128), 128, 0, s>>>(in, n, blas, nblas, out, boxes);
+    return cudaGetLastError();
+}
+
+cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
+    if (b.n <= 1) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(b.flags, 0, sizeof(uint32_t) * (b.n - 1), s);
+    if (e != cudaSuccess) return e;
+    k_bottom_up<<<blocks(b.n, 256), 256, 0, s>>>(b.primBoxes, b.order, b.n, b.left, b.right, b.parents, b.flags, b.nodeBoxes, b.nodes);
+    return cudaGetLastError();
+}
+
+cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s) {
+    const uint32_t n = b.n;
+    if (n == 0) return cudaSuccess;
+    k_bounds_init<<<1, 32, 0, s>>>(b.bounds);
+    uint32_t gb = min(blocks(n, 256), 1024u);
+    k_centroid_bounds<<<gb, 256, 0, s>>>(b.primBoxes, n, b.bounds);
+    k_morton<<<blocks(n, 256), 256, 0, s>>>(b.primBoxes, n, b.bounds, b.morton, b.keysA, b.valsA);
+    const uint32_t nb = (uint32_t)sort_block_count(n);
+    uint32_t *kin = b.keysA, *vin = b.valsA, *kout = b.keysB, *vout = b.valsB;
+    for (int pass = 0; pass < 4; ++pass) {
+        int shift = 8 * pass;
+        k_sort_hist<<<nb, kSortThreads, 0, s>>>(kin, n, shift, b.blockHist, nb);
+        k_sort_scan<<<1, 1024, 0, s>>>(b.blockHist, 256u * nb);
+        k_sort_scatter<<<nb, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, b.blockHist, nb);
+        uint32_t* t = kin; kin = kout; kout = t;
+        t = vin; vin = vout; vout = t;
+    }
+    // after 4 passes the sorted data is back in keysA / valsA
+    cudaError_t e = cudaMemcpyAsync(b.order, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    if (n == 1) return cudaGetLastError();
+    k_karras<<<blocks(n - 1, 256), 256, 0, s>>>(kin, n, b.left, b.right, b.parents);
+    return lbvh_refit(b, s);
+}
+
+}  // namespace rg

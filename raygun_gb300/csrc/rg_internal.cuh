@@ -1,0 +1,161 @@
+// rg_internal.cuh -- device-side layouts and helpers shared by the rgcuda kernels.
+//
+// All translation units are compiled with -fmad=false: every + - * / below is one IEEE operation,
+// so the ray geometry (Morton codes, traversal, intersection, secondary ray set-up) reproduces the
+// same bits as a plain C++ evaluation of the same expressions.  Fused multiply-adds are written
+// out as fmaf() where they are wanted.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rgcuda.h"
+
+namespace rg {
+
+constexpr uint32_t kLeaf = 0x80000000u;
+constexpr int kTraversalStack = 64;
+constexpr int kMaxFrames = 10;  // maxRecursions (<= 8 supported) + primary + masked-miss leaf
+
+// BVH2 node: boxes of BOTH children so one 64-byte node fetch (four 16-byte loads) tests two
+// children.  refs: bit 31 set = leaf (payload = sorted position), else internal node index.
+struct __align__(16) BvhNode {
+    float4 a;  // L.lo.x, L.hi.x, L.lo.y, L.hi.y
+    float4 b;  // L.lo.z, L.hi.z, R.lo.x, R.hi.x
+    float4 c;  // R.lo.y, R.hi.y, R.lo.z, R.hi.z
+    uint4 d;   // left ref, right ref, 0, 0
+};
+static_assert(sizeof(BvhNode) == 64, "node");
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+// per-BLAS record read by the traversal kernel
+struct DevBlas {
+    const BvhNode* nodes;
+    const float4* tris;  // 3 float4 per sorted leaf: v0 (w = primitive id bits), v1, v2
+    uint32_t n;          // triangle count
+    uint32_t pad;
+    float root[6];       // root box (lo xyz, hi xyz)
+};
+
+// per-instance record read by the traversal and shading code
+struct __align__(16) DevInstance {
+    float4 inv[3];  // world -> object rows
+    float4 m[3];    // object -> world rows
+    uint32_t blas, valid, vOff, iOff;
+    uint32_t mOff, mask, pad0, pad1;
+};
+static_assert(sizeof(DevInstance) == 128, "instance");
+
+struct DevScene {
+    const DevBlas* blas;
+    const DevInstance* inst;
+    const BvhNode* tlasNodes;
+    const uint32_t* tlasOrder;  // sorted position -> instance
+    uint32_t tlasN;
+    uint32_t pad;
+    const float* tlasRoot;      // root box (lo xyz, hi xyz), device memory
+    const rg_vertex* vertices;
+    const uint32_t* indices;
+    const rg_material* materials;
+};
+
+// ---- explicit-rounding helpers ------------------------------------------------------------------
+__host__ __device__ inline uint32_t expand10(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__device__ inline uint32_t quant10(float c, float lo, float inv) {
+    float d = __fsub_rn(c, lo);
+    float q = __fmul_rn(d, inv);
+    float s = __fmul_rn(q, 1024.0f);
+    s = fminf(fmaxf(s, 0.0f), 1023.0f);
+    return (uint32_t)s;
+}
+
+// order-preserving float <-> uint mapping for atomic min/max
+__device__ inline uint32_t f2ord(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ inline float ord2f(uint32_t u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u); }
+
+__host__ __device__ inline float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+
+}  // namespace rg
+
+// internal launchers implemented in the .cu files
+namespace rg {
+
+struct LbvhBuffers {  // scratch + outputs of one LBVH build, sized by the caller (n primitives)
+    uint32_t n;
+    // inputs
+    float* primBoxes;      // n x 6, primitive order
+    // outputs
+    uint32_t* morton;      // n, primitive order
+    uint32_t* order;       // n, sorted position -> primitive
+    uint32_t* left;        // n-1
+    uint32_t* right;       // n-1
+    float* nodeBoxes;      // (n-1) x 6
+    BvhNode* nodes;        // n-1
+    // scratch
+    uint32_t* keysA; uint32_t* keysB; uint32_t* valsA; uint32_t* valsB;
+    uint32_t* blockHist;   // 256 * numBlocks(n)
+    uint32_t* parents;     // 2n (internal n-1 then leaves n)
+    uint32_t* flags;       // n-1
+    uint32_t* bounds;      // 6 (ordered uints)
+};
+
+size_t sort_block_count(uint32_t n);
+cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s);
+cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s);  // topology kept, primBoxes changed
+cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes,
+                      cudaStream_t s);
+cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, const uint32_t* order, uint32_t n,
+                        float4* tris, cudaStream_t s);
+cudaError_t setup_instances(const rg_instance* in, uint32_t n, const DevBlas* blas, uint32_t nblas, DevInstance* out,
+                            float* boxes, cudaStream_t s);
+
+struct TraceParams {
+    DevScene scene;
+    rg_ubo ubo;
+    uint32_t W, H;
+    uint2* base;    // RGBA16F images (8 B per pixel)
+    uint2* normal;
+    uint2* rough;
+    unsigned long long* counters;  // 8
+    int countVisits;
+};
+cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
+cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
+
+struct PostParams {
+    uint32_t W, H;
+    const uint2* base;     // half4 images (8 B per pixel)
+    const uint2* normal;
+    const uint2* rough;
+    uint2* finalImg;       // half4, postprocess output (FXAA input)
+    uint2* fxaaOut;        // half4, FXAA output (becomes the final image)
+    float4* framebuffer;   // RGBA32F output
+    // debug outputs (nullable)
+    float* dbgTransition;  // W*H floats
+    uint2* dbgA;           // half4
+    uint2* dbgB;           // half4
+    float fade[4];
+    int showAlpha;
+    int fxaa;
+};
+cudaError_t launch_rough_post(const PostParams& p, cudaStream_t s);
+cudaError_t launch_fxaa(const PostParams& p, cudaStream_t s);
+cudaError_t f32_to_h16(const float4* in, uint2* out, size_t n, cudaStream_t s);
+cudaError_t h16_to_f32(const uint2* in, float4* out, size_t n, cudaStream_t s);
+cudaError_t r32_to_rgba(const float* in, float4* out, size_t n, cudaStream_t s);
+
+}  // namespace rg

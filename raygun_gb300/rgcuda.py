@@ -1,0 +1,286 @@
+"""ctypes bindings of the rgcuda C ABI (include/rgcuda.h) and a thin Python mirror of the
+reference's render-facing interface (Raytracer / RenderSystem).
+
+The library is built in-tree (``raygun_gb300/librgcuda.so``).  There is no fallback: when the
+library is missing or no GPU is present every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import scenes
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librgcuda.so")
+
+RG_OK = 0
+ERRORS = {-1: "RG_ERR_INVALID_ARG", -2: "RG_ERR_CUDA", -3: "RG_ERR_OUT_OF_MEMORY", -4: "RG_ERR_NOT_READY",
+          -5: "RG_ERR_STACK_OVERFLOW", -6: "RG_ERR_BUDGET", -7: "RG_ERR_NO_DEVICE"}
+RG_FLAG_DEBUG_IMAGES = 1
+RG_FLAG_COUNT_VISITS = 2
+IMAGES = {"final": 0, "base": 1, "normal": 2, "rough": 3, "rough_transition": 4, "rough_colors_a": 5,
+          "rough_colors_b": 6, "pre_fxaa": 7}
+
+EXPORTS = [
+    "rg_create", "rg_destroy", "rg_last_error", "rg_upload_geometry", "rg_update_vertices", "rg_update_materials",
+    "rg_build_blas", "rg_refit_blas", "rg_build_tlas", "rg_build_tlas_device", "rg_set_resolution", "rg_render",
+    "rg_download", "rg_framebuffer_device", "rg_download_image", "rg_synchronize", "rg_get_timings", "rg_get_stats",
+    "rg_get_stream", "rg_bvh_info", "rg_instance_inverse", "rg_trace_rays", "rg_post_only", "rg_lbvh_build_host",
+]
+
+
+class DeviceOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("flags", ctypes.c_uint32), ("hbm_budget_bytes", ctypes.c_uint64)]
+
+
+class Timings(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_float) for k in ("asBuild", "rtTotal", "rtOnly", "postproc", "rough", "refit")]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("primary", "shadow", "secondary", "masked", "nodes", "tris",
+                                               "stack_overflows", "pad")]
+
+
+class RgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load librgcuda.so and declare its signatures (no GPU needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run `python -m raygun_gb300.build` (no CPU fallback exists)")
+    L = ctypes.CDLL(path)
+    P, U32, I32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32
+    sig = {
+        "rg_create": ([ctypes.POINTER(P), ctypes.POINTER(DeviceOpts)], I32),
+        "rg_destroy": ([P], I32),
+        "rg_last_error": ([P], ctypes.c_char_p),
+        "rg_upload_geometry": ([P, P, U32, P, U32, P, U32], I32),
+        "rg_update_vertices": ([P, U32, P, U32], I32),
+        "rg_update_materials": ([P, U32, P, U32], I32),
+        "rg_build_blas": ([P, U32, U32, U32, ctypes.POINTER(U32)], I32),
+        "rg_refit_blas": ([P, U32], I32),
+        "rg_build_tlas": ([P, P, U32], I32),
+        "rg_build_tlas_device": ([P, P, U32], I32),
+        "rg_set_resolution": ([P, U32, U32], I32),
+        "rg_render": ([P, P, I32], I32),
+        "rg_download": ([P, P], I32),
+        "rg_framebuffer_device": ([P, ctypes.POINTER(P)], I32),
+        "rg_download_image": ([P, I32, P], I32),
+        "rg_synchronize": ([P], I32),
+        "rg_get_timings": ([P, ctypes.POINTER(Timings)], I32),
+        "rg_get_stats": ([P, ctypes.POINTER(Stats)], I32),
+        "rg_get_stream": ([P, ctypes.POINTER(P)], I32),
+        "rg_bvh_info": ([P, U32, ctypes.POINTER(U32), P, P, P, P, P], I32),
+        "rg_instance_inverse": ([P, P], I32),
+        "rg_trace_rays": ([P, P, U32, P, P], I32),
+        "rg_post_only": ([P, P, P, P, P, I32], I32),
+        "rg_lbvh_build_host": ([P, P, U32, P, P, P, P, P], I32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    """One rgcuda context (one device, one stream).  Methods follow the reference's Raytracer /
+    RenderSystem calls they replace (see include/rgcuda.h)."""
+
+    def __init__(self, device=0, flags=0, hbm_budget_bytes=0):
+        self.L = load()
+        self.h = ctypes.c_void_p()
+        opts = DeviceOpts(device, flags, hbm_budget_bytes)
+        rc = self.L.rg_create(ctypes.byref(self.h), ctypes.byref(opts))
+        if rc != RG_OK:
+            raise RgError(rc, "rg_create failed (no CUDA device?)")
+        self.width = self.height = 0
+
+    def _ck(self, rc):
+        if rc != RG_OK:
+            raise RgError(rc, self.L.rg_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.L.rg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- RenderSystem::setupModelBuffers / updateModelBuffers
+    def upload_geometry(self, vertices, indices, materials):
+        v = np.ascontiguousarray(vertices, dtype=scenes.VERTEX)
+        i = np.ascontiguousarray(indices, dtype=np.uint32)
+        m = np.ascontiguousarray(materials, dtype=scenes.MATERIAL)
+        self._ck(self.L.rg_upload_geometry(self.h, _p(v), len(v), _p(i), len(i), _p(m), len(m)))
+
+    def update_vertices(self, first, vertices):
+        v = np.ascontiguousarray(vertices, dtype=scenes.VERTEX)
+        self._ck(self.L.rg_update_vertices(self.h, first, _p(v), len(v)))
+
+    def update_materials(self, first, materials):
+        m = np.ascontiguousarray(materials, dtype=scenes.MATERIAL)
+        self._ck(self.L.rg_update_materials(self.h, first, _p(m), len(m)))
+
+    # -- Raytracer::setupBottomLevelAS / setupTopLevelAS
+    def build_blas(self, vertex_offset, index_offset, tri_count) -> int:
+        out = ctypes.c_uint32()
+        self._ck(self.L.rg_build_blas(self.h, vertex_offset, index_offset, tri_count, ctypes.byref(out)))
+        return out.value
+
+    def refit_blas(self, blas):
+        self._ck(self.L.rg_refit_blas(self.h, blas))
+
+    def build_tlas(self, instances):
+        inst = np.ascontiguousarray(instances, dtype=scenes.INSTANCE)
+        self._ck(self.L.rg_build_tlas(self.h, _p(inst), len(inst)))
+
+    def build_tlas_device(self, dev_ptr: int, n: int):
+        self._ck(self.L.rg_build_tlas_device(self.h, ctypes.c_void_p(dev_ptr), n))
+
+    def set_resolution(self, w, h):
+        self._ck(self.L.rg_set_resolution(self.h, w, h))
+        self.width, self.height = w, h
+
+    # -- RenderSystem::render -> Raytracer::doRaytracing
+    def render(self, ubo, fxaa=True):
+        u = np.ascontiguousarray(ubo, dtype=scenes.UBO)
+        self._ck(self.L.rg_render(self.h, _p(u), 1 if fxaa else 0))
+
+    def download(self, out=None):
+        if out is None:
+            out = np.empty((self.height, self.width, 4), np.float32)
+        self._ck(self.L.rg_download(self.h, _p(out)))
+        return out
+
+    def download_to(self, host_ptr: int):
+        self._ck(self.L.rg_download(self.h, ctypes.c_void_p(host_ptr)))
+
+    def framebuffer_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        self._ck(self.L.rg_framebuffer_device(self.h, ctypes.byref(p)))
+        return p.value
+
+    def download_image(self, which):
+        out = np.empty((self.height, self.width, 4), np.float32)
+        self._ck(self.L.rg_download_image(self.h, IMAGES[which] if isinstance(which, str) else which, _p(out)))
+        return out
+
+    def synchronize(self):
+        self._ck(self.L.rg_synchronize(self.h))
+
+    def timings(self) -> dict:
+        t = Timings()
+        self._ck(self.L.rg_get_timings(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in Timings._fields_}
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._ck(self.L.rg_get_stats(self.h, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in Stats._fields_ if k != "pad"}
+
+    def stream(self) -> int:
+        p = ctypes.c_void_p()
+        self._ck(self.L.rg_get_stream(self.h, ctypes.byref(p)))
+        return p.value or 0
+
+    # -- parity / inspection
+    def bvh(self, blas: int):
+        b = 0xFFFFFFFF if blas < 0 else blas
+        n = ctypes.c_uint32()
+        self._ck(self.L.rg_bvh_info(self.h, b, ctypes.byref(n), None, None, None, None, None))
+        n = n.value
+        out = dict(morton=np.zeros(n, np.uint32), order=np.zeros(n, np.uint32),
+                   left=np.zeros(max(n - 1, 0), np.uint32), right=np.zeros(max(n - 1, 0), np.uint32),
+                   nodeboxes=np.zeros((max(n - 1, 0), 6), np.float32))
+        self._ck(self.L.rg_bvh_info(self.h, b, None, _p(out["morton"]), _p(out["order"]), _p(out["left"]),
+                                    _p(out["right"]), _p(out["nodeboxes"])))
+        return out
+
+    def instance_inverse(self, n):
+        out = np.zeros((n, 12), np.float32)
+        self._ck(self.L.rg_instance_inverse(self.h, _p(out)))
+        return out
+
+    def trace_rays(self, rays):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = len(rays)
+        tuv = np.zeros((n, 3), np.float32)
+        ids = np.zeros((n, 2), np.uint32)
+        self._ck(self.L.rg_trace_rays(self.h, _p(rays), n, _p(tuv), _p(ids)))
+        return tuv, ids
+
+    def post_only(self, ubo, base, normal, rough, fxaa=True):
+        u = np.ascontiguousarray(ubo, dtype=scenes.UBO)
+        b, n, r = (np.ascontiguousarray(x, np.float32) for x in (base, normal, rough))
+        self._ck(self.L.rg_post_only(self.h, _p(u), _p(b), _p(n), _p(r), 1 if fxaa else 0))
+
+    def lbvh_build_host(self, boxes):
+        boxes = np.ascontiguousarray(boxes, np.float32)
+        n = len(boxes)
+        out = dict(morton=np.zeros(n, np.uint32), order=np.zeros(n, np.uint32),
+                   left=np.zeros(max(n - 1, 0), np.uint32), right=np.zeros(max(n - 1, 0), np.uint32),
+                   nodeboxes=np.zeros((max(n - 1, 0), 6), np.float32))
+        self._ck(self.L.rg_lbvh_build_host(self.h, _p(boxes), n, _p(out["morton"]), _p(out["order"]),
+                                           _p(out["left"]), _p(out["right"]), _p(out["nodeboxes"])))
+        return out
+
+
+class Raytracer:
+    """Drop-in shape of raygun::render::Raytracer + the RenderSystem calls around it
+    (render/raytracer.hpp:36-46, render/render_system.hpp:52-63) over one Context."""
+
+    def __init__(self, scene: scenes.Scene, device=0, flags=0, hbm_budget_bytes=0):
+        self.ctx = Context(device, flags, hbm_budget_bytes)
+        self.scene = scene
+        self.blas_ids = []
+        self.ctx.set_resolution(scene.width, scene.height)
+
+    def setup_model_buffers(self):                # RenderSystem::setupModelBuffers
+        s = self.scene
+        self.ctx.upload_geometry(s.vertices, s.indices, s.materials)
+
+    def setup_bottom_level_as(self):              # Raytracer::setupBottomLevelAS
+        self.blas_ids = [self.ctx.build_blas(int(m["vertexOffset"]), int(m["indexOffset"]), int(m["triCount"]))
+                         for m in self.scene.meshes]
+
+    def setup_top_level_as(self, instances=None):  # Raytracer::setupTopLevelAS
+        inst = self.scene.instances if instances is None else instances
+        inst = inst.copy()
+        inst["blas"] = np.asarray(self.blas_ids, np.uint32)[inst["blas"]]
+        self.ctx.build_tlas(inst)
+
+    def do_raytracing(self, ubo=None, fxaa=True):  # Raytracer::doRaytracing
+        self.ctx.render(self.scene.ubo if ubo is None else ubo, fxaa)
+
+    def prepare(self):
+        self.setup_model_buffers()
+        self.setup_bottom_level_as()
+        self.setup_top_level_as()
+        return self
+
+    def render(self, ubo=None, fxaa=True):         # RenderSystem::render (headless)
+        self.do_raytracing(ubo, fxaa)
+        return self.ctx.download()

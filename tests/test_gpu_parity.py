@@ -1,0 +1,215 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle on the same seeded
+inputs.
+
+Bars (written per test):
+* LBVH: Morton codes, sorted order, topology, node boxes -- bit exact.
+* closest hit: instance / primitive ids and t, u, v -- bit exact (both sides evaluate the same
+  IEEE operations in the same order).
+* G-buffers and the final image: per-channel |diff| <= 2/255 on >= 99.9 % of pixels and
+  PSNR >= 50 dB against the oracle.  Ray geometry is bit exact; the residue comes from logf/powf
+  (CUDA vs glibc), which only reach colours.
+* post passes on identical G-buffers: bit exact.
+* ray counts (primary / shadow / secondary / mask-0): exact.
+"""
+import numpy as np
+import pytest
+
+from raygun_gb300 import scenes as S
+from test_oracle import camera_rays, random_boxes, random_rays
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2.0 / 255.0
+
+
+def psnr(a, b):
+    mse = float(np.mean((a.astype(np.float64) - b.astype(np.float64)) ** 2))
+    return float("inf") if mse == 0 else 10 * np.log10(1.0 / mse)
+
+
+def assert_image_close(gpu, ref, what, frac=0.999, min_psnr=50.0):
+    assert np.isfinite(gpu).all(), f"{what}: non-finite values"
+    err = np.abs(gpu - ref)
+    ok = (err <= TOL).all(-1)
+    p = psnr(np.clip(gpu, 0, 1), np.clip(ref, 0, 1))
+    print(f"{what}: exact {np.mean(err.max(-1) == 0):.5f}, within 2/255 {ok.mean():.5f}, max {err.max():.4g}, psnr {p:.1f} dB")
+    assert ok.mean() >= frac, f"{what}: only {ok.mean():.5f} of pixels within 2/255"
+    assert p >= min_psnr, f"{what}: PSNR {p:.1f} dB < {min_psnr}"
+
+
+def lbvh_equal(g, o):
+    for k in ("morton", "order", "left", "right"):
+        assert np.array_equal(g[k], o[k]), k
+    assert np.array_equal(g["nodeboxes"], o["nodeboxes"]), "nodeboxes"
+
+
+@pytest.mark.parametrize("n,dup", [(1, False), (2, False), (3, False), (100, False), (2049, True), (70000, False),
+                                   (300000, True)])
+def test_lbvh_build_bit_exact(rg, orc, n, dup):
+    boxes = random_boxes(n, 7 + n, dup)
+    ctx = rg.Context()
+    lbvh_equal(ctx.lbvh_build_host(boxes), orc.lbvh(boxes))
+
+
+def test_lbvh_all_equal_keys(rg, orc):
+    boxes = np.tile(np.array([[0, 0, 0, 1, 1, 1]], np.float32), (5000, 1))
+    ctx = rg.Context()
+    lbvh_equal(ctx.lbvh_build_host(boxes), orc.lbvh(boxes))
+
+
+def small_two_level():
+    return S.instanced_scene(width=96, height=54, counts=(6, 5, 3, 1, 4, 4, 1, 1), hf_n=32, ico_levels=(1, 2, 3, 3),
+                             num_samples=2, max_recursions=5, name="mini-c1")
+
+
+@pytest.fixture(scope="module")
+def c0_pair(rg, orc):
+    sc = S.c0_scene()
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES).prepare()
+    return sc, rt, orc.OracleScene(sc)
+
+
+@pytest.fixture(scope="module")
+def c1_pair(rg, orc):
+    sc = small_two_level()
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES).prepare()
+    return sc, rt, orc.OracleScene(sc)
+
+
+def test_blas_tlas_c0(c0_pair):
+    sc, rt, o = c0_pair
+    lbvh_equal(rt.ctx.bvh(0), o.bvh(0))
+    g, r = rt.ctx.bvh(-1), o.bvh(-1)
+    assert np.array_equal(g["morton"], r["morton"]) and np.array_equal(g["order"], r["order"])
+
+
+def test_two_level_bvh(c1_pair):
+    sc, rt, o = c1_pair
+    for b in range(len(sc.meshes)):
+        lbvh_equal(rt.ctx.bvh(b), o.bvh(b))
+    lbvh_equal(rt.ctx.bvh(-1), o.bvh(-1))
+    assert np.array_equal(rt.ctx.instance_inverse(len(sc.instances)), o.instance_inverse())
+
+
+@pytest.mark.parametrize("which", ["c0", "c1"])
+def test_closest_hit_bit_exact(which, c0_pair, c1_pair):
+    sc, rt, o = c0_pair if which == "c0" else c1_pair
+    if which == "c0":
+        rays = np.concatenate([camera_rays(sc, stride=2), random_rays(20000, 3)])
+    else:
+        rays = np.concatenate([camera_rays(sc), random_rays(20000, 4, lo=(-60, 0, -60), hi=(60, 14, 60))])
+    rays = np.concatenate([rays, rays[:5] * np.array([1, 1, 1, 1, 0, 0, 0, 1], np.float32)])  # zero directions miss
+    tg, ig = rt.ctx.trace_rays(rays)
+    to, io = o.trace(rays)
+    assert np.array_equal(ig, io)
+    assert np.array_equal(tg, to)
+    assert (ig[-5:, 0] == 0xFFFFFFFF).all()
+    assert (ig[:, 0] != 0xFFFFFFFF).mean() > (0.2 if which == "c0" else 0.03)
+
+
+def _gbuffers(rt):
+    return [rt.ctx.download_image(k) for k in ("base", "normal", "rough")]
+
+
+@pytest.mark.parametrize("which", ["c0", "c1"])
+def test_gbuffer_and_frame_parity(which, c0_pair, c1_pair, orc):
+    sc, rt, o = c0_pair if which == "c0" else c1_pair
+    rt.do_raytracing(fxaa=False)
+    gb = _gbuffers(rt)
+    st = rt.ctx.stats()
+    ob, on, orr, ost = o.render()
+    for k in ("primary", "shadow", "secondary", "masked"):
+        assert st[k] == ost[k], (k, st[k], ost[k])
+    assert st["stack_overflows"] == 0
+    for name, g, r in zip(("base", "normal", "rough"), gb, (ob, on, orr)):
+        assert_image_close(g, r, f"{which} {name}")
+    rt.do_raytracing(fxaa=True)
+    fin = rt.ctx.download()
+    ref = orc.post(sc.ubo, ob, on, orr)
+    assert_image_close(fin, ref, f"{which} final")
+
+
+@pytest.mark.parametrize("show_alpha,fade", [(0, (0, 0, 0, 0)), (1, (0, 0, 0, 0)), (0, (0.2, 0.4, 0.6, 0.5))])
+def test_post_passes_bit_exact(c0_pair, orc, show_alpha, fade):
+    sc, rt, o = c0_pair
+    ob, on, orr, _ = o.render()
+    u = sc.ubo.copy()
+    u["showAlpha"], u["fadeColor"] = show_alpha, fade
+    for fx in (False, True):
+        rt.ctx.post_only(u, ob, on, orr, fxaa=fx)
+        fin = rt.ctx.download()
+        ref, dbg = orc.post(u, ob, on, orr, fxaa=fx, debug=True)
+        assert np.array_equal(fin, ref), f"fxaa={fx}: {np.mean(fin != ref)} differ"
+    assert np.array_equal(rt.ctx.download_image("rough_transition")[..., 0], dbg[0][..., 0])
+    assert np.array_equal(rt.ctx.download_image("rough_colors_a"), dbg[1])
+    assert np.array_equal(rt.ctx.download_image("rough_colors_b"), dbg[2])
+    assert np.array_equal(rt.ctx.download_image("pre_fxaa"), dbg[3])
+
+
+def test_animation_refit_and_tlas_rebuild(rg, orc):
+    sc = small_two_level()
+    rt = rg.Raytracer(sc).prepare()
+    o = orc.OracleScene(sc)
+    anim = S.FrameAnimator(sc, seed=7, refit_prob=0.5)
+    for frame in range(3):
+        refits = anim.step()
+        for b, vo, nv in refits:
+            rt.ctx.update_vertices(vo, sc.vertices[vo:vo + nv])
+            rt.ctx.refit_blas(rt.blas_ids[b])
+            o.refit(b, sc.vertices[vo:vo + nv], vo)
+        rt.setup_top_level_as()
+        o.set_instances(sc.instances)
+        for b, _, _ in refits:
+            lbvh_equal(rt.ctx.bvh(b), o.bvh(b))
+        lbvh_equal(rt.ctx.bvh(-1), o.bvh(-1))
+        fin = rt.render()
+        ob, on, orr, _ = o.render()
+        assert_image_close(fin, orc.post(sc.ubo, ob, on, orr), f"frame {frame}")
+
+
+@pytest.mark.parametrize("spp,depth", [(1, 0), (3, 1), (4, 7), (9, 2)])
+def test_samples_and_depths(rg, orc, spp, depth):
+    sc = S.spheres_scene(n_spheres=16, width=80, height=45, num_samples=spp, max_recursions=depth, seed=5)
+    rt = rg.Raytracer(sc).prepare()
+    o = orc.OracleScene(sc)
+    fin = rt.render()
+    st = rt.ctx.stats()
+    ob, on, orr, ost = o.render()
+    for k in ("primary", "shadow", "secondary", "masked"):
+        assert st[k] == ost[k], (k, st[k], ost[k])
+    assert_image_close(fin, orc.post(sc.ubo, ob, on, orr), f"spp{spp} depth{depth}")
+
+
+def test_errors_are_status_codes(rg):
+    ctx = rg.Context()
+    sc = S.spheres_scene(n_spheres=2, width=16, height=16, slices=8, stacks=4)
+    with pytest.raises(rg.RgError) as e:
+        ctx.render(sc.ubo)
+    assert e.value.code in (-4,)
+    bad = sc.indices.copy()
+    bad[0] = 10 ** 6
+    with pytest.raises(rg.RgError) as e:
+        ctx.upload_geometry(sc.vertices, bad, sc.materials)
+    assert e.value.code == -1
+    m = sc.materials.copy()
+    m["rayConsumption"] = 0
+    with pytest.raises(rg.RgError):
+        ctx.upload_geometry(sc.vertices, sc.indices, m)
+    ctx.upload_geometry(sc.vertices, sc.indices, sc.materials)
+    with pytest.raises(rg.RgError):
+        ctx.build_blas(0, 0, len(sc.indices))  # range beyond the index buffer
+    u = sc.ubo.copy()
+    u["numSamples"] = 0
+    ctx.set_resolution(16, 16)
+    b = ctx.build_blas(0, 0, len(sc.indices) // 3)
+    inst = S.identity_instance(b)
+    ctx.build_tlas(inst)
+    with pytest.raises(rg.RgError):
+        ctx.render(u)
+
+
+def test_hbm_budget_rejects(rg):
+    ctx = rg.Context(hbm_budget_bytes=1 << 20)
+    with pytest.raises(rg.RgError) as e:
+        ctx.set_resolution(1920, 1080)
+    assert e.value.code == -6

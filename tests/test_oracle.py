@@ -1,0 +1,162 @@
+"""CPU tests of the oracle itself: LBVH invariants, Morton codes against an independent numpy
+evaluation, traversal against brute force, FP16 rounding, policies."""
+import numpy as np
+import pytest
+
+from raygun_gb300 import scenes as S
+
+
+def _expand10(v):
+    v = v.astype(np.uint64)
+    v = (v * 0x00010001) & 0xFF0000FF
+    v = (v * 0x00000101) & 0x0F00F00F
+    v = (v * 0x00000011) & 0xC30C30C3
+    v = (v * 0x00000005) & 0x49249249
+    return v.astype(np.uint32)
+
+
+def numpy_morton(boxes):
+    """Independent float32 evaluation of the Morton codes (same operation order)."""
+    b = boxes.astype(np.float32)
+    c = (b[:, :3] + b[:, 3:]) * np.float32(0.5)
+    lo, hi = c.min(0), c.max(0)
+    ext = hi - lo
+    with np.errstate(divide="ignore"):
+        inv = np.where(ext > 0, np.float32(1.0) / ext, np.float32(0.0)).astype(np.float32)
+    q = ((c - lo) * inv) * np.float32(1024.0)
+    q = np.clip(q, np.float32(0), np.float32(1023)).astype(np.uint32)
+    return (_expand10(q[:, 0]) << 2) | (_expand10(q[:, 1]) << 1) | _expand10(q[:, 2])
+
+
+def random_boxes(n, seed, dup=False):
+    rng = np.random.RandomState(seed)
+    c = rng.uniform(-10, 10, (n, 3)).astype(np.float32)
+    if dup:
+        c[: n // 2] = c[0]
+    e = rng.uniform(0.01, 0.5, (n, 3)).astype(np.float32)
+    return np.concatenate([c - e, c + e], 1).astype(np.float32)
+
+
+def check_topology(n, left, right, order):
+    """Every leaf reached exactly once from the root; every internal node once."""
+    if n == 1:
+        return
+    seen_leaf = np.zeros(n, int)
+    seen_node = np.zeros(n - 1, int)
+    stack = [0]
+    while stack:
+        i = stack.pop()
+        seen_node[i] += 1
+        for c in (left[i], right[i]):
+            if c & 0x80000000:
+                seen_leaf[c & 0x7FFFFFFF] += 1
+            else:
+                stack.append(int(c))
+    assert (seen_leaf == 1).all() and (seen_node == 1).all()
+    assert np.array_equal(np.sort(order), np.arange(n))
+
+
+@pytest.mark.parametrize("n,dup", [(1, False), (2, False), (3, False), (17, False), (1000, False), (5000, True)])
+def test_lbvh_oracle(orc, n, dup):
+    boxes = random_boxes(n, n, dup)
+    r = orc.lbvh(boxes)
+    assert np.array_equal(r["morton"], numpy_morton(boxes))
+    assert np.array_equal(r["order"], np.argsort(r["morton"], kind="stable"))
+    check_topology(n, r["left"], r["right"], r["order"])
+    if n > 1:
+        nb = r["nodeboxes"]
+        sorted_boxes = boxes[r["order"]]
+        for i in range(n - 1):
+            for c in (r["left"][i], r["right"][i]):
+                cb = sorted_boxes[c & 0x7FFFFFFF] if c & 0x80000000 else nb[c]
+                assert (nb[i, :3] <= cb[:3]).all() and (nb[i, 3:] >= cb[3:]).all()
+        assert np.array_equal(nb[0, :3], boxes[:, :3].min(0)) and np.array_equal(nb[0, 3:], boxes[:, 3:].max(0))
+
+
+def camera_rays(scene, stride=1):
+    """Primary rays of the raygen (1 spp), float32, built in numpy."""
+    u = scene.ubo[0]
+    vi = u["viewInverse"].astype(np.float32)  # [col][row]
+    pi = u["projInverse"].astype(np.float32)
+    W, H = scene.width, scene.height
+    ys, xs = np.mgrid[0:H:stride, 0:W:stride]
+    px = (xs.astype(np.float32) + np.float32(0.5)) / np.float32(W)
+    py = (ys.astype(np.float32) + np.float32(0.5)) / np.float32(H)
+    d = np.stack([px * 2 - 1, py * 2 - 1, np.ones_like(px), np.ones_like(px)], -1).reshape(-1, 4).astype(np.float32)
+    tg = d @ pi  # column-major: result_r = sum_c m[c][r] v_c
+    t3 = tg[:, :3] / np.linalg.norm(tg[:, :3], axis=1, keepdims=True)
+    dirs = t3 @ vi[:3, :3]
+    o = np.broadcast_to(vi[3, :3], dirs.shape)
+    rays = np.zeros((len(dirs), 8), np.float32)
+    rays[:, :3], rays[:, 3], rays[:, 4:7], rays[:, 7] = o, 0.001, dirs, 10000.0
+    return rays
+
+
+def random_rays(n, seed, lo=(-12, 0.2, -12), hi=(12, 8, 12)):
+    rng = np.random.RandomState(seed)
+    o = rng.uniform(lo, hi, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3], rays[:, 3], rays[:, 4:7], rays[:, 7] = o, 0.01, d, 1000.0
+    return rays
+
+
+def test_traversal_matches_brute_force(orc):
+    sc = S.spheres_scene(n_spheres=12, width=64, height=36, slices=16, stacks=8)
+    o = orc.OracleScene(sc)
+    rays = np.concatenate([camera_rays(sc), random_rays(3000, 1)])
+    f1, i1 = o.trace(rays)
+    f2, i2 = o.trace(rays, brute=True)
+    assert np.array_equal(i1, i2)
+    assert np.array_equal(f1, f2)
+    assert (i1[:, 0] != 0xFFFFFFFF).mean() > 0.3
+
+
+def test_traversal_two_level_matches_brute_force(orc):
+    sc = S.instanced_scene(width=64, height=36, counts=(6, 5, 3, 0, 4, 4, 1, 1), hf_n=24, ico_levels=(1, 2, 2, 3))
+    o = orc.OracleScene(sc)
+    rays = random_rays(3000, 2, lo=(-60, 0, -60), hi=(60, 14, 60))
+    f1, i1 = o.trace(rays)
+    f2, i2 = o.trace(rays, brute=True)
+    assert np.array_equal(i1, i2) and np.array_equal(f1, f2)
+    assert (i1[:, 0] != 0xFFFFFFFF).sum() > 50
+
+
+def test_half_rounding(orc):
+    x = np.concatenate([np.random.RandomState(0).randn(200000).astype(np.float32) * 30,
+                        np.array([65504, 65520, 65519.9, 1e-8, -1e-8, 6e-5, 6.1e-5, 2.98e-8, np.inf, -np.inf], np.float32)])
+    assert np.array_equal(orc.round_half(x), x.astype(np.float16).astype(np.float32))
+
+
+def test_render_small_scene_finite(orc):
+    sc = S.spheres_scene(n_spheres=8, width=48, height=27, slices=16, stacks=8)
+    o = orc.OracleScene(sc)
+    b, n, r, st = o.render(nthreads=2)
+    assert np.isfinite(b).all() and np.isfinite(n).all() and np.isfinite(r).all()
+    assert st["primary"] == 48 * 27
+    fin = orc.post(sc.ubo, b, n, r)
+    assert np.isfinite(fin).all() and (fin[..., :3] >= 0).all() and (fin[..., :3] <= 1).all()
+
+
+def test_render_fp64_close_to_fp32(orc):
+    sc = S.spheres_scene(n_spheres=8, width=48, height=27, slices=16, stacks=8)
+    o = orc.OracleScene(sc)
+    b32 = o.render(nthreads=2)[0]
+    b64 = o.render(nthreads=2, fp64=True)[0]
+    err = np.abs(b32[..., :3] - b64[..., :3])
+    assert np.quantile(err, 0.99) < 2 / 255
+
+
+def test_show_alpha_and_fade(orc):
+    sc = S.spheres_scene(n_spheres=4, width=32, height=18, slices=12, stacks=6)
+    o = orc.OracleScene(sc)
+    b, n, r, _ = o.render(nthreads=1)
+    u = sc.ubo.copy()
+    u["showAlpha"] = 1
+    fin = orc.post(u, b, n, r, fxaa=False)
+    assert np.allclose(fin[..., 0], fin[..., 3]) and np.allclose(fin[..., 1], fin[..., 3])
+    u = sc.ubo.copy()
+    u["fadeColor"] = (1.0, 0.0, 0.0, 1.0)
+    fin = orc.post(u, b, n, r, fxaa=False)
+    assert np.allclose(fin[..., :3], [1.0, 0.0, 0.0])
