@@ -1,0 +1,402 @@
+#!/usr/bin/env python
+"""Benchmark of the game-frame path on GB300.
+
+Workload (one step = one frame): 1920x1080 with 4x SSAA (8,294,400 camera rays), maximum
+recursion depth 5, two-level BVH of 1024 instances drawn from 8 seeded procedural meshes
+(~11.7M instanced / 377k unique triangles).  Every frame 10% of the instances move (TLAS rebuilt
+from scratch), each BLAS is refit with probability 0.05 after per-vertex jitter, then trace +
+shade, the roughness approximation, the postprocess composite and FXAA run into the RGBA32F
+framebuffer.
+
+metric = Mrays/s: every ray that traverses the BVH (camera, shadow, reflection, refraction) per
+second of the whole frame (TLAS build + refits + trace + post).
+  value: inputs already resident in HBM (per-frame instance arrays and jittered vertices are
+         device buffers), timed with CUDA events on the library's stream, L2 flushed (256 MiB
+         memset) between frames.
+  e2e:   the same frames through the C ABI with host buffers: per frame the instance array and the
+         refit vertices are copied from pinned host memory and the framebuffer is read back into
+         pinned host memory, all inside the timed region.
+
+--impl reference runs the reference arm: the reference's own GPU path needs a Vulkan ray-tracing
+driver (unavailable on this machine), so it times the CPU restatement of the same shaders (the oracle)
+on all host cores, each step the same frame sequence sampled on rows spread over the frame.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from raygun_gb300 import scenes as S  # noqa: E402
+
+WORKLOAD = "game-frame: {w}x{h}, 4x SSAA, depth 5, 1024 instances of 8 procedural meshes (~11.7M instanced tris), " \
+           "TLAS rebuilt + BLAS refit per frame, trace + roughness + composite + FXAA"
+BYTES_RAY = 32 + 20   # ray in (origin+tmin, dir+tmax) + hit out (t, u, v, prim, inst)
+BYTES_NODE = 64       # BVH2 node: two child boxes + two child refs
+BYTES_TRI = 36        # three vertex positions
+CPU_ROWS_PER_STEP = 27
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=54, help="rows of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--res", default="1920x1080", help="WxH; smaller sizes are for profiling captures only")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def trace_traffic():
+    """DRAM bytes of one trace-kernel launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_trace_c1.json")
+    try:
+        d = json.load(open(p))
+        return d.get("dram_bytes_per_launch"), d.get("source")
+    except (OSError, ValueError):
+        return None, None
+
+
+class FrameInputs:
+    """Per-frame inputs of the animated scene, precomputed so timed frames only move data."""
+
+    def __init__(self, scene, nframes, seed=101):
+        anim = S.FrameAnimator(scene, seed=seed)
+        self.instances = []
+        self.refits = []  # per frame: list of (blas, vertex_offset, nverts, vertex array)
+        for _ in range(nframes):
+            r = anim.step()
+            self.instances.append(scene.instances.copy())
+            self.refits.append([(b, vo, nv, scene.vertices[vo:vo + nv].copy()) for b, vo, nv in r])
+
+
+def run_ours(args):
+    import torch
+    from raygun_gb300 import build as rgbuild, rgcuda
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    rgbuild.build()
+    w, h = (int(x) for x in args.res.split("x"))
+    sc = S.instanced_scene(width=w, height=h)
+    orc_scene = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        orc_scene = oracle.OracleScene(sc)  # pristine frame-0 state, before any animation
+    rt = rgcuda.Raytracer(sc, device=local).prepare()
+    ctx = rt.ctx
+    K, W = args.steps, args.warmup
+    total = 2 * (W + K) + 1
+    frames = FrameInputs(sc, total)
+    dev = torch.device("cuda", local)
+    ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    ninst = len(sc.instances)
+    blas_ids = np.asarray(rt.blas_ids, np.uint32)
+
+    def inst_bytes(f):
+        inst = frames.instances[f].copy()
+        inst["blas"] = blas_ids[inst["blas"]]
+        return inst
+
+    # device-resident inputs for the `value` loop
+    inst_dev = torch.from_numpy(np.stack([inst_bytes(f).view(np.uint8) for f in range(total)])).to(dev)
+    vert_chunks, vert_offsets, off = [], {}, 0
+    for f in range(total):
+        for j, (b, vo, nv, arr) in enumerate(frames.refits[f]):
+            vert_chunks.append(arr.view(np.uint8).reshape(-1))
+            vert_offsets[(f, j)] = off
+            off += arr.nbytes
+    vert_dev = torch.from_numpy(np.concatenate(vert_chunks) if vert_chunks else np.zeros(16, np.uint8)).to(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ubo = sc.ubo
+    stride = ninst * S.INSTANCE.itemsize
+
+    def step_device(f):
+        for j, (b, vo, nv, _) in enumerate(frames.refits[f]):
+            ctx.update_vertices_device(vo, vert_dev.data_ptr() + vert_offsets[(f, j)], nv)
+            ctx.refit_blas(int(blas_ids[b]))
+        ctx.build_tlas_device(inst_dev.data_ptr() + f * stride, ninst)
+        ctx.render(ubo, True)
+        with torch.cuda.stream(ext):
+            flush.zero_()
+
+    # pinned host inputs / outputs for the e2e loop
+    inst_pin = torch.from_numpy(np.stack([inst_bytes(f).view(np.uint8) for f in range(total)])).pin_memory()
+    inst_host = inst_pin.numpy()
+    vert_pin = torch.from_numpy(np.concatenate(vert_chunks) if vert_chunks else np.zeros(16, np.uint8)).pin_memory()
+    vert_host = vert_pin.numpy()
+    fb_pin = torch.empty(sc.height * sc.width * 16, dtype=torch.uint8).pin_memory()
+
+    def step_host(f):
+        h2d = 0
+        for j, (b, vo, nv, _) in enumerate(frames.refits[f]):
+            o = vert_offsets[(f, j)]
+            ctx.update_vertices(vo, vert_host[o:o + nv * 32].view(S.VERTEX))
+            ctx.refit_blas(int(blas_ids[b]))
+            h2d += nv * 32
+        ctx.build_tlas(inst_host[f].view(S.INSTANCE))
+        ctx.render(ubo, True)
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        ctx.download_to(fb_pin.data_ptr())
+        return h2d + stride + S.UBO.itemsize
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        ctx.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    # ---------------- value: device-resident inputs ----------------
+    f = 0
+    for _ in range(W):
+        step_device(f)
+        f += 1
+    barrier()
+    ctx.timings()  # drop warm-up frames from the timing sums
+    ctx.reset_total_stats()
+    launches0 = rgcuda.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(ext)
+    for _ in range(K):
+        step_device(f)
+        f += 1
+    e1.record(ext)
+    barrier()
+    clk = clocks.stop()
+    launches = rgcuda.launch_count() - launches0
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    tot = ctx.total_stats()
+    rays = tot["primary"] + tot["shadow"] + tot["secondary"]
+    tm = ctx.timings()
+    all_rays = sum_over_ranks(rays)
+    value = all_rays / (ms * 1e-3) / 1e6
+
+    # ---------------- e2e: host buffers through the C ABI ----------------
+    for _ in range(W):
+        step_host(f)
+        f += 1
+    barrier()
+    ctx.reset_total_stats()
+    h2d = 0
+    barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(ext)
+    for _ in range(K):
+        h2d += step_host(f)
+        f += 1
+    e3.record(ext)
+    barrier()
+    ms_e2e = max_over_ranks(e2.elapsed_time(e3))
+    tot2 = ctx.total_stats()
+    rays2 = sum_over_ranks(tot2["primary"] + tot2["shadow"] + tot2["secondary"])
+    e2e = {"value": rays2 / (ms_e2e * 1e-3) / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d // K),
+           "d2h_bytes_per_step": sc.height * sc.width * 16, "ms_per_step": ms_e2e / K}
+
+    # ---------------- roofline of the trace kernel ----------------
+    ctx.set_flags(rgcuda.RG_FLAG_COUNT_VISITS)
+    ctx.timings()
+    step_device(f)
+    barrier()
+    cst = ctx.stats()
+    ctx.set_flags(0)
+    crays = cst["primary"] + cst["shadow"] + cst["secondary"]
+    bytes_per_ray = (crays * BYTES_RAY + cst["nodes"] * BYTES_NODE + cst["tris"] * BYTES_TRI) / max(crays, 1)
+    trace_ms = tm["rtOnlySum"] / max(tm["frames"], 1)
+    bytes_launch = bytes_per_ray * rays / K
+    achieved = bytes_launch / (trace_ms * 1e-3) / 1e9
+    peak, peak_src = measured_peak_hbm()
+    traffic, traffic_src = trace_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "k_trace", "peak_source": f"{peak_src} hbm_gbs",
+                "algorithmic_bytes_per_launch": bytes_launch, "bytes_per_ray": bytes_per_ray,
+                "node_visits_per_ray": cst["nodes"] / max(crays, 1), "tri_tests_per_ray": cst["tris"] / max(crays, 1),
+                "trace_ms_per_launch": trace_ms, "traffic_source": traffic_src}
+
+    out = {
+        "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded procedural scene (no dataset)",
+        "config": {"workload": WORKLOAD.format(w=sc.width, h=sc.height), "width": sc.width, "height": sc.height, "spp": int(sc.ubo["numSamples"][0]),
+                   "max_recursions": int(sc.ubo["maxRecursions"][0]), "instances": ninst,
+                   "instanced_tris": sc.instanced_tri_count, "unique_tris": sc.tri_count,
+                   "l2": "flushed between frames (256 MiB memset on the library stream)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "frames_per_s": K / (ms * 1e-3),
+        "rays_per_frame": rays / K,
+        "profiler_ranges_ms": {k: tm[k + "Sum"] / max(tm["frames"], 1) for k in
+                               ("asBuild", "refit", "rtOnly", "rough", "postproc", "rtTotal")},
+        "e2e": e2e, "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
+    }
+    if orc_scene is not None:
+        out["cpu_baseline"] = cpu_baseline(orc_scene, sc, args.cpu_rows)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline(orc_scene, sc, rows):
+    """The oracle on all host cores over `rows` rows spread evenly over frame 0."""
+    nthreads = os.cpu_count() or 1
+    step = max(1, sc.height // rows)
+    t = time.perf_counter()
+    _, _, _, st = orc_scene.render(rows=(0, sc.height), row_step=step, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    rays = st["primary"] + st["shadow"] + st["secondary"]
+    n = (sc.height + step - 1) // step
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "sample": f"every {step}th row of frame 0 ({n} rows x {sc.width} px, {int(sc.ubo['numSamples'][0])} spp): "
+                      f"{rays} rays in {dt:.2f} s (trace + shade)"}
+
+
+def run_reference(args):
+    """Reference arm: the CPU restatement of the reference shaders on all host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    sc = S.c1_scene()
+    o = oracle.OracleScene(sc)
+    nthreads = os.cpu_count() or 1
+    K, W = args.steps, args.warmup
+    frames = FrameInputs(sc, W + K)
+    rows = CPU_ROWS_PER_STEP
+
+    def step(f):
+        for b, vo, nv, arr in frames.refits[f]:
+            o.refit(b, arr, vo)
+        o.set_instances(frames.instances[f])
+        step_rows = sc.height // rows
+        _, _, _, st = o.render(rows=(f % step_rows, sc.height), row_step=step_rows, nthreads=nthreads)
+        return st["primary"] + st["shadow"] + st["secondary"]
+
+    for f in range(W):
+        step(f)
+    t = time.perf_counter()
+    rays = sum(step(W + k) for k in range(K))
+    dt = time.perf_counter() - t
+    v = rays / dt / 1e6
+    out = {"metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": world, "steps": K, "warmup": W,
+           "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic: seeded procedural scene (no dataset)", "impl": "reference",
+           "config": {"workload": WORKLOAD.format(w=sc.width, h=sc.height), "width": sc.width, "height": sc.height, "spp": int(sc.ubo["numSamples"][0]),
+                      "max_recursions": int(sc.ubo["maxRecursions"][0]), "instances": len(sc.instances)},
+           "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+                            "sample": f"per step: BLAS refits + TLAS rebuild of that frame, then {rows} rows spread over the frame "
+                                      f"x {sc.width} px at {int(sc.ubo['numSamples'][0])} spp (trace + shade); the "
+                                      f"reference's Vulkan RT path needs a ray-tracing driver, unavailable on this box"},
+           "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

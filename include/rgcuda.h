@@ -91,14 +91,18 @@ typedef struct {
     uint32_t pad;
 } rg_instance;
 
-/* GPU time of the profiler ranges of raygun/profiler.def:6-10, milliseconds of the last frame. */
+/* GPU time of the profiler ranges of raygun/profiler.def:6-10 in milliseconds: the last frame,
+ * and sums over every frame since the previous rg_get_timings call (raygun/profiler.cpp keeps
+ * 500-frame rolling statistics of the same ranges). */
 typedef struct {
     float asBuild;   /* TLAS build (raytracer.cpp:78,84) */
     float rtTotal;   /* trace + post (raytracer.cpp:93,144) */
     float rtOnly;    /* trace (raytracer.cpp:95,104) */
     float postproc;  /* roughness + composite + FXAA (raytracer.cpp:106,142) */
     float rough;     /* roughness approximation (raytracer.cpp:111,123) */
-    float refit;     /* BLAS refits issued since the previous frame (not in the reference) */
+    float refit;     /* BLAS refits issued before the frame (not in the reference) */
+    uint32_t frames; /* frames in the sums below */
+    float asBuildSum, rtTotalSum, rtOnlySum, postprocSum, roughSum, refitSum;
 } rg_timings;
 
 /* Ray statistics of the last frame. */
@@ -140,6 +144,8 @@ rg_status rg_upload_geometry(rg_ctx* ctx, const rg_vertex* vertices, uint32_t nv
  * gpu/gpu_material.cpp:52-94). */
 rg_status rg_update_vertices(rg_ctx* ctx, uint32_t first, const rg_vertex* vertices, uint32_t n);
 rg_status rg_update_materials(rg_ctx* ctx, uint32_t first, const rg_material* materials, uint32_t n);
+/* Same as rg_update_vertices from vertices already in device memory (device pointer). */
+rg_status rg_update_vertices_device(rg_ctx* ctx, uint32_t first, const rg_vertex* d_vertices, uint32_t n);
 
 /* Replaces BottomLevelAS::BottomLevelAS (render/acceleration_structure.cpp:140-194) as driven by
  * Raytracer::setupBottomLevelAS (render/raytracer.cpp:54-74): triangles
@@ -176,6 +182,13 @@ rg_status rg_synchronize(rg_ctx* ctx);
 /* Replaces Profiler (raygun/profiler.cpp:55-105): GPU ranges of the last frame. */
 rg_status rg_get_timings(rg_ctx* ctx, rg_timings* out);
 rg_status rg_get_stats(rg_ctx* ctx, rg_stats* out);
+/* Ray statistics summed over every frame since the context was created or last reset. */
+rg_status rg_get_total_stats(rg_ctx* ctx, rg_stats* out);
+rg_status rg_reset_total_stats(rg_ctx* ctx);
+/* Replace the RG_FLAG_* set of rg_device_opts (debug images, visit counting). */
+rg_status rg_set_flags(rg_ctx* ctx, uint32_t flags);
+/* Number of kernels this library has launched in this process. */
+rg_status rg_launch_count(uint64_t* out);
 /* The CUDA stream the context orders its work on (cudaStream_t). */
 rg_status rg_get_stream(rg_ctx* ctx, void** stream);
 

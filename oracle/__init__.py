@@ -48,7 +48,7 @@ def lib():
         L.orc_instance_inverse.restype = I
         L.orc_trace.argtypes = [P, P, U32, P, P, I, I]
         L.orc_trace.restype = I
-        L.orc_render.argtypes = [P, P, U32, U32, U32, U32, P, P, P, P, I, I]
+        L.orc_render.argtypes = [P, P, U32, U32, U32, U32, U32, P, P, P, P, I, I]
         L.orc_render.restype = I
         L.orc_post.argtypes = [P, U32, U32, P, P, P, P, P, I]
         L.orc_post.restype = I
@@ -122,16 +122,16 @@ class OracleScene:
         lib().orc_trace(self.h, _p(rays), n, _p(hf), _p(hi), 1 if brute else 0, nthreads or os.cpu_count())
         return hf, hi
 
-    def render(self, ubo=None, rows=None, nthreads=None, fp64=False):
+    def render(self, ubo=None, rows=None, nthreads=None, fp64=False, row_step=1):
         """-> (base, normal, rough) float32 (H, W, 4) images and stats dict; rows=(r0, r1) limits
-        the raygen to a band of rows (others stay zero)."""
+        the raygen to rows r0, r0+row_step, ... < r1 (others stay zero)."""
         s = self.scene
         ubo = np.ascontiguousarray(s.ubo if ubo is None else ubo)
         W, H = s.width, s.height
         r0, r1 = rows if rows else (0, H)
         imgs = [np.zeros((H, W, 4), np.float32) for _ in range(3)]
         st = np.zeros(6, np.uint64)
-        lib().orc_render(self.h, _p(ubo), W, H, r0, r1, _p(imgs[0]), _p(imgs[1]), _p(imgs[2]), _p(st),
+        lib().orc_render(self.h, _p(ubo), W, H, r0, r1, row_step, _p(imgs[0]), _p(imgs[1]), _p(imgs[2]), _p(st),
                          nthreads or os.cpu_count(), 1 if fp64 else 0)
         keys = ("primary", "shadow", "secondary", "masked", "nodes", "tris")
         return imgs[0], imgs[1], imgs[2], {k: int(v) for k, v in zip(keys, st)}

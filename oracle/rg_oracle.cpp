@@ -3,6 +3,9 @@
 // TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the smoke check and the
 // CPU-baseline leg of the benchmark call it; nothing in the product links or calls it.
 //
+// Parity unpinned: the reference has no tests, golden vectors or fixtures for this path, and its
+// own GPU path needs a Vulkan ray-tracing driver, so this restatement follows the shader source.
+//
 // It is a scalar C++ restatement of the reference's per-frame path:
 //   * LBVH over triangle / instance boxes (30-bit Morton, stable sort, Karras 2012 hierarchy,
 //     bottom-up boxes).  The reference leaves BVHs to the Vulkan driver
@@ -1284,16 +1287,19 @@ int orc_trace(orc_scene* sc, const float* rays, uint32_t n, float* hit_f, uint32
     return 0;
 }
 
-// raygen for rows [row0, row1): writes base/normal/rough images (W*H*4 floats each, FP16-rounded
-// values).  stats (6 x u64): primary, shadow, secondary, masked-miss traces, nodes, triangles.
-int orc_render(orc_scene* sc, const void* ubo, uint32_t W, uint32_t H, uint32_t row0, uint32_t row1, float* base, float* normal,
-               float* rough, uint64_t* stats, int nthreads, int fp64) {
+// raygen for rows row0, row0+row_step, ... < row1: writes base/normal/rough images (W*H*4 floats
+// each, FP16-rounded values).  stats (6 x u64): primary, shadow, secondary, masked-miss traces, nodes, triangles.
+int orc_render(orc_scene* sc, const void* ubo, uint32_t W, uint32_t H, uint32_t row0, uint32_t row1, uint32_t row_step, float* base,
+               float* normal, float* rough, uint64_t* stats, int nthreads, int fp64) {
     const Scene* s = (const Scene*)sc;
     const Ubo& u = *(const Ubo*)ubo;
     if (row1 > H) row1 = H;
+    if (row_step < 1) row_step = 1;
     int nt = nthreads < 1 ? 1 : nthreads;
     std::vector<Counters> cs(nt);
-    parallel_rows(row0, row1, nt, [&](uint32_t y, int t) {
+    uint32_t nrows = row1 > row0 ? (row1 - row0 + row_step - 1) / row_step : 0;
+    parallel_rows(0, nrows, nt, [&](uint32_t k, int t) {
+        uint32_t y = row0 + k * row_step;
         for (uint32_t x = 0; x < W; ++x) {
             float o[12];
             if (fp64) raygen_pixel<double>(*s, u, x, y, W, H, o, cs[t]);

@@ -33,7 +33,18 @@ struct BlasRec {
     DevBuf tris;
 };
 
+// CUDA events of one frame's profiler ranges (raygun/profiler.def:6-10)
+enum { EV_AS0, EV_AS1, EV_REFIT0, EV_REFIT1, EV_RT0, EV_POST0, EV_ROUGH1, EV_POST1, EV_COUNT };
+struct FrameEvents {
+    cudaEvent_t ev[EV_COUNT] = {};
+    bool hasAs = false, hasRefit = false, hasFrame = false;
+};
+
 }  // namespace
+
+namespace rg {
+std::atomic<uint64_t> g_launches{0};
+}
 
 struct rg_ctx {
     int device = 0;
@@ -58,9 +69,10 @@ struct rg_ctx {
     DevBuf base, normal, rough, finalImg, fxaaOut, fb, dbgT, dbgA, dbgB;
     bool lastFxaa = true;
     // misc
-    DevBuf counters, tmpA, tmpB, tmpC, tmpD;
-    cudaEvent_t ev[8] = {};
-    bool refitPending = false;
+    DevBuf counters, tmpA, tmpB, tmpC, tmpD;  // counters: 8 per-frame + 8 cumulative
+    std::vector<FrameEvents*> evPool, evPending;
+    FrameEvents* evCur = nullptr;  // ranges recorded since the last frame
+    rg_timings lastTimings{};
     bool haveFrame = false;
 };
 
@@ -185,6 +197,29 @@ rg_status set_device(rg_ctx* c) {
     return RG_OK;
 }
 
+// event set collecting the ranges of the frame being assembled
+rg_status cur_events(rg_ctx* c, FrameEvents** out) {
+    if (!c->evCur) {
+        if (!c->evPool.empty()) {
+            c->evCur = c->evPool.back();
+            c->evPool.pop_back();
+        } else {
+            FrameEvents* f = new FrameEvents();
+            for (auto& e : f->ev) {
+                cudaError_t r = cudaEventCreate(&e);
+                if (r != cudaSuccess) {
+                    delete f;
+                    CK(r);
+                }
+            }
+            c->evCur = f;
+        }
+        c->evCur->hasAs = c->evCur->hasRefit = c->evCur->hasFrame = false;
+    }
+    *out = c->evCur;
+    return RG_OK;
+}
+
 DevScene scene_of(rg_ctx* c) {
     DevScene s;
     s.blas = c->blasTable.as<DevBlas>();
@@ -205,11 +240,14 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
     c->tlasReady = false;
     TRY(ensure(c, c->instDev, sizeof(DevInstance) * (size_t)(n ? n : 1)));
     TRY(ensure_bvh(c, c->tlas, n));
-    CK(cudaEventRecord(c->ev[0], c->stream));
+    FrameEvents* fe;
+    TRY(cur_events(c, &fe));
+    CK(cudaEventRecord(fe->ev[EV_AS0], c->stream));
     CK(setup_instances(c->instIn.as<rg_instance>(), n, c->blasTable.as<DevBlas>(), (uint32_t)c->blas.size(),
                        c->instDev.as<DevInstance>(), c->tlas.primBoxes.as<float>(), c->stream));
     CK(lbvh_build(buffers(c, c->tlas), c->stream));
-    CK(cudaEventRecord(c->ev[1], c->stream));
+    CK(cudaEventRecord(fe->ev[EV_AS1], c->stream));
+    fe->hasAs = true;
     c->tlasReady = true;
     return RG_OK;
 }
@@ -237,16 +275,11 @@ rg_status rg_create(rg_ctx** out, const rg_device_opts* opts) {
         delete c;
         return RG_ERR_CUDA;
     }
-    for (auto& e : c->ev)
-        if (cudaEventCreate(&e) != cudaSuccess) {
-            delete c;
-            return RG_ERR_CUDA;
-        }
-    if (ensure(c, c->counters, 8 * sizeof(unsigned long long)) != RG_OK) {
+    if (ensure(c, c->counters, 16 * sizeof(unsigned long long)) != RG_OK) {
         delete c;
         return RG_ERR_OUT_OF_MEMORY;
     }
-    cudaMemsetAsync(c->counters.p, 0, 64, c->stream);
+    cudaMemsetAsync(c->counters.p, 0, 128, c->stream);
     *out = c;
     return RG_OK;
 }
@@ -268,8 +301,14 @@ rg_status rg_destroy(rg_ctx* c) {
         relBvh(r.bvh);
         release(c, r.tris);
     }
-    for (auto& e : c->ev)
-        if (e) cudaEventDestroy(e);
+    std::vector<FrameEvents*> all = c->evPool;
+    all.insert(all.end(), c->evPending.begin(), c->evPending.end());
+    if (c->evCur) all.push_back(c->evCur);
+    for (FrameEvents* f : all) {
+        for (auto& e : f->ev)
+            if (e) cudaEventDestroy(e);
+        delete f;
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return RG_OK;
@@ -303,6 +342,13 @@ rg_status rg_update_vertices(rg_ctx* c, uint32_t first, const rg_vertex* v, uint
     if (!c || (n && !v) || (uint64_t)first + n > c->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
     TRY(set_device(c));
     if (n) CK(cudaMemcpyAsync(c->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    return RG_OK;
+}
+
+rg_status rg_update_vertices_device(rg_ctx* c, uint32_t first, const rg_vertex* v, uint32_t n) {
+    if (!c || (n && !v) || (uint64_t)first + n > c->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
+    TRY(set_device(c));
+    if (n) CK(cudaMemcpyAsync(c->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
     return RG_OK;
 }
 
@@ -356,14 +402,16 @@ rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
     BlasRec& r = c->blas[b];
     uint32_t n = r.bvh.n;
     if (!n) return RG_OK;
-    if (!c->refitPending) CK(cudaEventRecord(c->ev[6], c->stream));
+    FrameEvents* fe;
+    TRY(cur_events(c, &fe));
+    if (!fe->hasRefit) CK(cudaEventRecord(fe->ev[EV_REFIT0], c->stream));
     CK(tri_boxes(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, n, r.bvh.primBoxes.as<float>(), c->stream));
     CK(lbvh_refit(buffers(c, r.bvh), c->stream));
     CK(tri_records(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, r.bvh.order.as<uint32_t>(), n,
                    r.tris.as<float4>(), c->stream));
     CK(cudaMemcpyAsync(c->blasTable.as<DevBlas>()[b].root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
-    CK(cudaEventRecord(c->ev[7], c->stream));
-    c->refitPending = true;
+    CK(cudaEventRecord(fe->ev[EV_REFIT1], c->stream));
+    fe->hasRefit = true;
     return RG_OK;
 }
 
@@ -423,11 +471,16 @@ static rg_status run_post(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     for (int k = 0; k < 4; ++k) pp.fade[k] = ubo->fadeColor[k];
     pp.showAlpha = ubo->showAlpha ? 1 : 0;
     pp.fxaa = fxaa ? 1 : 0;
-    CK(cudaEventRecord(c->ev[3], c->stream));
+    FrameEvents* fe;
+    TRY(cur_events(c, &fe));
+    CK(cudaEventRecord(fe->ev[EV_POST0], c->stream));
     CK(launch_rough_post(pp, c->stream));
-    CK(cudaEventRecord(c->ev[4], c->stream));
+    CK(cudaEventRecord(fe->ev[EV_ROUGH1], c->stream));
     CK(launch_fxaa(pp, c->stream));
-    CK(cudaEventRecord(c->ev[5], c->stream));
+    CK(cudaEventRecord(fe->ev[EV_POST1], c->stream));
+    fe->hasFrame = true;
+    c->evPending.push_back(fe);
+    c->evCur = nullptr;
     c->lastFxaa = fxaa != 0;
     c->haveFrame = true;
     return RG_OK;
@@ -458,7 +511,9 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     tp.counters = c->counters.as<unsigned long long>();
     tp.countVisits = (c->flags & RG_FLAG_COUNT_VISITS) ? 1 : 0;
     CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
-    CK(cudaEventRecord(c->ev[2], c->stream));
+    FrameEvents* fe;
+    TRY(cur_events(c, &fe));
+    CK(cudaEventRecord(fe->ev[EV_RT0], c->stream));
     CK(launch_trace(tp, c->stream));
     return run_post(c, ubo, fxaa);
 }
@@ -476,7 +531,9 @@ rg_status rg_post_only(rg_ctx* c, const rg_ubo* ubo, const float* base, const fl
         CK(cudaMemcpyAsync(c->tmpA.p, src[k], 16 * px, cudaMemcpyHostToDevice, c->stream));
         CK(f32_to_h16(c->tmpA.as<float4>(), dst[k]->as<uint2>(), px, c->stream));
     }
-    CK(cudaEventRecord(c->ev[2], c->stream));
+    FrameEvents* fe;
+    TRY(cur_events(c, &fe));
+    CK(cudaEventRecord(fe->ev[EV_RT0], c->stream));
     return run_post(c, ubo, fxaa);
 }
 
@@ -538,43 +595,74 @@ rg_status rg_get_timings(rg_ctx* c, rg_timings* t) {
     if (!c || !t) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
     CK(cudaStreamSynchronize(c->stream));
-    std::memset(t, 0, sizeof(*t));
-    auto el = [&](int a, int b) {
+    auto el = [&](cudaEvent_t a, cudaEvent_t b) {
         float ms = 0.0f;
-        if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) {
+        if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
             cudaGetLastError();
             ms = 0.0f;
         }
         return ms;
     };
-    if (c->tlasReady) t->asBuild = el(0, 1);
-    if (c->haveFrame) {
-        t->rtOnly = el(2, 3);
-        t->rough = el(3, 4);
-        t->postproc = el(3, 5);
-        t->rtTotal = el(2, 5);
+    rg_timings r = c->lastTimings;
+    r.frames = 0;
+    r.asBuildSum = r.rtTotalSum = r.rtOnlySum = r.postprocSum = r.roughSum = r.refitSum = 0.0f;
+    for (FrameEvents* f : c->evPending) {
+        float as = f->hasAs ? el(f->ev[EV_AS0], f->ev[EV_AS1]) : 0.0f;
+        float rf = f->hasRefit ? el(f->ev[EV_REFIT0], f->ev[EV_REFIT1]) : 0.0f;
+        float rt = el(f->ev[EV_RT0], f->ev[EV_POST0]);
+        float ro = el(f->ev[EV_POST0], f->ev[EV_ROUGH1]);
+        float po = el(f->ev[EV_POST0], f->ev[EV_POST1]);
+        r.asBuild = as; r.refit = rf; r.rtOnly = rt; r.rough = ro; r.postproc = po; r.rtTotal = rt + po;
+        r.asBuildSum += as; r.refitSum += rf; r.rtOnlySum += rt; r.roughSum += ro; r.postprocSum += po; r.rtTotalSum += rt + po;
+        r.frames++;
+        c->evPool.push_back(f);
     }
-    if (c->refitPending) {
-        t->refit = el(6, 7);
-        c->refitPending = false;
-    }
+    c->evPending.clear();
+    c->lastTimings = r;
+    *t = r;
     return RG_OK;
 }
 
-rg_status rg_get_stats(rg_ctx* c, rg_stats* s) {
+static rg_status read_stats(rg_ctx* c, rg_stats* s, int base);
+rg_status rg_get_stats(rg_ctx* c, rg_stats* s) { return read_stats(c, s, 0); }
+
+static rg_status read_stats(rg_ctx* c, rg_stats* s, int base) {
     if (!c || !s) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
-    unsigned long long v[8];
-    CK(cudaMemcpyAsync(v, c->counters.p, 64, cudaMemcpyDeviceToHost, c->stream));
+    unsigned long long v[16];
+    CK(cudaMemcpyAsync(v, c->counters.p, 128, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    s->primary = v[0];
-    s->shadow = v[1];
-    s->secondary = v[2];
-    s->masked = v[3];
-    s->nodes = v[4];
-    s->tris = v[5];
-    s->stack_overflows = v[6];
+    s->primary = v[base + 0];
+    s->shadow = v[base + 1];
+    s->secondary = v[base + 2];
+    s->masked = v[base + 3];
+    s->nodes = v[base + 4];
+    s->tris = v[base + 5];
+    s->stack_overflows = v[base + 6];
     s->pad = 0;
+    return RG_OK;
+}
+
+rg_status rg_get_total_stats(rg_ctx* c, rg_stats* s) { return read_stats(c, s, 8); }
+
+rg_status rg_reset_total_stats(rg_ctx* c) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    CK(cudaMemsetAsync(c->counters.as<unsigned long long>() + 8, 0, 64, c->stream));
+    return RG_OK;
+}
+
+rg_status rg_set_flags(rg_ctx* c, uint32_t flags) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    TRY(set_device(c));
+    c->flags = flags;
+    if ((flags & RG_FLAG_DEBUG_IMAGES) && c->W) TRY(rg_set_resolution(c, c->W, c->H));
+    return RG_OK;
+}
+
+rg_status rg_launch_count(uint64_t* out) {
+    if (!out) return RG_ERR_INVALID_ARG;
+    *out = rg::g_launches.load();
     return RG_OK;
 }
 

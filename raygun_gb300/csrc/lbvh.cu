@@ -326,6 +326,7 @@ size_t sort_block_count(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
 cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_tri_boxes<<<blocks(n, 256), 256, 0, s>>>(v, idx, vOff, iOff, n, boxes);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -333,6 +334,7 @@ cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, 
                         float4* tris, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_tri_records<<<blocks(n, 256), 256, 0, s>>>(v, idx, vOff, iOff, order, n, tris);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -340,6 +342,7 @@ cudaError_t setup_instances(const rg_instance* in, uint32_t n, const DevBlas* bl
                             cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_instances<<<blocks(n, 128), 128, 0, s>>>(in, n, blas, nblas, out, boxes);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -348,6 +351,7 @@ cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b.flags, 0, sizeof(uint32_t) * (b.n - 1), s);
     if (e != cudaSuccess) return e;
     k_bottom_up<<<blocks(b.n, 256), 256, 0, s>>>(b.primBoxes, b.order, b.n, b.left, b.right, b.parents, b.flags, b.nodeBoxes, b.nodes);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -358,6 +362,7 @@ cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s) {
     uint32_t gb = min(blocks(n, 256), 1024u);
     k_centroid_bounds<<<gb, 256, 0, s>>>(b.primBoxes, n, b.bounds);
     k_morton<<<blocks(n, 256), 256, 0, s>>>(b.primBoxes, n, b.bounds, b.morton, b.keysA, b.valsA);
+    count_launch(3);
     const uint32_t nb = (uint32_t)sort_block_count(n);
     uint32_t *kin = b.keysA, *vin = b.valsA, *kout = b.keysB, *vout = b.valsB;
     for (int pass = 0; pass < 4; ++pass) {
@@ -365,6 +370,7 @@ cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s) {
         k_sort_hist<<<nb, kSortThreads, 0, s>>>(kin, n, shift, b.blockHist, nb);
         k_sort_scan<<<1, 1024, 0, s>>>(b.blockHist, 256u * nb);
         k_sort_scatter<<<nb, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, b.blockHist, nb);
+        count_launch(3);
         uint32_t* t = kin; kin = kout; kout = t;
         t = vin; vin = vout; vout = t;
     }
@@ -373,6 +379,7 @@ cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     if (n == 1) return cudaGetLastError();
     k_karras<<<blocks(n - 1, 256), 256, 0, s>>>(kin, n, b.left, b.right, b.parents);
+    count_launch();
     return lbvh_refit(b, s);
 }
 

@@ -355,16 +355,19 @@ __global__ void k_r32_to_rgba(const float* __restrict__ in, float4* __restrict__
 cudaError_t f32_to_h16(const float4* in, uint2* out, size_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_f32_to_h16<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, n);
+    count_launch();
     return cudaGetLastError();
 }
 cudaError_t h16_to_f32(const uint2* in, float4* out, size_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_h16_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, n);
+    count_launch();
     return cudaGetLastError();
 }
 cudaError_t r32_to_rgba(const float* in, float4* out, size_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_r32_to_rgba<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, n);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -378,17 +381,20 @@ cudaError_t launch_rough_post(const PostParams& p, cudaStream_t s) {
     }
     dim3 grid((p.W + TW - 1) / TW, (p.H + TH - 1) / TH);
     k_rough_post<<<grid, kPostThreads, smem, s>>>(p);
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !p.showAlpha) return e;
     size_t n = (size_t)p.W * p.H;
     k_show_alpha<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(const_cast<uint2*>(p.base), const_cast<uint2*>(p.normal),
                                                             const_cast<uint2*>(p.rough), n);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_fxaa(const PostParams& p, cudaStream_t s) {
     dim3 grid((p.W + 15) / 16, (p.H + 15) / 16);
     k_fxaa<<<grid, 256, 0, s>>>(p);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/rgcuda.h"
 
 namespace rg {
@@ -93,6 +95,10 @@ __host__ __device__ inline float3 f3(float x, float y, float z) { return make_fl
 
 // internal launchers implemented in the .cu files
 namespace rg {
+
+// kernels launched by this library in this process (rg_launch_count)
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 struct LbvhBuffers {  // scratch + outputs of one LBVH build, sized by the caller (n primitives)
     uint32_t n;

@@ -661,11 +661,17 @@ __global__ void __launch_bounds__(128) k_trace(const TraceParams P) {
     if (mask == 0xFFFFFFFFu) {
         if ((threadIdx.x & 31) == 0)
             for (int k = 0; k < 7; ++k)
-                if (c[k]) atomicAdd(P.counters + k, c[k]);
+                if (c[k]) {
+                    atomicAdd(P.counters + k, c[k]);
+                    atomicAdd(P.counters + 8 + k, c[k]);
+                }
     } else {
         unsigned long long own[7] = {nPrimary, nShadow, nSecondary, nMasked, vc.nodes, vc.tris, vc.overflow};
         for (int k = 0; k < 7; ++k)
-            if (own[k]) atomicAdd(P.counters + k, own[k]);
+            if (own[k]) {
+                atomicAdd(P.counters + k, own[k]);
+                atomicAdd(P.counters + 8 + k, own[k]);
+            }
     }
 }
 
@@ -690,12 +696,14 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t s) {
     dim3 grid((p.W + 15) / 16, (p.H + 7) / 8);
     if (p.countVisits) k_trace<true><<<grid, 128, 0, s>>>(p);
     else k_trace<false><<<grid, 128, 0, s>>>(p);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_trace_rays<<<(n + 127) / 128, 128, 0, s>>>(sc, rays, n, tuv, ids);
+    count_launch();
     return cudaGetLastError();
 }
 

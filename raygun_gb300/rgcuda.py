@@ -29,6 +29,7 @@ EXPORTS = [
     "rg_build_blas", "rg_refit_blas", "rg_build_tlas", "rg_build_tlas_device", "rg_set_resolution", "rg_render",
     "rg_download", "rg_framebuffer_device", "rg_download_image", "rg_synchronize", "rg_get_timings", "rg_get_stats",
     "rg_get_stream", "rg_bvh_info", "rg_instance_inverse", "rg_trace_rays", "rg_post_only", "rg_lbvh_build_host",
+    "rg_update_vertices_device", "rg_get_total_stats", "rg_reset_total_stats", "rg_set_flags", "rg_launch_count",
 ]
 
 
@@ -37,7 +38,10 @@ class DeviceOpts(ctypes.Structure):
 
 
 class Timings(ctypes.Structure):
-    _fields_ = [(k, ctypes.c_float) for k in ("asBuild", "rtTotal", "rtOnly", "postproc", "rough", "refit")]
+    _fields_ = ([(k, ctypes.c_float) for k in ("asBuild", "rtTotal", "rtOnly", "postproc", "rough", "refit")]
+                + [("frames", ctypes.c_uint32)]
+                + [(k, ctypes.c_float) for k in ("asBuildSum", "rtTotalSum", "rtOnlySum", "postprocSum", "roughSum",
+                                                 "refitSum")])
 
 
 class Stats(ctypes.Structure):
@@ -88,6 +92,11 @@ def load(path: str = LIB_PATH):
         "rg_trace_rays": ([P, P, U32, P, P], I32),
         "rg_post_only": ([P, P, P, P, P, I32], I32),
         "rg_lbvh_build_host": ([P, P, U32, P, P, P, P, P], I32),
+        "rg_update_vertices_device": ([P, U32, P, U32], I32),
+        "rg_get_total_stats": ([P, ctypes.POINTER(Stats)], I32),
+        "rg_reset_total_stats": ([P], I32),
+        "rg_set_flags": ([P, U32], I32),
+        "rg_launch_count": ([ctypes.POINTER(ctypes.c_uint64)], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -95,6 +104,15 @@ def load(path: str = LIB_PATH):
         f.restype = res
     _lib = L
     return L
+
+
+def launch_count() -> int:
+    """Kernels the library launched in this process."""
+    v = ctypes.c_uint64()
+    rc = load().rg_launch_count(ctypes.byref(v))
+    if rc != RG_OK:
+        raise RgError(rc, "rg_launch_count")
+    return v.value
 
 
 def _p(a):
@@ -139,6 +157,9 @@ class Context:
     def update_vertices(self, first, vertices):
         v = np.ascontiguousarray(vertices, dtype=scenes.VERTEX)
         self._ck(self.L.rg_update_vertices(self.h, first, _p(v), len(v)))
+
+    def update_vertices_device(self, first, dev_ptr: int, n: int):
+        self._ck(self.L.rg_update_vertices_device(self.h, first, ctypes.c_void_p(dev_ptr), n))
 
     def update_materials(self, first, materials):
         m = np.ascontiguousarray(materials, dtype=scenes.MATERIAL)
@@ -200,6 +221,17 @@ class Context:
         s = Stats()
         self._ck(self.L.rg_get_stats(self.h, ctypes.byref(s)))
         return {k: int(getattr(s, k)) for k, _ in Stats._fields_ if k != "pad"}
+
+    def total_stats(self) -> dict:
+        s = Stats()
+        self._ck(self.L.rg_get_total_stats(self.h, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in Stats._fields_ if k != "pad"}
+
+    def reset_total_stats(self):
+        self._ck(self.L.rg_reset_total_stats(self.h))
+
+    def set_flags(self, flags):
+        self._ck(self.L.rg_set_flags(self.h, flags))
 
     def stream(self) -> int:
         p = ctypes.c_void_p()
