@@ -27,7 +27,8 @@ enum {
     RG_ERR_NOT_READY = -4,     /* e.g. render before geometry/TLAS */
     RG_ERR_STACK_OVERFLOW = -5,
     RG_ERR_BUDGET = -6,        /* HBM budget of rg_device_opts exceeded */
-    RG_ERR_NO_DEVICE = -7
+    RG_ERR_NO_DEVICE = -7,
+    RG_ERR_TOO_LARGE = -8      /* input beyond a fixed-size entry point's stated maximum */
 };
 
 typedef struct rg_ctx rg_ctx;
@@ -212,6 +213,21 @@ rg_status rg_post_only(rg_ctx* ctx, const rg_ubo* ubo, const float* base, const 
 /* Raw LBVH build over host boxes (n x 6 floats), for the builder's parity tests. */
 rg_status rg_lbvh_build_host(rg_ctx* ctx, const float* boxes, uint32_t n, uint32_t* morton, uint32_t* order,
                              uint32_t* left, uint32_t* right, float* nodeboxes);
+
+/* LBVH build that allocates nothing (no counterpart in the reference).  For callers that must not
+ * allocate device memory after start-up -- an engine that owns a fixed memory arena, or a frame
+ * loop that cannot afford the device synchronisation a cudaMalloc may cause.  Same results as
+ * rg_lbvh_build_host, but every pointer is a caller-owned DEVICE buffer (d_boxes: n x 6 floats;
+ * d_morton, d_order: n; d_left, d_right: n-1; d_nodeboxes: (n-1) x 6 floats) and the work is queued
+ * on `stream` (a cudaStream_t, NULL = legacy default stream) without waiting for it.  Scratch memory
+ * is one fixed file-scope device array (about 6 MiB) that each GPU loading this library holds until
+ * exit.  n > RG_LBVH_NOALLOC_MAX_PRIMS returns RG_ERR_TOO_LARGE.  All calls share that array: calls
+ * whose GPU work overlaps (e.g. on two unsynchronised streams) race.  The first call on a device
+ * looks up the array's device address with that device current; make it before any stream
+ * capture. */
+#define RG_LBVH_NOALLOC_MAX_PRIMS 65536u
+rg_status rg_lbvh_build_device_noalloc(const float* d_boxes, uint32_t n, uint32_t* d_morton, uint32_t* d_order,
+                                       uint32_t* d_left, uint32_t* d_right, float* d_nodeboxes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "librgcuda.so")
 
 RG_OK = 0
 ERRORS = {-1: "RG_ERR_INVALID_ARG", -2: "RG_ERR_CUDA", -3: "RG_ERR_OUT_OF_MEMORY", -4: "RG_ERR_NOT_READY",
-          -5: "RG_ERR_STACK_OVERFLOW", -6: "RG_ERR_BUDGET", -7: "RG_ERR_NO_DEVICE"}
+          -5: "RG_ERR_STACK_OVERFLOW", -6: "RG_ERR_BUDGET", -7: "RG_ERR_NO_DEVICE", -8: "RG_ERR_TOO_LARGE"}
 RG_FLAG_DEBUG_IMAGES = 1
 RG_FLAG_COUNT_VISITS = 2
 IMAGES = {"final": 0, "base": 1, "normal": 2, "rough": 3, "rough_transition": 4, "rough_colors_a": 5,
@@ -30,6 +30,7 @@ EXPORTS = [
     "rg_download", "rg_framebuffer_device", "rg_download_image", "rg_synchronize", "rg_get_timings", "rg_get_stats",
     "rg_get_stream", "rg_bvh_info", "rg_instance_inverse", "rg_trace_rays", "rg_post_only", "rg_lbvh_build_host",
     "rg_update_vertices_device", "rg_get_total_stats", "rg_reset_total_stats", "rg_set_flags", "rg_launch_count",
+    "rg_lbvh_build_device_noalloc",
 ]
 
 
@@ -97,6 +98,7 @@ def load(path: str = LIB_PATH):
         "rg_reset_total_stats": ([P], I32),
         "rg_set_flags": ([P, U32], I32),
         "rg_launch_count": ([ctypes.POINTER(ctypes.c_uint64)], I32),
+        "rg_lbvh_build_device_noalloc": ([P, U32, P, P, P, P, P, P], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
