@@ -40,6 +40,7 @@ typedef struct {
 } rg_device_opts;
 #define RG_FLAG_DEBUG_IMAGES 1u /* keep roughTransitions / roughColorsA/B for rg_download_image */
 #define RG_FLAG_COUNT_VISITS 2u /* count BVH node / triangle visits (roofline accounting) */
+#define RG_FLAG_MEGAKERNEL 4u   /* trace + shade in one persistent kernel instead of the wavefront loop */
 
 /* resources/shaders/vertex.def:3-7 (render/vertex.hpp:27-29): 32 B */
 typedef struct {
@@ -115,7 +116,7 @@ typedef struct {
     uint64_t nodes;      /* BVH node visits (RG_FLAG_COUNT_VISITS) */
     uint64_t tris;       /* triangle tests (RG_FLAG_COUNT_VISITS) */
     uint64_t stack_overflows;
-    uint64_t pad;
+    uint64_t iterations; /* trace/shade rounds of the wavefront loop (0 for the megakernel) */
 } rg_stats;
 
 /* Debug images of Raytracer::selectResultImage (raytracer.cpp:379-392). */

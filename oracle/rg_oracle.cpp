@@ -255,11 +255,12 @@ static void lbvh_build(Lbvh& b, const std::vector<Box>& prim) {
             cmin[a] = std::fmin(cmin[a], c);
             cmax[a] = std::fmax(cmax[a], c);
         }
+    // every axis is scaled by the LARGEST centroid extent (a cube), so a thin axis spends few of its
+    // 10 bits and the hierarchy splits mostly along the long axes
     float inv[3];
-    for (int a = 0; a < 3; ++a) {
-        float ext = cmax[a] - cmin[a];
-        inv[a] = ext > 0.0f ? 1.0f / ext : 0.0f;
-    }
+    float emax = 0.0f;
+    for (int a = 0; a < 3; ++a) emax = std::fmax(emax, cmax[a] - cmin[a]);
+    for (int a = 0; a < 3; ++a) inv[a] = emax > 0.0f ? 1.0f / emax : 0.0f;
     for (uint32_t i = 0; i < n; ++i) {
         uint32_t x = quant10(cen[3 * (size_t)i + 0], cmin[0], inv[0]);
         uint32_t y = quant10(cen[3 * (size_t)i + 1], cmin[1], inv[1]);

@@ -24,7 +24,7 @@ struct DevBuf {
 
 struct BvhSet {  // buffers of one LBVH (BLAS or TLAS)
     uint32_t n = 0;
-    DevBuf primBoxes, morton, order, left, right, nodeBoxes, nodes, parents, flags;
+    DevBuf primBoxes, morton, order, left, right, nodeBoxes, nodes, parents, flags, wide;
 };
 
 struct BlasRec {
@@ -70,6 +70,11 @@ struct rg_ctx {
     bool lastFxaa = true;
     // misc
     DevBuf counters, tmpA, tmpB, tmpC, tmpD;  // counters: 8 per-frame + 8 cumulative
+    DevBuf samples, workCounter;               // per-sample payload sums, persistent-kernel work counter
+    // wavefront path state
+    DevBuf wfPayload, wfMeta, wfFrames, wfQO0, wfQO1, wfQD0, wfQD1, wfQP0, wfQP1, wfHitTUV, wfHitInst, wfCounts;
+    uint32_t* hostCount = nullptr;             // pinned word for polling the queue length
+    int lastIterations = 0;
     std::vector<FrameEvents*> evPool, evPending;
     FrameEvents* evCur = nullptr;  // ranges recorded since the last frame
     rg_timings lastTimings{};
@@ -152,6 +157,7 @@ rg_status ensure_bvh(rg_ctx* c, BvhSet& s, uint32_t n) {
     TRY(ensure(c, s.nodes, sizeof(BvhNode) * m));
     TRY(ensure(c, s.parents, 8ull * n));
     TRY(ensure(c, s.flags, 4ull * m));
+    TRY(ensure(c, s.wide, sizeof(WideNode) * m));
     return ensure_sort_scratch(c, n);
 }
 
@@ -184,6 +190,7 @@ rg_status upload_blas_entry(rg_ctx* c, uint32_t b) {
     DevBlas e;
     std::memset(&e, 0, sizeof(e));
     e.nodes = r.bvh.nodes.as<BvhNode>();
+    e.wide = r.bvh.wide.as<WideNode>();
     e.tris = r.tris.as<float4>();
     e.n = r.bvh.n;
     DevBlas* d = c->blasTable.as<DevBlas>() + b;
@@ -225,6 +232,7 @@ DevScene scene_of(rg_ctx* c) {
     s.blas = c->blasTable.as<DevBlas>();
     s.inst = c->instDev.as<DevInstance>();
     s.tlasNodes = c->tlas.nodes.as<BvhNode>();
+    s.tlasWide = c->tlas.wide.as<WideNode>();
     s.tlasOrder = c->tlas.order.as<uint32_t>();
     s.tlasN = c->nInst;
     s.pad = 0;
@@ -246,6 +254,7 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
     CK(setup_instances(c->instIn.as<rg_instance>(), n, c->blasTable.as<DevBlas>(), (uint32_t)c->blas.size(),
                        c->instDev.as<DevInstance>(), c->tlas.primBoxes.as<float>(), c->stream));
     CK(lbvh_build(buffers(c, c->tlas), c->stream));
+    CK(wide_records(buffers(c, c->tlas), c->tlas.wide.as<WideNode>(), c->stream));
     CK(cudaEventRecord(fe->ev[EV_AS1], c->stream));
     fe->hasAs = true;
     c->tlasReady = true;
@@ -280,6 +289,10 @@ rg_status rg_create(rg_ctx** out, const rg_device_opts* opts) {
         return RG_ERR_OUT_OF_MEMORY;
     }
     cudaMemsetAsync(c->counters.p, 0, 128, c->stream);
+    if (cudaHostAlloc(&c->hostCount, sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
+        rg_destroy(c);
+        return RG_ERR_OUT_OF_MEMORY;
+    }
     *out = c;
     return RG_OK;
 }
@@ -290,10 +303,12 @@ rg_status rg_destroy(rg_ctx* c) {
     cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->vertices, &c->indices, &c->materials, &c->blasTable, &c->instIn, &c->instDev, &c->keysA, &c->keysB,
                       &c->valsA, &c->valsB, &c->blockHist, &c->bounds, &c->base, &c->normal, &c->rough, &c->finalImg,
-                      &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC, &c->tmpD};
+                      &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC, &c->tmpD,
+                      &c->samples, &c->workCounter, &c->wfPayload, &c->wfMeta, &c->wfFrames, &c->wfQO0, &c->wfQO1,
+                      &c->wfQD0, &c->wfQD1, &c->wfQP0, &c->wfQP1, &c->wfHitTUV, &c->wfHitInst, &c->wfCounts};
     for (DevBuf* b : bufs) release(c, *b);
     auto relBvh = [&](BvhSet& s) {
-        DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags};
+        DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags, &s.wide};
         for (DevBuf* b : bb) release(c, *b);
     };
     relBvh(c->tlas);
@@ -309,6 +324,7 @@ rg_status rg_destroy(rg_ctx* c) {
             if (e) cudaEventDestroy(e);
         delete f;
     }
+    if (c->hostCount) cudaFreeHost(c->hostCount);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return RG_OK;
@@ -378,6 +394,7 @@ rg_status rg_build_blas(rg_ctx* c, uint32_t vOff, uint32_t iOff, uint32_t triCou
     if (triCount) {
         CK(tri_boxes(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), vOff, iOff, triCount, r.bvh.primBoxes.as<float>(), c->stream));
         CK(lbvh_build(buffers(c, r.bvh), c->stream));
+        CK(wide_records(buffers(c, r.bvh), r.bvh.wide.as<WideNode>(), c->stream));
         CK(tri_records(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), vOff, iOff, r.bvh.order.as<uint32_t>(), triCount,
                        r.tris.as<float4>(), c->stream));
     }
@@ -407,6 +424,7 @@ rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
     if (!fe->hasRefit) CK(cudaEventRecord(fe->ev[EV_REFIT0], c->stream));
     CK(tri_boxes(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, n, r.bvh.primBoxes.as<float>(), c->stream));
     CK(lbvh_refit(buffers(c, r.bvh), c->stream));
+    CK(wide_records(buffers(c, r.bvh), r.bvh.wide.as<WideNode>(), c->stream));
     CK(tri_records(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, r.bvh.order.as<uint32_t>(), n,
                    r.tris.as<float4>(), c->stream));
     CK(cudaMemcpyAsync(c->blasTable.as<DevBlas>()[b].root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
@@ -499,6 +517,8 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     if (!c->W) return fail(c, RG_ERR_NOT_READY, "rg_set_resolution was not called");
     if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS (call rg_build_tlas after the last rg_build_blas)");
     TRY(set_device(c));
+    TRY(ensure(c, c->samples, 48ull * c->W * c->H * (uint32_t)ubo->numSamples));
+    TRY(ensure(c, c->workCounter, 16));
     TraceParams tp;
     std::memset(&tp, 0, sizeof(tp));
     tp.scene = scene_of(c);
@@ -510,11 +530,46 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     tp.rough = c->rough.as<uint2>();
     tp.counters = c->counters.as<unsigned long long>();
     tp.countVisits = (c->flags & RG_FLAG_COUNT_VISITS) ? 1 : 0;
+    tp.samples = c->samples.as<float4>();
+    tp.workCounter = c->workCounter.as<uint32_t>();
+    const bool mega = (c->flags & RG_FLAG_MEGAKERNEL) != 0;
+    if (!mega) {
+        const size_t P = (size_t)c->W * c->H * (uint32_t)ubo->numSamples;
+        TRY(ensure(c, c->wfPayload, 64 * P));
+        TRY(ensure(c, c->wfMeta, 8 * P));
+        TRY(ensure(c, c->wfFrames, 144ull * kMaxFrames * P));
+        TRY(ensure(c, c->wfQO0, 16 * P));
+        TRY(ensure(c, c->wfQO1, 16 * P));
+        TRY(ensure(c, c->wfQD0, 16 * P));
+        TRY(ensure(c, c->wfQD1, 16 * P));
+        TRY(ensure(c, c->wfQP0, 4 * P));
+        TRY(ensure(c, c->wfQP1, 4 * P));
+        TRY(ensure(c, c->wfHitTUV, 16 * P));
+        TRY(ensure(c, c->wfHitInst, 4 * P));
+        TRY(ensure(c, c->wfCounts, 16));
+        WavefrontBuffers& w = tp.wf;
+        w.payload = c->wfPayload.as<float4>();
+        w.meta = c->wfMeta.as<int2>();
+        w.frames = c->wfFrames.p;
+        w.qO[0] = c->wfQO0.as<float4>();
+        w.qO[1] = c->wfQO1.as<float4>();
+        w.qD[0] = c->wfQD0.as<float4>();
+        w.qD[1] = c->wfQD1.as<float4>();
+        w.qPath[0] = c->wfQP0.as<uint32_t>();
+        w.qPath[1] = c->wfQP1.as<uint32_t>();
+        w.hitTUV = c->wfHitTUV.as<float4>();
+        w.hitInst = c->wfHitInst.as<uint32_t>();
+        w.counts = c->wfCounts.as<uint32_t>();
+    }
     CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
     CK(cudaEventRecord(fe->ev[EV_RT0], c->stream));
-    CK(launch_trace(tp, c->stream));
+    if (mega) {
+        c->lastIterations = 0;
+        CK(launch_trace(tp, c->stream));
+    }
+    else CK(launch_trace_wavefront(tp, c->stream, c->hostCount, &c->lastIterations));
     return run_post(c, ubo, fxaa);
 }
 
@@ -639,7 +694,7 @@ static rg_status read_stats(rg_ctx* c, rg_stats* s, int base) {
     s->nodes = v[base + 4];
     s->tris = v[base + 5];
     s->stack_overflows = v[base + 6];
-    s->pad = 0;
+    s->iterations = base == 0 ? (uint64_t)c->lastIterations : 0;
     return RG_OK;
 }
 
@@ -748,7 +803,7 @@ rg_status rg_lbvh_build_host(rg_ctx* c, const float* boxes, uint32_t n, uint32_t
         if (e != cudaSuccess) st = fail(c, RG_ERR_CUDA, cudaGetErrorString(e));
         if (st == RG_OK) st = download_bvh(c, s, morton, order, left, right, nodeboxes);
     }
-    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags};
+    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags, &s.wide};
     cudaStreamSynchronize(c->stream);
     for (DevBuf* b : bb) release(c, *b);
     return st;

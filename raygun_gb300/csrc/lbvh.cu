@@ -4,7 +4,7 @@
 // (render/acceleration_structure.cpp:55-194), which the reference leaves opaque:
 //   1. primitive boxes (triangles: min/max of the three vertices)
 //   2. centroid bounds (order-preserving uint atomics: exact, order independent)
-//   3. 30-bit Morton codes of the centroids, normalised to the centroid bounds
+//   3. 30-bit Morton codes of the centroids, normalised to the cube of the largest centroid extent
 //   4. stable LSD radix sort of (code, primitive) in four 8-bit passes
 //   5. Karras 2012 hierarchy (n-1 internal nodes; equal codes split on the index)
 //   6. bottom-up boxes: one thread per leaf climbs; the second arrival at a node writes its box
@@ -92,12 +92,15 @@ __global__ void k_morton(const float* __restrict__ boxes, uint32_t n, const uint
                          uint32_t* __restrict__ morton, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
+    // every axis is scaled by the LARGEST centroid extent (a cube), so a thin axis spends few of its
+    // 10 bits and the hierarchy splits mostly along the long axes
     float lo[3], inv[3];
+    float emax = 0.0f;
     for (int a = 0; a < 3; ++a) {
         lo[a] = ord2f(bounds[a]);
-        float ext = __fsub_rn(ord2f(bounds[3 + a]), lo[a]);
-        inv[a] = ext > 0.0f ? __fdiv_rn(1.0f, ext) : 0.0f;
+        emax = fmaxf(emax, __fsub_rn(ord2f(bounds[3 + a]), lo[a]));
     }
+    for (int a = 0; a < 3; ++a) inv[a] = emax > 0.0f ? __fdiv_rn(1.0f, emax) : 0.0f;
     float c[3];
     centroid(boxes + 6 * (size_t)p, c);
     uint32_t x = quant10(c[0], lo[0], inv[0]), y = quant10(c[1], lo[1], inv[1]), z = quant10(c[2], lo[2], inv[2]);
@@ -267,6 +270,58 @@ __global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t*
     }
 }
 
+// ---- 4-wide records ----------------------------------------------------------------------------
+__device__ inline void child_box(const float* __restrict__ primBoxes, const uint32_t* __restrict__ order, const float* nodeBoxes,
+                                 uint32_t ref, float* b) {
+    const float* p = (ref & kLeaf) ? primBoxes + 6 * (size_t)order[ref & ~kLeaf] : nodeBoxes + 6 * (size_t)ref;
+    for (int a = 0; a < 6; ++a) b[a] = p[a];
+}
+
+__global__ void k_wide_records(const float* __restrict__ primBoxes, const uint32_t* __restrict__ order, uint32_t n,
+                               const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                               const float* __restrict__ nodeBoxes, WideNode* __restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1 >= n) return;
+    uint32_t refs[4];
+    int k = 0;
+    for (uint32_t c : {left[i], right[i]}) {
+        if (c & kLeaf) {
+            refs[k++] = c;
+        } else {
+            refs[k++] = left[c];
+            refs[k++] = right[c];
+        }
+    }
+    float lo[3][4], hi[3][4];
+    uint32_t r[4];
+    for (int j = 0; j < 4; ++j) {
+        if (j < k) {
+            float b[6];
+            child_box(primBoxes, order, nodeBoxes, refs[j], b);
+            for (int a = 0; a < 3; ++a) {
+                lo[a][j] = b[a];
+                hi[a][j] = b[3 + a];
+            }
+            r[j] = refs[j];
+        } else {
+            for (int a = 0; a < 3; ++a) {
+                lo[a][j] = INFINITY;
+                hi[a][j] = -INFINITY;
+            }
+            r[j] = kEmptySlot;
+        }
+    }
+    WideNode w;
+    w.lox = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
+    w.hix = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
+    w.loy = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
+    w.hiy = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
+    w.loz = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
+    w.hiz = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+    w.ref = make_uint4(r[0], r[1], r[2], r[3]);
+    out[i] = w;
+}
+
 // ---- instances ----------------------------------------------------------------------------------
 __global__ void k_instances(const rg_instance* __restrict__ in, uint32_t n, const DevBlas* __restrict__ blas, uint32_t nblas,
                             DevInstance* __restrict__ out, float* __restrict__ boxes) {
@@ -351,6 +406,13 @@ cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b.flags, 0, sizeof(uint32_t) * (b.n - 1), s);
     if (e != cudaSuccess) return e;
     k_bottom_up<<<blocks(b.n, 256), 256, 0, s>>>(b.primBoxes, b.order, b.n, b.left, b.right, b.parents, b.flags, b.nodeBoxes, b.nodes);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t wide_records(const LbvhBuffers& b, WideNode* out, cudaStream_t s) {
+    if (b.n <= 1) return cudaSuccess;
+    k_wide_records<<<blocks(b.n - 1, 256), 256, 0, s>>>(b.primBoxes, b.order, b.n, b.left, b.right, b.nodeBoxes, out);
     count_launch();
     return cudaGetLastError();
 }

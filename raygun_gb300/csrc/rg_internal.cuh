@@ -17,7 +17,10 @@
 namespace rg {
 
 constexpr uint32_t kLeaf = 0x80000000u;
-constexpr int kTraversalStack = 64;
+#ifndef RG_STACK_DEPTH
+#define RG_STACK_DEPTH 48
+#endif
+constexpr int kTraversalStack = RG_STACK_DEPTH;
 constexpr int kMaxFrames = 10;  // maxRecursions (<= 8 supported) + primary + masked-miss leaf
 
 // BVH2 node: boxes of BOTH children so one 64-byte node fetch (four 16-byte loads) tests two
@@ -30,12 +33,24 @@ struct __align__(16) BvhNode {
 };
 static_assert(sizeof(BvhNode) == 64, "node");
 
+// 4-wide record of BVH2 node i: the boxes and refs of i's grandchildren (a leaf child stands in
+// for its own slot).  Traversal visits records only, so it skips every other BVH2 level; the
+// BVH2 itself stays the built and checked structure.  Empty slots have ref kEmptySlot and an
+// inverted box.  112 B = seven 16-byte loads.
+constexpr uint32_t kEmptySlot = 0xFFFFFFFEu;
+struct __align__(16) WideNode {
+    float4 lox, hix, loy, hiy, loz, hiz;  // per slot
+    uint4 ref;
+};
+static_assert(sizeof(WideNode) == 112, "wide node");
+
 struct Box {
     float lo[3], hi[3];
 };
 
 // per-BLAS record read by the traversal kernel
 struct DevBlas {
+    const WideNode* wide;
     const BvhNode* nodes;
     const float4* tris;  // 3 float4 per sorted leaf: v0 (w = primitive id bits), v1, v2
     uint32_t n;          // triangle count
@@ -56,6 +71,7 @@ struct DevScene {
     const DevBlas* blas;
     const DevInstance* inst;
     const BvhNode* tlasNodes;
+    const WideNode* tlasWide;
     const uint32_t* tlasOrder;  // sorted position -> instance
     uint32_t tlasN;
     uint32_t pad;
@@ -122,12 +138,26 @@ struct LbvhBuffers {  // scratch + outputs of one LBVH build, sized by the calle
 size_t sort_block_count(uint32_t n);
 cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s);  // topology kept, primBoxes changed
+cudaError_t wide_records(const LbvhBuffers& b, WideNode* out, cudaStream_t s);  // after build / refit
 cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes,
                       cudaStream_t s);
 cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, const uint32_t* order, uint32_t n,
                         float4* tris, cudaStream_t s);
 cudaError_t setup_instances(const rg_instance* in, uint32_t n, const DevBlas* blas, uint32_t nblas, DevInstance* out,
                             float* boxes, cudaStream_t s);
+
+// device buffers of the wavefront path (one path per pixel sample; P = paths)
+struct WavefrontBuffers {
+    float4* payload;   // P x 4 float4: the reference payload (payload.h:29-39)
+    int2* meta;        // P: frame-stack depth, miss index of the pending ray
+    void* frames;      // P x kMaxFrames paused closest-hit frames (144 B each)
+    float4* qO[2];     // ray queues: origin + tmin
+    float4* qD[2];     //             direction + tmax
+    uint32_t* qPath[2];
+    float4* hitTUV;    // per queue slot: t, u, v, primitive bits
+    uint32_t* hitInst; // per queue slot: instance or 0xFFFFFFFF (miss)
+    uint32_t* counts;  // [0], [1] queue lengths, [2] trace work counter
+};
 
 struct TraceParams {
     DevScene scene;
@@ -136,10 +166,15 @@ struct TraceParams {
     uint2* base;    // RGBA16F images (8 B per pixel)
     uint2* normal;
     uint2* rough;
-    unsigned long long* counters;  // 8
+    unsigned long long* counters;  // 8 per frame + 8 cumulative
+    float4* samples;               // W*H*S*3 per-sample payload sums (k_trace -> k_resolve)
+    uint32_t* workCounter;         // work-item counter of the persistent kernel
     int countVisits;
+    WavefrontBuffers wf;
 };
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
+// hostCount: pinned host word used to poll the queue length; iterations: trace/shade rounds run
+cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations);
 cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
 
 struct PostParams {

@@ -117,93 +117,177 @@ struct VisitCounts {
     unsigned long long nodes, tris, overflow;
 };
 
-template <bool COUNT>
-__device__ Hit closest_hit(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
-                           VisitCounts& vc) {
+constexpr int kTraceThreads = 128;
+#ifndef RG_TRACE_MIN_BLOCKS
+#define RG_TRACE_MIN_BLOCKS 4
+#endif
+
+// per-thread traversal stack in shared memory, laid out [depth][thread] so that the 32 lanes of a
+// warp touching the same depth hit 32 different banks
+struct SmemStack {
+    uint32_t* base;  // &stack[0][threadIdx.x]
+    __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i * kTraceThreads]; }
+};
+// the same stack in (L1-cached) local memory
+#ifndef RG_STACK_SMEM
+#define RG_STACK_SMEM 1
+#endif
+#if !RG_STACK_SMEM
+struct LocalStack {
+    uint32_t* base;
+    __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i]; }
+};
+#endif
+#if RG_STACK_SMEM
+#define RG_DECLARE_STACK(name)                                  \
+    __shared__ uint32_t name##_mem[kTraversalStack][kTraceThreads]; \
+    const SmemStack name{&name##_mem[0][threadIdx.x]}
+using TravStack = SmemStack;
+#else
+#define RG_DECLARE_STACK(name)                 \
+    uint32_t name##_mem[kTraversalStack];      \
+    const LocalStack name{name##_mem}
+using TravStack = LocalStack;
+#endif
+#ifndef RG_WF_MIN_BLOCKS
+#define RG_WF_MIN_BLOCKS 7
+#endif
+
+// Resumable traversal of one ray: trav_begin sets it up, each trav_step processes one node or one
+// leaf (a 4-wide record tests up to four grandchildren of a BVH2 node and descends into the nearest
+// hit; a TLAS leaf moves the ray into the instance's object space and descends into its BLAS
+// behind a marker entry; a BLAS leaf runs the triangle test).  The
+// kernel interleaves trav_step with shading so that a lane whose ray finished does not idle.
+struct Trav {
+    float ox, oy, oz, dx, dy, dz, tmin;  // world-space ray
+    Ray r;                               // the ray of the current level (world or object space)
     Hit h;
-    h.hit = false;
-    h.t = tmax;
-    h.u = h.v = 0.0f;
-    h.inst = h.prim = 0xFFFFFFFFu;
-    if ((dx == 0.0f && dy == 0.0f && dz == 0.0f) || sc.tlasN == 0) return h;
-    Ray wr;
-    ray_pre(wr, ox, oy, oz, dx, dy, dz);
-    if (sc.tlasN > 1 && slab(wr, sc.tlasRoot[0], sc.tlasRoot[3], sc.tlasRoot[1], sc.tlasRoot[4], sc.tlasRoot[2], sc.tlasRoot[5], tmin, h.t) == INFINITY)
-        return h;
-    uint32_t stack[kTraversalStack];
-    int sp = 0;
-    Ray r = wr;
-    const BvhNode* nodes = sc.tlasNodes;
-    const float4* tris = nullptr;
-    bool inBlas = false;
-    uint32_t inst = 0;
-    uint32_t ref = sc.tlasN == 1 ? kLeaf : 0u;
-    for (;;) {
-        if (!(ref & kLeaf)) {
-            if (COUNT) vc.nodes++;
-            const BvhNode* nd = nodes + ref;
-            float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
-            uint4 d = __ldg(&nd->d);
-            float tl = slab(r, a.x, a.y, a.z, a.w, b.x, b.y, tmin, h.t);
-            float tr = slab(r, b.z, b.w, c.x, c.y, c.z, c.w, tmin, h.t);
-            bool hl = tl != INFINITY, hr = tr != INFINITY;
-            if (hl && hr) {
-                bool rFirst = tr < tl;
-                uint32_t nearR = rFirst ? d.y : d.x, farR = rFirst ? d.x : d.y;
-                if (sp < kTraversalStack) stack[sp++] = farR;
-                else if (COUNT || true) vc.overflow++;
-                ref = nearR;
-                continue;
-            }
-            if (hl) { ref = d.x; continue; }
-            if (hr) { ref = d.y; continue; }
-        } else if (inBlas) {
-            if (COUNT) vc.tris++;
-            const float4* tp = tris + 3 * (size_t)(ref & ~kLeaf);
-            tri_test(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), tmin, inst, h);
-        } else {
-            uint32_t ii = __ldg(sc.tlasOrder + (ref & ~kLeaf));
-            const DevInstance* in = sc.inst + ii;
-            if (__ldg(&in->valid)) {
-                float4 i0 = __ldg(&in->inv[0]), i1 = __ldg(&in->inv[1]), i2 = __ldg(&in->inv[2]);
-                float qx = ((i0.x * ox + i0.y * oy) + i0.z * oz) + i0.w;
-                float qy = ((i1.x * ox + i1.y * oy) + i1.z * oz) + i1.w;
-                float qz = ((i2.x * ox + i2.y * oy) + i2.z * oz) + i2.w;
-                float ex = (i0.x * dx + i0.y * dy) + i0.z * dz;
-                float ey = (i1.x * dx + i1.y * dy) + i1.z * dz;
-                float ez = (i2.x * dx + i2.y * dy) + i2.z * dz;
-                if (!(ex == 0.0f && ey == 0.0f && ez == 0.0f)) {
-                    const DevBlas* bl = sc.blas + __ldg(&in->blas);
-                    uint32_t bn = __ldg(&bl->n);
-                    Ray orr;
-                    ray_pre(orr, qx, qy, qz, ex, ey, ez);
-                    const float* rb = bl->root;
-                    if (bn > 0 && slab(orr, __ldg(rb + 0), __ldg(rb + 3), __ldg(rb + 1), __ldg(rb + 4), __ldg(rb + 2), __ldg(rb + 5), tmin, h.t) != INFINITY) {
-                        if (sp < kTraversalStack) {
-                            stack[sp++] = kMarker;
-                            r = orr;
-                            nodes = bl->nodes;
-                            tris = bl->tris;
-                            inst = ii;
-                            inBlas = true;
-                            ref = bn == 1 ? kLeaf : 0u;
-                            continue;
-                        }
-                        vc.overflow++;
+    const WideNode* nodes;
+    const float4* tris;
+    uint32_t ref, inst;
+    int sp;
+    bool inBlas, active;
+};
+
+__device__ __forceinline__ void trav_begin(Trav& T, const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz,
+                                           float tmin, float tmax) {
+    T.h.hit = false;
+    T.h.t = tmax;
+    T.h.u = T.h.v = 0.0f;
+    T.h.inst = T.h.prim = 0xFFFFFFFFu;
+    T.active = false;
+    if ((dx == 0.0f && dy == 0.0f && dz == 0.0f) || sc.tlasN == 0) return;
+    T.ox = ox; T.oy = oy; T.oz = oz;
+    T.dx = dx; T.dy = dy; T.dz = dz;
+    T.tmin = tmin;
+    ray_pre(T.r, ox, oy, oz, dx, dy, dz);
+    if (sc.tlasN > 1 && slab(T.r, sc.tlasRoot[0], sc.tlasRoot[3], sc.tlasRoot[1], sc.tlasRoot[4], sc.tlasRoot[2], sc.tlasRoot[5], tmin, T.h.t) == INFINITY)
+        return;
+    T.sp = 0;
+    T.nodes = sc.tlasWide;
+    T.tris = nullptr;
+    T.inBlas = false;
+    T.inst = 0;
+    T.ref = sc.tlasN == 1 ? kLeaf : 0u;
+    T.active = true;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const TravStack& stack, VisitCounts& vc) {
+    const uint32_t ref = T.ref;
+    const float tmin = T.tmin;
+    if (!(ref & kLeaf)) {
+        if (COUNT) vc.nodes++;
+        const WideNode* nd = T.nodes + ref;
+        const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix), ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+        const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+        const uint4 rf = __ldg(&nd->ref);
+        float t[4];
+        uint32_t r[4] = {rf.x, rf.y, rf.z, rf.w};
+        t[0] = slab(T.r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, tmin, T.h.t);
+        t[1] = slab(T.r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, tmin, T.h.t);
+        t[2] = r[2] != kEmptySlot ? slab(T.r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, tmin, T.h.t) : INFINITY;
+        t[3] = r[3] != kEmptySlot ? slab(T.r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, tmin, T.h.t) : INFINITY;
+        // nearest first: 5 compare-exchanges sort the four (t, ref) pairs
+#define RG_CSWAP(a, b)                                           \
+        if (t[b] < t[a]) {                                       \
+            float tt = t[a]; t[a] = t[b]; t[b] = tt;             \
+            uint32_t rr = r[a]; r[a] = r[b]; r[b] = rr;          \
+        }
+        RG_CSWAP(0, 1) RG_CSWAP(2, 3) RG_CSWAP(0, 2) RG_CSWAP(1, 3) RG_CSWAP(1, 2)
+#undef RG_CSWAP
+        if (t[0] != INFINITY) {
+#pragma unroll
+            for (int j = 3; j >= 1; --j)
+                if (t[j] != INFINITY) {
+                    if (T.sp < kTraversalStack) stack[T.sp++] = r[j];
+                    else vc.overflow++;
+                }
+            T.ref = r[0];
+            return;
+        }
+    } else if (T.inBlas) {
+        if (COUNT) vc.tris++;
+        const float4* tp = T.tris + 3 * (size_t)(ref & ~kLeaf);
+        tri_test(T.r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), tmin, T.inst, T.h);
+    } else {
+        uint32_t ii = __ldg(sc.tlasOrder + (ref & ~kLeaf));
+        const DevInstance* in = sc.inst + ii;
+        if (__ldg(&in->valid)) {
+            const float ox = T.ox, oy = T.oy, oz = T.oz, dx = T.dx, dy = T.dy, dz = T.dz;
+            float4 i0 = __ldg(&in->inv[0]), i1 = __ldg(&in->inv[1]), i2 = __ldg(&in->inv[2]);
+            float qx = ((i0.x * ox + i0.y * oy) + i0.z * oz) + i0.w;
+            float qy = ((i1.x * ox + i1.y * oy) + i1.z * oz) + i1.w;
+            float qz = ((i2.x * ox + i2.y * oy) + i2.z * oz) + i2.w;
+            float ex = (i0.x * dx + i0.y * dy) + i0.z * dz;
+            float ey = (i1.x * dx + i1.y * dy) + i1.z * dz;
+            float ez = (i2.x * dx + i2.y * dy) + i2.z * dz;
+            if (!(ex == 0.0f && ey == 0.0f && ez == 0.0f)) {
+                const DevBlas* bl = sc.blas + __ldg(&in->blas);
+                uint32_t bn = __ldg(&bl->n);
+                Ray orr;
+                ray_pre(orr, qx, qy, qz, ex, ey, ez);
+                const float* rb = bl->root;
+                if (bn > 0 && slab(orr, __ldg(rb + 0), __ldg(rb + 3), __ldg(rb + 1), __ldg(rb + 4), __ldg(rb + 2), __ldg(rb + 5), tmin, T.h.t) != INFINITY) {
+                    if (T.sp < kTraversalStack) {
+                        stack[T.sp++] = kMarker;
+                        T.r = orr;
+                        T.nodes = bl->wide;
+                        T.tris = bl->tris;
+                        T.inst = ii;
+                        T.inBlas = true;
+                        T.ref = bn == 1 ? kLeaf : 0u;
+                        return;
                     }
+                    vc.overflow++;
                 }
             }
         }
-        // pop
-        for (;;) {
-            if (sp == 0) return h;
-            ref = stack[--sp];
-            if (ref != kMarker) break;
-            inBlas = false;
-            r = wr;
-            nodes = sc.tlasNodes;
-        }
     }
+    // pop (a marker leaves the BLAS: back to the world-space ray and the TLAS)
+    for (;;) {
+        if (T.sp == 0) {
+            T.active = false;
+            return;
+        }
+        uint32_t nr = stack[--T.sp];
+        if (nr != kMarker) {
+            T.ref = nr;
+            return;
+        }
+        T.inBlas = false;
+        T.nodes = sc.tlasWide;
+        ray_pre(T.r, T.ox, T.oy, T.oz, T.dx, T.dy, T.dz);
+    }
+}
+
+template <bool COUNT>
+__device__ Hit closest_hit(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
+                           const TravStack& stack, VisitCounts& vc) {
+    Trav T;
+    trav_begin(T, sc, ox, oy, oz, dx, dy, dz, tmin, tmax);
+    while (T.active) trav_step<COUNT>(T, sc, stack, vc);
+    return T.h;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -263,7 +347,7 @@ enum : int {
     R_ST_C = 6         // SHADOW_TRACE, after the shadow-internal ray (:158)
 };
 
-struct Frame {
+struct __align__(16) Frame {
     int kind, front, rayConsumption, pad;
     V3 origin, D, n;
     float t;
@@ -273,7 +357,9 @@ struct Frame {
     V3 shadow;        // GENERIC: shadowColor
     V3 reflectColor;  // GENERIC
     float reflectDepth;
+    float pad1;
 };
+static_assert(sizeof(Frame) == 144, "frame");
 
 // miss.rmiss:38-83
 __device__ void sky(Payload& p, V3 D, V3 L) {
@@ -339,348 +425,688 @@ struct RayReq {
     bool masked;
 };
 
+struct RayCounts {
+    unsigned long long primary, shadow, secondary, masked;
+};
+
+// One step of the closest-hit / miss state machine: consume the result `h` of the pending trace and
+// run the paused invocations on the frame stack until the next trace is needed (returns true, `ray`
+// set) or the sample's primary trace has returned (returns false).
+__device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const int maxRec, const Hit& h, Payload& p, RayReq& ray,
+                                           Frame* frames, int& fsp, Frame& cur, RayCounts& cnt) {
+    int ph;
+    if (!h.hit) {
+        if (ray.missIndex == 0) sky(p, ray.d, L);
+        else p.hitValue = v3s(1.0f);  // shadowMiss.rmiss:30-34
+        ph = PH_RETURN;
+    } else {
+        ph = PH_HIT;
+    }
+    bool newRay = false;
+    V3 refractColor = v3s(1.0f);
+    while (!newRay) {
+        if (ph == PH_HIT) {
+            // closesthit.rchit:95-122 -- fetch, world position, world normal, grid effect
+            const DevInstance* in = sc.inst + h.inst;
+            const uint32_t vOff = __ldg(&in->vOff), iOff = __ldg(&in->iOff), mOff = __ldg(&in->mOff);
+            const float4 m0 = __ldg(&in->m[0]), m1 = __ldg(&in->m[1]), m2 = __ldg(&in->m[2]);
+            const float hitT = h.t;
+            const float bx = (1.0f - h.u) - h.v, by = h.u, bz = h.v;
+            const uint32_t ib = iOff + 3 * h.prim;
+            const rg_vertex* v0 = sc.vertices + vOff + __ldg(sc.indices + ib);
+            const rg_vertex* v1 = sc.vertices + vOff + __ldg(sc.indices + ib + 1);
+            const rg_vertex* v2 = sc.vertices + vOff + __ldg(sc.indices + ib + 2);
+            const uint32_t matIndex = __ldg(&v0->matIndex);
+            V3 n0 = v3(__ldg(&v0->normal[0]), __ldg(&v0->normal[1]), __ldg(&v0->normal[2]));
+            V3 n1 = v3(__ldg(&v1->normal[0]), __ldg(&v1->normal[1]), __ldg(&v1->normal[2]));
+            V3 n2 = v3(__ldg(&v2->normal[0]), __ldg(&v2->normal[1]), __ldg(&v2->normal[2]));
+            const rg_material* M = sc.materials + mOff + matIndex;
+            cur.diffuse = v3(__ldg(&M->diffuse[0]), __ldg(&M->diffuse[1]), __ldg(&M->diffuse[2]));
+            cur.specular = v3(__ldg(&M->specular[0]), __ldg(&M->specular[1]), __ldg(&M->specular[2]));
+            cur.transparency = __ldg(&M->transparency);
+            cur.reflectivity = __ldg(&M->reflectivity);
+            cur.roughness = __ldg(&M->roughness);
+            cur.ior = __ldg(&M->ior);
+            cur.emission = __ldg(&M->emission);
+            cur.rayConsumption = (int)__ldg(&M->rayConsumption);
+            const uint32_t effectId = __ldg(&M->effectId);
+            cur.origin = ray.o + ray.d * hitT;
+            cur.D = ray.d;
+            cur.t = hitT;
+            V3 vn = (n0 * bx + n1 * by) + n2 * bz;
+            V3 wn = v3((m0.x * vn.x + m0.y * vn.y) + m0.z * vn.z, (m1.x * vn.x + m1.y * vn.y) + m1.z * vn.z,
+                       (m2.x * vn.x + m2.y * vn.y) + m2.z * vn.z);
+            cur.n = normalize(wn);
+            if (effectId == 1) {  // gridEffect, closesthit.rchit:74-91
+                V3 pos = cur.origin;
+                float aa = ((p.refDepth + hitT) + 8.0f) / 30.0f;
+                float aa2 = aa / 2.0f;
+                float minmod = fminf(fabsf(glsl_mod((pos.x + 1000.0f) * 10.0f + aa2, 20.0f) - aa2),
+                                     fabsf(glsl_mod((pos.z + 1000.0f) * 10.0f + aa2, 20.0f) - aa2));
+                if (minmod < aa2) {
+                    float aa_sq = aa * aa;
+                    minmod = minmod - (aa2 - aa_sq / 3.0f);
+                    minmod = minmod * (3.0f / aa_sq);
+                    float f = mixs(aa / 10.0f, 1.0f, minmod);
+                    cur.diffuse = cur.diffuse * f;
+                    cur.specular = cur.specular * f;
+                    cur.reflectivity = cur.reflectivity * f;
+                }
+                if (glsl_mod((pos.x + 1000.0f) * 5.0f, 20.0f) < 10.0f && glsl_mod((pos.z + 1000.0f) * 5.0f, 20.0f) < 10.0f)
+                    cur.reflectivity = cur.reflectivity * 1.5f;
+            }
+            if (p.rayType == RT_SHADOW_INTERNAL) {  // :125-152
+                float thick = clampf(hitT * (1.0f - cur.transparency) * 10.0f, 0.0f, 1.0f);
+                V3 shadowCol = p.hitValue - mix(v3s(0.0f), normalize(v3s(1.1f) - cur.diffuse) + v3s(0.1f), thick);
+                if (p.recDepth < maxRec) {
+                    p.rayType = RT_SHADOW_TRACE;
+                    p.recDepth++;
+                    cnt.shadow++;
+                    cur.base = shadowCol;
+                    cur.kind = R_SI_A;
+                    frames[fsp++] = cur;
+                    ray.o = cur.origin; ray.d = cur.D; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = false;
+                    newRay = true;
+                } else {
+                    p.hitValue = shadowCol * 0.4f;
+                    ph = PH_RETURN;
+                }
+            } else if (p.rayType == RT_SHADOW_TRACE) {  // :153-166
+                if (cur.transparency > 0.0f) {
+                    if (p.recDepth < maxRec) {
+                        p.rayType = RT_SHADOW_INTERNAL;
+                        p.recDepth++;
+                        cnt.shadow++;
+                        cur.kind = R_ST_C;
+                        frames[fsp++] = cur;
+                        ray.o = cur.origin; ray.d = cur.D; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 1; ray.masked = false;
+                        newRay = true;
+                    } else {
+                        ph = PH_RETURN;
+                    }
+                } else {
+                    float f = mixs(0.4f, 0.8f, clampf(logf(hitT) / 8.0f, 0.0f, 1.0f));
+                    p.hitValue = p.hitValue * f;
+                    ph = PH_RETURN;
+                }
+            } else {  // GENERIC, :168-204
+                cur.front = dot(-cur.D, cur.n) > 0.0f;
+                if (!cur.front) cur.n = normalize(-cur.n);
+                float ndl = dot(-L, cur.n);
+                float dp = fmaxf(ndl, 0.2f);
+                cur.base = cur.diffuse * dp;
+                cur.reflectColor = v3s(1.0f);
+                cur.reflectDepth = 0.0f;
+                if (ndl > 0.07f) {
+                    if (p.recDepth < maxRec) {
+                        p.hitValue = v3s(1.0f);
+                        p.rayType = RT_SHADOW_TRACE;
+                        p.recDepth++;
+                        cnt.shadow++;
+                        cur.kind = R_G_SHADOW;
+                        frames[fsp++] = cur;
+                        ray.o = cur.origin; ray.d = -L; ray.tmin = 0.01f * 10.0f; ray.tmax = 1000.0f; ray.missIndex = 1; ray.masked = false;
+                        newRay = true;
+                    } else {
+                        cur.shadow = v3s(1.0f);
+                        ph = PH_G_REFLECT;
+                    }
+                } else {
+                    float tr = cur.transparency;
+                    float sm = tr * tr;
+                    cur.shadow = tr < 1.0f ? mix(v3s(1.0f), cur.diffuse * sm, tr) : v3s(0.4f);
+                    ph = PH_G_REFLECT;
+                }
+            }
+        } else if (ph == PH_G_REFLECT) {  // :206-221
+            if (p.recDepth < maxRec && cur.reflectivity > 0.0f) {
+                V3 dir = reflect(cur.D, cur.n);
+                p.recDepth += cur.rayConsumption;
+                p.refDepth = p.refDepth + cur.t;
+                cnt.secondary++;
+                cur.kind = R_G_REFLECT;
+                frames[fsp++] = cur;
+                ray.o = cur.origin; ray.d = dir; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = false;
+                newRay = true;
+            } else {
+                ph = PH_G_REFRACT;
+            }
+        } else if (ph == PH_G_REFRACT) {  // :223-251
+            if (p.recDepth < maxRec && cur.transparency > 0.0f) {
+                V3 dir;
+                if (cur.front) {
+                    float eta = p.curIOR / cur.ior;
+                    dir = refract(cur.D, cur.n, eta);
+                    p.curIOR = cur.ior;
+                    cur.kind = R_G_REFR_F;
+                } else {
+                    float eta = cur.ior / 1.0f;
+                    dir = refract(cur.D, cur.n, eta);
+                    p.curIOR = 1.0f;
+                    cur.kind = R_G_REFR_B;
+                }
+                p.recDepth++;
+                cnt.secondary++;
+                frames[fsp++] = cur;
+                ray.o = cur.origin; ray.d = dir; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = false;
+                newRay = true;
+            } else {
+                refractColor = v3s(1.0f);
+                ph = PH_G_COMPOSE;
+            }
+        } else if (ph == PH_G_COMPOSE) {  // :253-267
+            V3 baseColor = cur.base * cur.shadow;
+            baseColor = baseColor + cur.diffuse * cur.emission;
+            float total = fmaxf(cur.transparency, cur.reflectivity);
+            float den = cur.transparency + cur.reflectivity;
+            float w = den == 0.0f ? 0.0f : cur.reflectivity / den;
+            V3 roughCol = mix(refractColor, cur.reflectColor, w);
+            p.hitValue = mix(baseColor, roughCol, total);
+            if (p.recDepth == 0) {
+                p.hitValue = baseColor;
+                p.normal = cur.n;
+                p.roughRGB = roughCol;
+                p.roughA = fminf((cur.reflectDepth / 50.0f) * cur.roughness, cur.roughness / 2.1f);
+                p.reflectContribution = total;
+            }
+            p.depth = cur.t;
+            ph = PH_RETURN;
+        } else {  // PH_RETURN: resume the paused invocation
+            if (fsp == 0) break;
+            cur = frames[--fsp];
+            switch (cur.kind) {
+                case R_G_SHADOW:
+                    p.recDepth--;
+                    cur.shadow = p.hitValue;
+                    p.rayType = RT_GENERIC;
+                    ph = PH_G_REFLECT;
+                    break;
+                case R_G_REFLECT:
+                    p.recDepth -= cur.rayConsumption;
+                    cur.reflectColor = p.hitValue * cur.specular;
+                    cur.reflectDepth = p.depth;
+                    ph = PH_G_REFRACT;
+                    break;
+                case R_G_REFR_F:
+                    p.recDepth--;
+                    refractColor = p.hitValue;
+                    ph = PH_G_COMPOSE;
+                    break;
+                case R_G_REFR_B:
+                    p.recDepth--;
+                    refractColor = mix(v3s(1.0f), cur.diffuse, logf(1.0f + cur.t)) * p.hitValue;
+                    ph = PH_G_COMPOSE;
+                    break;
+                case R_SI_A:
+                    p.recDepth--;
+                    if (p.depth < 1000.0f) {
+                        p.hitValue = p.hitValue * cur.base;
+                        ph = PH_RETURN;
+                    } else {
+                        float eta = cur.ior / 1.0f;
+                        V3 dir = refract(cur.D, cur.n, eta);
+                        float x = dot(L, dir);
+                        float dp = x * x * x * x * x + 0.75f;
+                        cur.base = cur.base * dp;
+                        cur.kind = R_SI_B;
+                        frames[fsp++] = cur;
+                        cnt.masked++;
+                        ray.o = cur.origin; ray.d = -dir; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = true;
+                        newRay = true;
+                    }
+                    break;
+                case R_SI_B:
+                    p.hitValue = cur.base + p.hitValue * 0.1f;
+                    ph = PH_RETURN;
+                    break;
+                default:  // R_ST_C
+                    p.recDepth--;
+                    ph = PH_RETURN;
+                    break;
+            }
+        }
+    }
+    return newRay;
+}
+
+// raygen.h:84-102: camera ray of one sample and the payload initialisation
+__device__ __forceinline__ void start_sample(const rg_ubo& U, const V3 camO, uint32_t px, uint32_t py, uint32_t W, uint32_t H,
+                                             int sample, int aaRow, Payload& p, RayReq& ray) {
+    float pcx = ((float)px + 0.5f) + kAA[aaRow][sample & 7][0];
+    float pcy = ((float)py + 0.5f) + kAA[aaRow][sample & 7][1];
+    float ux = pcx / (float)W, uy = pcy / (float)H;
+    float dx = ux * 2.0f - 1.0f, dy = uy * 2.0f - 1.0f;
+    float tg[4], dw[4];
+    mul4(U.projInverse, dx, dy, 1.0f, 1.0f, tg);
+    V3 tn = normalize(v3(tg[0], tg[1], tg[2]));
+    mul4(U.viewInverse, tn.x, tn.y, tn.z, 0.0f, dw);
+    ray.o = camO;
+    ray.d = v3(dw[0], dw[1], dw[2]);
+    ray.tmin = 0.001f;
+    ray.tmax = 10000.0f;
+    ray.missIndex = 0;
+    ray.masked = false;
+    p.hitValue = v3s(0.0f);
+    p.normal = v3s(0.0f);
+    p.roughRGB = v3s(0.0f);
+    p.roughA = 0.0f;
+    p.depth = 0.0f;
+    p.refDepth = 0.0f;
+    p.curIOR = 1.0f;
+    p.rayType = RT_GENERIC;
+    p.recDepth = 0;
+    p.reflectContribution = 0.0f;
+}
+
+#ifndef RG_TRACE_STEPS
+#define RG_TRACE_STEPS 4
+#endif
+#ifndef RG_SHADE_THRESHOLD
+#define RG_SHADE_THRESHOLD 16
+#endif
+enum : int { kIdle = 0, kTraverse = 1, kResult = 2 };
+
+// starts the traversal of the pending trace; mask-0 traces and zero directions need none
+__device__ __forceinline__ int begin_ray(Trav& T, const DevScene& sc, const RayReq& ray) {
+    if (ray.masked) {
+        T.h.hit = false;
+        T.active = false;
+        return kResult;
+    }
+    trav_begin(T, sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax);
+    return T.active ? kTraverse : kResult;
+}
+
+constexpr int kTileW = 8, kTileH = 4;  // 32 pixels of one work tile
+
+// Persistent kernel: each lane takes (pixel, sample) work items from a global counter -- in
+// warp-aggregated batches -- and runs the sample's whole depth-first trace sequence.  Traversal is
+// resumable: every loop iteration advances each lane's ray by up to RG_TRACE_STEPS nodes, and a
+// lane whose ray finished shades it and starts its next ray (or takes the next work item) while
+// the other lanes keep traversing, so no lane idles behind the longest ray of its warp.  Work items
+// enumerate 8x4 pixel tiles, then pixels, then samples, so consecutive items are coherent.
+// Each sample's payload sums go to `samples` (12 floats); k_resolve averages them in sample order.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_trace(const TraceParams P) {
-    const uint32_t px = blockIdx.x * 16 + (threadIdx.x & 15);
-    const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 4);
-    if (px >= P.W || py >= P.H) return;
+__global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(const TraceParams P) {
+    RG_DECLARE_STACK(stk);
     const DevScene& sc = P.scene;
     const rg_ubo& U = P.ubo;
     const V3 L = v3(U.lightDir[0], U.lightDir[1], U.lightDir[2]);
     const int maxRec = U.maxRecursions;
-    const int S = U.numSamples;
-    const int aaRow = S < 8 ? S : 8;
-
-    unsigned long long nPrimary = 0, nShadow = 0, nSecondary = 0, nMasked = 0;
-    VisitCounts vc = {0, 0, 0};
+    const uint32_t S = (uint32_t)U.numSamples;
+    const int aaRow = S < 8 ? (int)S : 8;
+    const uint32_t tilesX = (P.W + kTileW - 1) / kTileW, tilesY = (P.H + kTileH - 1) / kTileH;
+    const uint32_t total = tilesX * tilesY * (kTileW * kTileH) * S;
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned ltmask = (1u << lane) - 1u;
 
     float org[4];
     mul4(U.viewInverse, 0.0f, 0.0f, 0.0f, 1.0f, org);
     const V3 camO = v3(org[0], org[1], org[2]);
 
-    V3 accColor = v3s(0.0f), accNormal = v3s(0.0f), accRough = v3s(0.0f);
-    float accRoughA = 0.0f, accReflect = 0.0f, accDepth = 0.0f;
-
-    Frame stack[kMaxFrames];
+    RayCounts cnt = {0, 0, 0, 0};
+    VisitCounts vc = {0, 0, 0};
+    Frame frames[kMaxFrames];
     int fsp = 0;
     Payload p;
     RayReq ray;
     Frame cur;
+    Trav T;
+    T.active = false;
+    bool alive = true;
+    int state = kIdle;
+    uint32_t px = 0, py = 0, sample = 0;
 
-    for (int sample = 0; sample < S; ++sample) {
-        // raygen.h:84-102 -- camera ray of this sample, payload initialisation
-        {
-            float pcx = ((float)px + 0.5f) + kAA[aaRow][sample & 7][0];
-            float pcy = ((float)py + 0.5f) + kAA[aaRow][sample & 7][1];
-            float ux = pcx / (float)P.W, uy = pcy / (float)P.H;
-            float dx = ux * 2.0f - 1.0f, dy = uy * 2.0f - 1.0f;
-            float tg[4], dw[4];
-            mul4(U.projInverse, dx, dy, 1.0f, 1.0f, tg);
-            V3 tn = normalize(v3(tg[0], tg[1], tg[2]));
-            mul4(U.viewInverse, tn.x, tn.y, tn.z, 0.0f, dw);
-            ray.o = camO;
-            ray.d = v3(dw[0], dw[1], dw[2]);
-            ray.tmin = 0.001f;
-            ray.tmax = 10000.0f;
-            ray.missIndex = 0;
-            ray.masked = false;
-            p.hitValue = v3s(0.0f);
-            p.normal = v3s(0.0f);
-            p.roughRGB = v3s(0.0f);
-            p.roughA = 0.0f;
-            p.depth = 0.0f;
-            p.refDepth = 0.0f;
-            p.curIOR = 1.0f;
-            p.rayType = RT_GENERIC;
-            p.recDepth = 0;
-            p.reflectContribution = 0.0f;
-            nPrimary++;
-        }
-        for (;;) {
-            // ---- traceRayEXT ----
-            Hit h;
-            h.hit = false;
-            if (!ray.masked) h = closest_hit<COUNT>(sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, vc);
-            int ph;
-            if (!h.hit) {
-                if (ray.missIndex == 0) sky(p, ray.d, L);
-                else p.hitValue = v3s(1.0f);  // shadowMiss.rmiss:30-34
-                ph = PH_RETURN;
-            } else {
-                ph = PH_HIT;
+    for (;;) {
+        // A shading round runs when at least RG_SHADE_THRESHOLD lanes of the warp wait (finished ray
+        // or no work) or no lane is traversing: the waiting lanes shade together, idle lanes take new
+        // work items (one atomic per warp), then every lane with a ray continues traversing.
+        const unsigned travMask = __ballot_sync(0xFFFFFFFFu, state == kTraverse);
+        const unsigned waitMask = __ballot_sync(0xFFFFFFFFu, state == kResult || (alive && state == kIdle));
+        if (travMask == 0 || __popc(waitMask) >= RG_SHADE_THRESHOLD) {
+            if (state == kResult) {
+                // closest-hit / miss shading of the finished trace, up to the next trace
+                if (shade_step(sc, L, maxRec, T.h, p, ray, frames, fsp, cur, cnt)) {
+                    state = begin_ray(T, sc, ray);
+                } else {
+                    float4* o = P.samples + 3 * ((size_t)(py * P.W + px) * S + sample);
+                    o[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
+                    o[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
+                    o[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
+                    state = kIdle;
+                }
             }
-            bool newRay = false;
-            V3 refractColor = v3s(1.0f);
-            while (!newRay) {
-                if (ph == PH_HIT) {
-                    // closesthit.rchit:95-122 -- fetch, world position, world normal, grid effect
-                    const DevInstance* in = sc.inst + h.inst;
-                    const uint32_t vOff = __ldg(&in->vOff), iOff = __ldg(&in->iOff), mOff = __ldg(&in->mOff);
-                    const float4 m0 = __ldg(&in->m[0]), m1 = __ldg(&in->m[1]), m2 = __ldg(&in->m[2]);
-                    const float hitT = h.t;
-                    const float bx = (1.0f - h.u) - h.v, by = h.u, bz = h.v;
-                    const uint32_t ib = iOff + 3 * h.prim;
-                    const rg_vertex* v0 = sc.vertices + vOff + __ldg(sc.indices + ib);
-                    const rg_vertex* v1 = sc.vertices + vOff + __ldg(sc.indices + ib + 1);
-                    const rg_vertex* v2 = sc.vertices + vOff + __ldg(sc.indices + ib + 2);
-                    const uint32_t matIndex = __ldg(&v0->matIndex);
-                    V3 n0 = v3(__ldg(&v0->normal[0]), __ldg(&v0->normal[1]), __ldg(&v0->normal[2]));
-                    V3 n1 = v3(__ldg(&v1->normal[0]), __ldg(&v1->normal[1]), __ldg(&v1->normal[2]));
-                    V3 n2 = v3(__ldg(&v2->normal[0]), __ldg(&v2->normal[1]), __ldg(&v2->normal[2]));
-                    const rg_material* M = sc.materials + mOff + matIndex;
-                    cur.diffuse = v3(__ldg(&M->diffuse[0]), __ldg(&M->diffuse[1]), __ldg(&M->diffuse[2]));
-                    cur.specular = v3(__ldg(&M->specular[0]), __ldg(&M->specular[1]), __ldg(&M->specular[2]));
-                    cur.transparency = __ldg(&M->transparency);
-                    cur.reflectivity = __ldg(&M->reflectivity);
-                    cur.roughness = __ldg(&M->roughness);
-                    cur.ior = __ldg(&M->ior);
-                    cur.emission = __ldg(&M->emission);
-                    cur.rayConsumption = (int)__ldg(&M->rayConsumption);
-                    const uint32_t effectId = __ldg(&M->effectId);
-                    cur.origin = ray.o + ray.d * hitT;
-                    cur.D = ray.d;
-                    cur.t = hitT;
-                    V3 vn = (n0 * bx + n1 * by) + n2 * bz;
-                    V3 wn = v3((m0.x * vn.x + m0.y * vn.y) + m0.z * vn.z, (m1.x * vn.x + m1.y * vn.y) + m1.z * vn.z,
-                               (m2.x * vn.x + m2.y * vn.y) + m2.z * vn.z);
-                    cur.n = normalize(wn);
-                    if (effectId == 1) {  // gridEffect, closesthit.rchit:74-91
-                        V3 pos = cur.origin;
-                        float aa = ((p.refDepth + hitT) + 8.0f) / 30.0f;
-                        float aa2 = aa / 2.0f;
-                        float minmod = fminf(fabsf(glsl_mod((pos.x + 1000.0f) * 10.0f + aa2, 20.0f) - aa2),
-                                             fabsf(glsl_mod((pos.z + 1000.0f) * 10.0f + aa2, 20.0f) - aa2));
-                        if (minmod < aa2) {
-                            float aa_sq = aa * aa;
-                            minmod = minmod - (aa2 - aa_sq / 3.0f);
-                            minmod = minmod * (3.0f / aa_sq);
-                            float f = mixs(aa / 10.0f, 1.0f, minmod);
-                            cur.diffuse = cur.diffuse * f;
-                            cur.specular = cur.specular * f;
-                            cur.reflectivity = cur.reflectivity * f;
-                        }
-                        if (glsl_mod((pos.x + 1000.0f) * 5.0f, 20.0f) < 10.0f && glsl_mod((pos.z + 1000.0f) * 5.0f, 20.0f) < 10.0f)
-                            cur.reflectivity = cur.reflectivity * 1.5f;
-                    }
-                    if (p.rayType == RT_SHADOW_INTERNAL) {  // :125-152
-                        float thick = clampf(hitT * (1.0f - cur.transparency) * 10.0f, 0.0f, 1.0f);
-                        V3 shadowCol = p.hitValue - mix(v3s(0.0f), normalize(v3s(1.1f) - cur.diffuse) + v3s(0.1f), thick);
-                        if (p.recDepth < maxRec) {
-                            p.rayType = RT_SHADOW_TRACE;
-                            p.recDepth++;
-                            nShadow++;
-                            cur.base = shadowCol;
-                            cur.kind = R_SI_A;
-                            stack[fsp++] = cur;
-                            ray.o = cur.origin; ray.d = cur.D; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = false;
-                            newRay = true;
-                        } else {
-                            p.hitValue = shadowCol * 0.4f;
-                            ph = PH_RETURN;
-                        }
-                    } else if (p.rayType == RT_SHADOW_TRACE) {  // :153-166
-                        if (cur.transparency > 0.0f) {
-                            if (p.recDepth < maxRec) {
-                                p.rayType = RT_SHADOW_INTERNAL;
-                                p.recDepth++;
-                                nShadow++;
-                                cur.kind = R_ST_C;
-                                stack[fsp++] = cur;
-                                ray.o = cur.origin; ray.d = cur.D; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 1; ray.masked = false;
-                                newRay = true;
-                            } else {
-                                ph = PH_RETURN;
-                            }
-                        } else {
-                            float f = mixs(0.4f, 0.8f, clampf(logf(hitT) / 8.0f, 0.0f, 1.0f));
-                            p.hitValue = p.hitValue * f;
-                            ph = PH_RETURN;
-                        }
-                    } else {  // GENERIC, :168-204
-                        cur.front = dot(-cur.D, cur.n) > 0.0f;
-                        if (!cur.front) cur.n = normalize(-cur.n);
-                        float ndl = dot(-L, cur.n);
-                        float dp = fmaxf(ndl, 0.2f);
-                        cur.base = cur.diffuse * dp;
-                        cur.reflectColor = v3s(1.0f);
-                        cur.reflectDepth = 0.0f;
-                        if (ndl > 0.07f) {
-                            if (p.recDepth < maxRec) {
-                                p.hitValue = v3s(1.0f);
-                                p.rayType = RT_SHADOW_TRACE;
-                                p.recDepth++;
-                                nShadow++;
-                                cur.kind = R_G_SHADOW;
-                                stack[fsp++] = cur;
-                                ray.o = cur.origin; ray.d = -L; ray.tmin = 0.01f * 10.0f; ray.tmax = 1000.0f; ray.missIndex = 1; ray.masked = false;
-                                newRay = true;
-                            } else {
-                                cur.shadow = v3s(1.0f);
-                                ph = PH_G_REFLECT;
-                            }
-                        } else {
-                            float tr = cur.transparency;
-                            float sm = tr * tr;
-                            cur.shadow = tr < 1.0f ? mix(v3s(1.0f), cur.diffuse * sm, tr) : v3s(0.4f);
-                            ph = PH_G_REFLECT;
-                        }
-                    }
-                } else if (ph == PH_G_REFLECT) {  // :206-221
-                    if (p.recDepth < maxRec && cur.reflectivity > 0.0f) {
-                        V3 dir = reflect(cur.D, cur.n);
-                        p.recDepth += cur.rayConsumption;
-                        p.refDepth = p.refDepth + cur.t;
-                        nSecondary++;
-                        cur.kind = R_G_REFLECT;
-                        stack[fsp++] = cur;
-                        ray.o = cur.origin; ray.d = dir; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = false;
-                        newRay = true;
+            const bool need = alive && state == kIdle;
+            const unsigned needMask = __ballot_sync(0xFFFFFFFFu, need);
+            if (needMask) {
+                const int leader = __ffs(needMask) - 1;
+                uint32_t base = 0;
+                if ((int)lane == leader) base = atomicAdd(P.workCounter, (uint32_t)__popc(needMask));
+                base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                if (need) {
+                    const uint32_t id = base + (uint32_t)__popc(needMask & ltmask);
+                    if (id >= total) {
+                        alive = false;
                     } else {
-                        ph = PH_G_REFRACT;
-                    }
-                } else if (ph == PH_G_REFRACT) {  // :223-251
-                    if (p.recDepth < maxRec && cur.transparency > 0.0f) {
-                        V3 dir;
-                        if (cur.front) {
-                            float eta = p.curIOR / cur.ior;
-                            dir = refract(cur.D, cur.n, eta);
-                            p.curIOR = cur.ior;
-                            cur.kind = R_G_REFR_F;
-                        } else {
-                            float eta = cur.ior / 1.0f;
-                            dir = refract(cur.D, cur.n, eta);
-                            p.curIOR = 1.0f;
-                            cur.kind = R_G_REFR_B;
+                        sample = id % S;
+                        const uint32_t pid = id / S, tile = pid / (kTileW * kTileH), within = pid % (kTileW * kTileH);
+                        px = (tile % tilesX) * kTileW + within % kTileW;
+                        py = (tile / tilesX) * kTileH + within / kTileW;
+                        if (px < P.W && py < P.H) {
+                            start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray);
+                            cnt.primary++;
+                            fsp = 0;
+                            state = begin_ray(T, sc, ray);
                         }
-                        p.recDepth++;
-                        nSecondary++;
-                        stack[fsp++] = cur;
-                        ray.o = cur.origin; ray.d = dir; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = false;
-                        newRay = true;
-                    } else {
-                        refractColor = v3s(1.0f);
-                        ph = PH_G_COMPOSE;
-                    }
-                } else if (ph == PH_G_COMPOSE) {  // :253-267
-                    V3 baseColor = cur.base * cur.shadow;
-                    baseColor = baseColor + cur.diffuse * cur.emission;
-                    float total = fmaxf(cur.transparency, cur.reflectivity);
-                    float den = cur.transparency + cur.reflectivity;
-                    float w = den == 0.0f ? 0.0f : cur.reflectivity / den;
-                    V3 roughCol = mix(refractColor, cur.reflectColor, w);
-                    p.hitValue = mix(baseColor, roughCol, total);
-                    if (p.recDepth == 0) {
-                        p.hitValue = baseColor;
-                        p.normal = cur.n;
-                        p.roughRGB = roughCol;
-                        p.roughA = fminf((cur.reflectDepth / 50.0f) * cur.roughness, cur.roughness / 2.1f);
-                        p.reflectContribution = total;
-                    }
-                    p.depth = cur.t;
-                    ph = PH_RETURN;
-                } else {  // PH_RETURN: resume the paused invocation
-                    if (fsp == 0) break;
-                    cur = stack[--fsp];
-                    switch (cur.kind) {
-                        case R_G_SHADOW:
-                            p.recDepth--;
-                            cur.shadow = p.hitValue;
-                            p.rayType = RT_GENERIC;
-                            ph = PH_G_REFLECT;
-                            break;
-                        case R_G_REFLECT:
-                            p.recDepth -= cur.rayConsumption;
-                            cur.reflectColor = p.hitValue * cur.specular;
-                            cur.reflectDepth = p.depth;
-                            ph = PH_G_REFRACT;
-                            break;
-                        case R_G_REFR_F:
-                            p.recDepth--;
-                            refractColor = p.hitValue;
-                            ph = PH_G_COMPOSE;
-                            break;
-                        case R_G_REFR_B:
-                            p.recDepth--;
-                            refractColor = mix(v3s(1.0f), cur.diffuse, logf(1.0f + cur.t)) * p.hitValue;
-                            ph = PH_G_COMPOSE;
-                            break;
-                        case R_SI_A:
-                            p.recDepth--;
-                            if (p.depth < 1000.0f) {
-                                p.hitValue = p.hitValue * cur.base;
-                                ph = PH_RETURN;
-                            } else {
-                                float eta = cur.ior / 1.0f;
-                                V3 dir = refract(cur.D, cur.n, eta);
-                                float x = dot(L, dir);
-                                float dp = x * x * x * x * x + 0.75f;
-                                cur.base = cur.base * dp;
-                                cur.kind = R_SI_B;
-                                stack[fsp++] = cur;
-                                nMasked++;
-                                ray.o = cur.origin; ray.d = -dir; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = true;
-                                newRay = true;
-                            }
-                            break;
-                        case R_SI_B:
-                            p.hitValue = cur.base + p.hitValue * 0.1f;
-                            ph = PH_RETURN;
-                            break;
-                        default:  // R_ST_C
-                            p.recDepth--;
-                            ph = PH_RETURN;
-                            break;
                     }
                 }
             }
-            if (!newRay) break;  // sample finished
+            if (!__any_sync(0xFFFFFFFFu, alive)) break;
         }
-        accColor = accColor + p.hitValue;
-        accNormal = accNormal + p.normal;
-        accRough = accRough + p.roughRGB;
-        accRoughA = accRoughA + p.roughA;
-        accReflect = accReflect + p.reflectContribution;
-        accDepth = accDepth + p.depth;
+        if (state == kTraverse) {
+#pragma unroll 1
+            for (int k = 0; k < RG_TRACE_STEPS; ++k) {
+                trav_step<COUNT>(T, sc, stk, vc);
+                if (!T.active) {
+                    state = kResult;
+                    break;
+                }
+            }
+        }
     }
-    const float fs = (float)S;
-    const size_t pix = (size_t)py * P.W + px;
-    P.base[pix] = pack_half4(accColor.x / fs, accColor.y / fs, accColor.z / fs, accReflect / fs);
-    P.normal[pix] = pack_half4(accNormal.x / fs, accNormal.y / fs, accNormal.z / fs, (logf(accDepth) * 0.25f) / fs);
-    P.rough[pix] = pack_half4(accRough.x / fs, accRough.y / fs, accRough.z / fs, accRoughA / fs);
 
-    // ray statistics: warp reduction then one atomic per warp
-    unsigned long long c[7] = {nPrimary, nShadow, nSecondary, nMasked, vc.nodes, vc.tris, vc.overflow};
-    const unsigned mask = __activemask();
+    // ray statistics: warp reduction then one atomic per warp (all lanes are here)
+    unsigned long long c[7] = {cnt.primary, cnt.shadow, cnt.secondary, cnt.masked, vc.nodes, vc.tris, vc.overflow};
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
         unsigned long long v = c[k];
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(mask, v, off);
-        c[k] = v;
-    }
-    // with a partial warp the xor-reduction is incomplete; fall back to per-thread atomics then
-    if (mask == 0xFFFFFFFFu) {
-        if ((threadIdx.x & 31) == 0)
-            for (int k = 0; k < 7; ++k)
-                if (c[k]) {
-                    atomicAdd(P.counters + k, c[k]);
-                    atomicAdd(P.counters + 8 + k, c[k]);
-                }
-    } else {
-        unsigned long long own[7] = {nPrimary, nShadow, nSecondary, nMasked, vc.nodes, vc.tris, vc.overflow};
-        for (int k = 0; k < 7; ++k)
-            if (own[k]) {
-                atomicAdd(P.counters + k, own[k]);
-                atomicAdd(P.counters + 8 + k, own[k]);
-            }
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+        if (lane == 0 && v) {
+            atomicAdd(P.counters + k, v);
+            atomicAdd(P.counters + 8 + k, v);
+        }
     }
 }
 
-__global__ void k_trace_rays(const DevScene sc, const float* __restrict__ rays, uint32_t n, float* __restrict__ tuv, uint32_t* __restrict__ ids) {
+// raygen.h:116 + raygen.rgen:36-38: average the samples (in sample order) into the three RGBA16F
+// G-buffer images; normal.w = log(sum of depths) * 0.25 / S
+__global__ void k_resolve(const TraceParams P) {
+    const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= P.W || y >= P.H) return;
+    const uint32_t S = (uint32_t)P.ubo.numSamples;
+    const size_t pix = (size_t)y * P.W + x;
+    const float4* s = P.samples + 3 * pix * S;
+    float4 a = s[0], b = s[1], c = s[2];
+    for (uint32_t k = 1; k < S; ++k) {
+        const float4 a2 = s[3 * k], b2 = s[3 * k + 1], c2 = s[3 * k + 2];
+        a.x = a.x + a2.x; a.y = a.y + a2.y; a.z = a.z + a2.z; a.w = a.w + a2.w;
+        b.x = b.x + b2.x; b.y = b.y + b2.y; b.z = b.z + b2.z; b.w = b.w + b2.w;
+        c.x = c.x + c2.x; c.y = c.y + c2.y; c.z = c.z + c2.z; c.w = c.w + c2.w;
+    }
+    const float fs = (float)S;
+    P.base[pix] = pack_half4(a.x / fs, a.y / fs, a.z / fs, a.w / fs);
+    P.normal[pix] = pack_half4(b.x / fs, b.y / fs, b.z / fs, (logf(b.w) * 0.25f) / fs);
+    P.rough[pix] = pack_half4(c.x / fs, c.y / fs, c.z / fs, c.w / fs);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Wavefront form of the same path: every (pixel, sample) is a path with exactly one outstanding
+// ray at a time (the reference's recursion is depth-first on one payload), so a frame is a loop of
+// (trace all pending rays, shade all their results).  The trace kernel only traverses: few
+// registers, high occupancy, dynamic ray fetch.  The shade kernel runs the same state machine as
+// the megakernel on the path's payload and frame stack, which live in device memory between the
+// two kernels, and appends each path's next ray to the other queue.
+
+struct PathMeta {
+    int fsp, missIndex;
+};
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, want);
+    if (!mask) return 0;
+    const unsigned lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void store_payload(float4* dst, const Payload& p) {
+    dst[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
+    dst[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
+    dst[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
+    dst[3] = make_float4(p.curIOR, p.refDepth, __int_as_float(p.rayType), __int_as_float(p.recDepth));
+}
+
+__device__ __forceinline__ void load_payload(const float4* src, Payload& p) {
+    const float4 a = src[0], b = src[1], c = src[2], d = src[3];
+    p.hitValue = v3(a.x, a.y, a.z);
+    p.reflectContribution = a.w;
+    p.normal = v3(b.x, b.y, b.z);
+    p.depth = b.w;
+    p.roughRGB = v3(c.x, c.y, c.z);
+    p.roughA = c.w;
+    p.curIOR = d.x;
+    p.refDepth = d.y;
+    p.rayType = __float_as_int(d.z);
+    p.recDepth = __float_as_int(d.w);
+}
+
+__device__ __forceinline__ void emit_ray(const WavefrontBuffers& wf, int q, uint32_t pos, uint32_t path, const RayReq& ray) {
+    wf.qO[q][pos] = make_float4(ray.o.x, ray.o.y, ray.o.z, ray.tmin);
+    wf.qD[q][pos] = make_float4(ray.d.x, ray.d.y, ray.d.z, ray.tmax);
+    wf.qPath[q][pos] = path;
+}
+
+__device__ __forceinline__ void flush_counts(const TraceParams& P, unsigned long long* c, int n) {
+    const unsigned lane = threadIdx.x & 31;
+    for (int k = 0; k < n; ++k) {
+        unsigned long long v = c[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+        c[k] = v;
+    }
+    if (lane == 0)
+        for (int k = 0; k < n; ++k)
+            if (c[k]) {
+                atomicAdd(P.counters + k, c[k]);
+                atomicAdd(P.counters + 8 + k, c[k]);
+            }
+}
+
+// raygen: one path per (pixel, sample) in 8x4-tile order; primary rays go to queue 0
+__global__ void __launch_bounds__(256) k_wf_raygen(const TraceParams P) {
+    const WavefrontBuffers& wf = P.wf;
+    const rg_ubo& U = P.ubo;
+    const uint32_t S = (uint32_t)U.numSamples;
+    const int aaRow = S < 8 ? (int)S : 8;
+    const uint32_t tilesX = (P.W + kTileW - 1) / kTileW, tilesY = (P.H + kTileH - 1) / kTileH;
+    const uint32_t total = tilesX * tilesY * (kTileW * kTileH) * S;
+    float org[4];
+    mul4(U.viewInverse, 0.0f, 0.0f, 0.0f, 1.0f, org);
+    const V3 camO = v3(org[0], org[1], org[2]);
+    unsigned long long c[4] = {0, 0, 0, 0};
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+        const uint32_t id = base + threadIdx.x;
+        uint32_t px = 0, py = 0, sample = 0;
+        bool valid = false;
+        if (id < total) {
+            sample = id % S;
+            const uint32_t pid = id / S, tile = pid / (kTileW * kTileH), within = pid % (kTileW * kTileH);
+            px = (tile % tilesX) * kTileW + within % kTileW;
+            py = (tile / tilesX) * kTileH + within / kTileW;
+            valid = px < P.W && py < P.H;
+        }
+        const uint32_t pos = warp_append(wf.counts + 0, valid);
+        if (valid) {
+            Payload p;
+            RayReq ray;
+            start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray);
+            const uint32_t path = (py * P.W + px) * S + sample;
+            store_payload(wf.payload + 4 * (size_t)path, p);
+            wf.meta[path] = make_int2(0, 0);
+            emit_ray(wf, 0, pos, path, ray);
+            c[0]++;
+        }
+    }
+    flush_counts(P, c, 1);
+}
+
+// closest hit of every ray of queue q.  Lanes whose ray finished take new rays from the queue (one
+// atomic per warp) as soon as RG_FETCH_THRESHOLD lanes of the warp are idle, so a warp does not wait
+// for its longest ray; between fetches every lane advances its ray by RG_TRACE_STEPS steps.
+#ifndef RG_FETCH_THRESHOLD
+#define RG_FETCH_THRESHOLD 8
+#endif
+#ifndef RG_WF_STEPS
+#define RG_WF_STEPS 8
+#endif
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads, RG_WF_MIN_BLOCKS) k_wf_trace(const TraceParams P, int q) {
+    RG_DECLARE_STACK(stk);
+    const WavefrontBuffers& wf = P.wf;
+    const DevScene& sc = P.scene;
+    const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
+    if (blockIdx.x == 0 && threadIdx.x == 0) wf.counts[q ^ 1] = 0;  // the shade kernel appends there next
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned ltmask = (1u << lane) - 1u;
+    VisitCounts vc = {0, 0, 0};
+    Trav T;
+    T.active = false;
+    uint32_t slot = 0;
+    bool exhausted = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !T.active);
+        if (__popc(idle) >= RG_FETCH_THRESHOLD || idle == 0xFFFFFFFFu) {
+            const bool need = !T.active && !exhausted;
+            const unsigned needMask = __ballot_sync(0xFFFFFFFFu, need);
+            if (needMask) {
+                const int leader = __ffs(needMask) - 1;
+                uint32_t base = 0;
+                if ((int)lane == leader) base = atomicAdd(wf.counts + 2, (uint32_t)__popc(needMask));
+                base = __shfl_sync(0xFFFFFFFFu, base, leader);
+                if (need) {
+                    slot = base + (uint32_t)__popc(needMask & ltmask);
+                    if (slot >= count) {
+                        exhausted = true;
+                    } else {
+                        const float4 o = wf.qO[q][slot], d = wf.qD[q][slot];
+                        trav_begin(T, sc, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w);
+                        if (!T.active) {  // zero direction or the scene box missed
+                            wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
+                            wf.hitInst[slot] = 0xFFFFFFFFu;
+                        }
+                    }
+                }
+            }
+            if (!__any_sync(0xFFFFFFFFu, T.active || !exhausted)) break;
+        }
+        if (T.active) {
+#pragma unroll 1
+            for (int k = 0; k < RG_WF_STEPS; ++k) {
+                trav_step<COUNT>(T, sc, stk, vc);
+                if (!T.active) {
+                    wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
+                    wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;
+                    break;
+                }
+            }
+        }
+    }
+    unsigned long long c[3] = {vc.nodes, vc.tris, vc.overflow};
+    for (int k = 0; k < 3; ++k) {
+        unsigned long long v = c[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+        if (lane == 0 && v) {
+            atomicAdd(P.counters + 4 + k, v);
+            atomicAdd(P.counters + 12 + k, v);
+        }
+    }
+}
+
+// shading of every result of queue q; next rays go to queue q^1, finished samples to P.samples
+__global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
+    const WavefrontBuffers& wf = P.wf;
+    const DevScene& sc = P.scene;
+    const rg_ubo& U = P.ubo;
+    const V3 L = v3(U.lightDir[0], U.lightDir[1], U.lightDir[2]);
+    const int maxRec = U.maxRecursions;
+    const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
+    if (blockIdx.x == 0 && threadIdx.x == 0) wf.counts[2] = 0;  // the next trace kernel's work counter
+    RayCounts cnt = {0, 0, 0, 0};
+    Frame* framesBase = static_cast<Frame*>(wf.frames);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool emit = false;
+        uint32_t path = 0;
+        Payload p;
+        RayReq ray;
+        int fsp = 0;
+        if (i < count) {
+            path = wf.qPath[q][i];
+            const float4 o = wf.qO[q][i], d = wf.qD[q][i];
+            const int2 meta = wf.meta[path];
+            fsp = meta.x;
+            ray.o = v3(o.x, o.y, o.z);
+            ray.tmin = o.w;
+            ray.d = v3(d.x, d.y, d.z);
+            ray.tmax = d.w;
+            ray.missIndex = meta.y;
+            ray.masked = false;
+            load_payload(wf.payload + 4 * (size_t)path, p);
+            const float4 ht = wf.hitTUV[i];
+            Hit h;
+            h.inst = wf.hitInst[i];
+            h.hit = h.inst != 0xFFFFFFFFu;
+            h.t = ht.x;
+            h.u = ht.y;
+            h.v = ht.z;
+            h.prim = __float_as_uint(ht.w);
+            Frame* frames = framesBase + (size_t)path * kMaxFrames;
+            Frame cur;
+            for (;;) {
+                if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) {
+                    float4* so = P.samples + 3 * (size_t)path;
+                    so[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
+                    so[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
+                    so[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
+                    break;
+                }
+                if (ray.masked || (ray.d.x == 0.0f && ray.d.y == 0.0f && ray.d.z == 0.0f)) {
+                    h.hit = false;  // no traversal: the trace's miss shader runs right away
+                    continue;
+                }
+                emit = true;
+                break;
+            }
+        }
+        const uint32_t pos = warp_append(wf.counts + (q ^ 1), emit);
+        if (emit) {
+            emit_ray(wf, q ^ 1, pos, path, ray);
+            store_payload(wf.payload + 4 * (size_t)path, p);
+            wf.meta[path] = make_int2(fsp, ray.missIndex);
+        }
+    }
+    unsigned long long c[3] = {cnt.shadow, cnt.secondary, cnt.masked};
+    const unsigned lane = threadIdx.x & 31;
+    for (int k = 0; k < 3; ++k) {
+        unsigned long long v = c[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+        if (lane == 0 && v) {
+            atomicAdd(P.counters + 1 + k, v);
+            atomicAdd(P.counters + 9 + k, v);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_trace_rays(const DevScene sc, const float* __restrict__ rays, uint32_t n,
+                                                               float* __restrict__ tuv, uint32_t* __restrict__ ids) {
+    RG_DECLARE_STACK(stk);
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const float* r = rays + 8 * (size_t)k;
     VisitCounts vc = {0, 0, 0};
-    Hit h = closest_hit<false>(sc, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], vc);
+    Hit h = closest_hit<false>(sc, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], stk, vc);
     if (h.hit) {
         tuv[3 * k] = h.t; tuv[3 * k + 1] = h.u; tuv[3 * k + 2] = h.v;
         ids[2 * k] = h.inst; ids[2 * k + 1] = h.prim;
@@ -693,9 +1119,70 @@ __global__ void k_trace_rays(const DevScene sc, const float* __restrict__ rays, 
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s) {
-    dim3 grid((p.W + 15) / 16, (p.H + 7) / 8);
-    if (p.countVisits) k_trace<true><<<grid, 128, 0, s>>>(p);
-    else k_trace<false><<<grid, 128, 0, s>>>(p);
+    static int gridBlocks[2] = {0, 0};
+    const int c = p.countVisits ? 1 : 0;
+    if (!gridBlocks[c]) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = c ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace<true>, kTraceThreads, 0)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace<false>, kTraceThreads, 0);
+        if (e != cudaSuccess) return e;
+        gridBlocks[c] = sms * (perSm > 0 ? perSm : 1);
+    }
+    cudaError_t e = cudaMemsetAsync(p.workCounter, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    if (p.countVisits) k_trace<true><<<gridBlocks[c], kTraceThreads, 0, s>>>(p);
+    else k_trace<false><<<gridBlocks[c], kTraceThreads, 0, s>>>(p);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 grid((p.W + 31) / 32, (p.H + 7) / 8);
+    k_resolve<<<grid, 256, 0, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+static int persistent_grid(const void* fn, int threads, int smem) {
+    int dev = 0, sms = 0, perSm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fn, threads, smem) != cudaSuccess) return 0;
+    return sms * (perSm > 0 ? perSm : 1);
+}
+
+cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations) {
+    static int gTrace[2] = {0, 0}, gShade = 0, gRaygen = 0;
+    const int c = p.countVisits ? 1 : 0;
+    if (!gTrace[c]) gTrace[c] = c ? persistent_grid((const void*)k_wf_trace<true>, kTraceThreads, 0)
+                                  : persistent_grid((const void*)k_wf_trace<false>, kTraceThreads, 0);
+    if (!gShade) gShade = persistent_grid((const void*)k_wf_shade, 128, 0);
+    if (!gRaygen) gRaygen = persistent_grid((const void*)k_wf_raygen, 256, 0);
+    if (!gTrace[c] || !gShade || !gRaygen) return cudaErrorUnknown;
+    cudaError_t e = cudaMemsetAsync(p.wf.counts, 0, 4 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    k_wf_raygen<<<gRaygen, 256, 0, s>>>(p);
+    count_launch();
+    int q = 0, it = 0;
+    const int kChunk = 4, kMaxIterations = 100000;
+    for (;;) {
+        for (int k = 0; k < kChunk; ++k, ++it) {
+            if (c) k_wf_trace<true><<<gTrace[c], kTraceThreads, 0, s>>>(p, q);
+            else k_wf_trace<false><<<gTrace[c], kTraceThreads, 0, s>>>(p, q);
+            k_wf_shade<<<gShade, 128, 0, s>>>(p, q);
+            count_launch(2);
+            q ^= 1;
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(hostCount, p.wf.counts + q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        if (*hostCount == 0) break;
+        if (it >= kMaxIterations) return cudaErrorLaunchTimeout;
+    }
+    if (iterations) *iterations = it;
+    dim3 grid((p.W + 31) / 32, (p.H + 7) / 8);
+    k_resolve<<<grid, 256, 0, s>>>(p);
     count_launch();
     return cudaGetLastError();
 }

@@ -21,6 +21,7 @@ ERRORS = {-1: "RG_ERR_INVALID_ARG", -2: "RG_ERR_CUDA", -3: "RG_ERR_OUT_OF_MEMORY
           -5: "RG_ERR_STACK_OVERFLOW", -6: "RG_ERR_BUDGET", -7: "RG_ERR_NO_DEVICE", -8: "RG_ERR_TOO_LARGE"}
 RG_FLAG_DEBUG_IMAGES = 1
 RG_FLAG_COUNT_VISITS = 2
+RG_FLAG_MEGAKERNEL = 4
 IMAGES = {"final": 0, "base": 1, "normal": 2, "rough": 3, "rough_transition": 4, "rough_colors_a": 5,
           "rough_colors_b": 6, "pre_fxaa": 7}
 
@@ -47,7 +48,7 @@ class Timings(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("primary", "shadow", "secondary", "masked", "nodes", "tris",
-                                               "stack_overflows", "pad")]
+                                               "stack_overflows", "iterations")]
 
 
 class RgError(RuntimeError):
@@ -222,12 +223,12 @@ class Context:
     def stats(self) -> dict:
         s = Stats()
         self._ck(self.L.rg_get_stats(self.h, ctypes.byref(s)))
-        return {k: int(getattr(s, k)) for k, _ in Stats._fields_ if k != "pad"}
+        return {k: int(getattr(s, k)) for k, _ in Stats._fields_}
 
     def total_stats(self) -> dict:
         s = Stats()
         self._ck(self.L.rg_get_total_stats(self.h, ctypes.byref(s)))
-        return {k: int(getattr(s, k)) for k, _ in Stats._fields_ if k != "pad"}
+        return {k: int(getattr(s, k)) for k, _ in Stats._fields_}
 
     def reset_total_stats(self):
         self._ck(self.L.rg_reset_total_stats(self.h))

@@ -186,18 +186,15 @@ def torus(major_segments=64, minor_segments=32, R=1.0, r=0.35) -> Mesh:
 
 
 def heightfield(rng: Rng, n=256, disp=0.5) -> Mesh:
-    """n x n grid over [-1,1]^2 (xz) with y ~ U[0, disp]; (n-1)^2*2 triangles.
-
-    Draws n*n uniforms (row-major) for the heights.
-    """
-    xs = np.linspace(-1.0, 1.0, n)
+    """n x n grid with unit cell spacing (x, z in [-(n-1)/2, (n-1)/2]) and heights y ~ U[0, disp];
+    (n-1)^2*2 triangles.  Draws n*n uniforms (row-major) for the heights."""
+    xs = np.arange(n, dtype=np.float64) - (n - 1) / 2.0
     gx, gz = np.meshgrid(xs, xs, indexing="xy")
     gy = rng.uniform(n * n, 0.0, disp).reshape(n, n)
     pos = np.stack([gx, gy, gz], -1).reshape(-1, 3)
     # normals from central differences of the height grid
-    h = (xs[1] - xs[0])
-    dyx = np.gradient(gy, h, axis=1)
-    dyz = np.gradient(gy, h, axis=0)
+    dyx = np.gradient(gy, 1.0, axis=1)
+    dyz = np.gradient(gy, 1.0, axis=0)
     nrm = np.stack([-dyx, np.ones_like(gy), -dyz], -1).reshape(-1, 3)
     nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
     i = np.arange(n - 1)[:, None]
@@ -394,12 +391,12 @@ C1_MESH_COUNTS = (300, 250, 150, 50, 130, 130, 7, 7)
 def instanced_scene(width=1920, height=1080, num_samples=4, max_recursions=5, seed=1,
                     counts=C1_MESH_COUNTS, hf_n=256, ico_levels=(3, 4, 5, 6), name="c1") -> Scene:
     """The two-level game-frame scene: 8 meshes (icospheres subdiv 3..6, two 64x32 tori,
-    two 256x256 heightfields with U[0,0.5] displacement), instanced ``sum(counts)`` times.
+    two 256x256 unit-spaced heightfields with U[0,0.5] displacement), instanced ``sum(counts)`` times.
 
     Draw order: heightfield A heights, heightfield B heights, then per instance (mesh order,
     then instance order): axis (2 draws), angle U[0,2pi), scale U[0.5,2.0], position (3 draws),
-    material (random_materials order). Heightfield instances are terrain tiles laid on a grid
-    instead (scale 24 in xz, 2 in y, no rotation), still drawing the same values.
+    material (random_materials order). Heightfield instances are terrain tiles laid on a 4x4 grid
+    instead (uniform scale to 48 x 48 world units, no rotation), still drawing the same values.
     """
     rng = Rng(seed)
     meshes = [icosphere(s) for s in ico_levels]
@@ -418,10 +415,10 @@ def instanced_scene(width=1920, height=1080, num_samples=4, max_recursions=5, se
             scale = rng.uniform(1, 0.5, 2.0)[0]
             p = np.array([rng.uniform(1, -60, 60)[0], rng.uniform(1, 0.5, 14)[0], rng.uniform(1, -60, 60)[0]])
             mats[k] = random_materials(rng, 1)[0]
-            if mesh_id >= 6:  # terrain tile
+            if mesh_id >= 6:  # terrain tile: uniform scale to a 48 x 48 tile
                 gx, gz = hf_k % 4, hf_k // 4
-                m3 = np.diag([24.0, 2.0, 24.0])
-                p = np.array([-72.0 + 48.0 * gx, -1.0, -72.0 + 48.0 * gz])
+                m3 = np.eye(3) * (48.0 / (hf_n - 1))
+                p = np.array([-72.0 + 48.0 * gx, -0.5, -72.0 + 48.0 * gz])
                 hf_k += 1
                 mats[k] = _material(mats[k]["diffuse"], roughness=float(mats[k]["roughness"]),
                                     reflectivity=0.3, effect_id=1)

@@ -167,17 +167,18 @@ def test_animation_refit_and_tlas_rebuild(rg, orc):
         assert_image_close(fin, orc.post(sc.ubo, ob, on, orr), f"frame {frame}")
 
 
-@pytest.mark.parametrize("spp,depth", [(1, 0), (3, 1), (4, 7), (9, 2)])
-def test_samples_and_depths(rg, orc, spp, depth):
+@pytest.mark.parametrize("spp,depth,mega", [(1, 0, False), (3, 1, False), (4, 7, False), (9, 2, False), (4, 7, True),
+                                            (2, 3, True)])
+def test_samples_and_depths(rg, orc, spp, depth, mega):
     sc = S.spheres_scene(n_spheres=16, width=80, height=45, num_samples=spp, max_recursions=depth, seed=5)
-    rt = rg.Raytracer(sc).prepare()
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_MEGAKERNEL if mega else 0).prepare()
     o = orc.OracleScene(sc)
     fin = rt.render()
     st = rt.ctx.stats()
     ob, on, orr, ost = o.render()
     for k in ("primary", "shadow", "secondary", "masked"):
         assert st[k] == ost[k], (k, st[k], ost[k])
-    assert_image_close(fin, orc.post(sc.ubo, ob, on, orr), f"spp{spp} depth{depth}")
+    assert_image_close(fin, orc.post(sc.ubo, ob, on, orr), f"spp{spp} depth{depth} mega={mega}")
 
 
 def test_errors_are_status_codes(rg):

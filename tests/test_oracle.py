@@ -20,9 +20,8 @@ def numpy_morton(boxes):
     b = boxes.astype(np.float32)
     c = (b[:, :3] + b[:, 3:]) * np.float32(0.5)
     lo, hi = c.min(0), c.max(0)
-    ext = hi - lo
-    with np.errstate(divide="ignore"):
-        inv = np.where(ext > 0, np.float32(1.0) / ext, np.float32(0.0)).astype(np.float32)
+    emax = np.float32((hi - lo).max())
+    inv = np.float32(1.0) / emax if emax > 0 else np.float32(0.0)
     q = ((c - lo) * inv) * np.float32(1024.0)
     q = np.clip(q, np.float32(0), np.float32(1023)).astype(np.uint32)
     return (_expand10(q[:, 0]) << 2) | (_expand10(q[:, 1]) << 1) | _expand10(q[:, 2])
