@@ -41,6 +41,7 @@ typedef struct {
 #define RG_FLAG_DEBUG_IMAGES 1u /* keep roughTransitions / roughColorsA/B for rg_download_image */
 #define RG_FLAG_COUNT_VISITS 2u /* count BVH node / triangle visits (roofline accounting) */
 #define RG_FLAG_MEGAKERNEL 4u   /* trace + shade in one persistent kernel instead of the wavefront loop */
+#define RG_FLAG_KERNEL_TIMING 8u /* CUDA events around every traversal launch (rg_timings.traceKernel) */
 
 /* resources/shaders/vertex.def:3-7 (render/vertex.hpp:27-29): 32 B */
 typedef struct {
@@ -105,6 +106,8 @@ typedef struct {
     float refit;     /* BLAS refits issued before the frame (not in the reference) */
     uint32_t frames; /* frames in the sums below */
     float asBuildSum, rtTotalSum, rtOnlySum, postprocSum, roughSum, refitSum;
+    float traceKernel, traceKernelSum; /* traversal kernels only (RG_FLAG_KERNEL_TIMING), within rtOnly */
+    uint32_t traceLaunches;            /* traversal launches in traceKernelSum */
 } rg_timings;
 
 /* Ray statistics of the last frame. */

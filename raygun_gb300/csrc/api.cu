@@ -38,7 +38,23 @@ enum { EV_AS0, EV_AS1, EV_REFIT0, EV_REFIT1, EV_RT0, EV_POST0, EV_ROUGH1, EV_POS
 struct FrameEvents {
     cudaEvent_t ev[EV_COUNT] = {};
     bool hasAs = false, hasRefit = false, hasFrame = false;
+    std::vector<cudaEvent_t> kernel;  // (start, end) pairs around traversal launches
+    size_t kernelUsed = 0;
 };
+
+// hands out the next (start, end) pair of a frame's traversal-launch events, creating them lazily
+bool next_kernel_events(void* user, cudaEvent_t* a, cudaEvent_t* b) {
+    FrameEvents* f = static_cast<FrameEvents*>(user);
+    while (f->kernel.size() < f->kernelUsed + 2) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return false;
+        f->kernel.push_back(e);
+    }
+    *a = f->kernel[f->kernelUsed];
+    *b = f->kernel[f->kernelUsed + 1];
+    f->kernelUsed += 2;
+    return true;
+}
 
 }  // namespace
 
@@ -222,6 +238,7 @@ rg_status cur_events(rg_ctx* c, FrameEvents** out) {
             c->evCur = f;
         }
         c->evCur->hasAs = c->evCur->hasRefit = c->evCur->hasFrame = false;
+        c->evCur->kernelUsed = 0;
     }
     *out = c->evCur;
     return RG_OK;
@@ -322,6 +339,7 @@ rg_status rg_destroy(rg_ctx* c) {
     for (FrameEvents* f : all) {
         for (auto& e : f->ev)
             if (e) cudaEventDestroy(e);
+        for (auto& e : f->kernel) cudaEventDestroy(e);
         delete f;
     }
     if (c->hostCount) cudaFreeHost(c->hostCount);
@@ -569,7 +587,10 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
         c->lastIterations = 0;
         CK(launch_trace(tp, c->stream));
     }
-    else CK(launch_trace_wavefront(tp, c->stream, c->hostCount, &c->lastIterations));
+    else if (c->flags & RG_FLAG_KERNEL_TIMING)
+        CK(launch_trace_wavefront(tp, c->stream, c->hostCount, &c->lastIterations, next_kernel_events, fe));
+    else
+        CK(launch_trace_wavefront(tp, c->stream, c->hostCount, &c->lastIterations));
     return run_post(c, ubo, fxaa);
 }
 
@@ -661,12 +682,19 @@ rg_status rg_get_timings(rg_ctx* c, rg_timings* t) {
     rg_timings r = c->lastTimings;
     r.frames = 0;
     r.asBuildSum = r.rtTotalSum = r.rtOnlySum = r.postprocSum = r.roughSum = r.refitSum = 0.0f;
+    r.traceKernelSum = 0.0f;
+    r.traceLaunches = 0;
     for (FrameEvents* f : c->evPending) {
         float as = f->hasAs ? el(f->ev[EV_AS0], f->ev[EV_AS1]) : 0.0f;
         float rf = f->hasRefit ? el(f->ev[EV_REFIT0], f->ev[EV_REFIT1]) : 0.0f;
         float rt = el(f->ev[EV_RT0], f->ev[EV_POST0]);
         float ro = el(f->ev[EV_POST0], f->ev[EV_ROUGH1]);
         float po = el(f->ev[EV_POST0], f->ev[EV_POST1]);
+        float tk = 0.0f;
+        for (size_t k = 0; k + 1 < f->kernelUsed; k += 2) tk += el(f->kernel[k], f->kernel[k + 1]);
+        r.traceLaunches += (uint32_t)(f->kernelUsed / 2);
+        r.traceKernel = tk;
+        r.traceKernelSum += tk;
         r.asBuild = as; r.refit = rf; r.rtOnly = rt; r.rough = ro; r.postproc = po; r.rtTotal = rt + po;
         r.asBuildSum += as; r.refitSum += rf; r.rtOnlySum += rt; r.roughSum += ro; r.postprocSum += po; r.rtTotalSum += rt + po;
         r.frames++;

@@ -174,7 +174,11 @@ struct TraceParams {
 };
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
 // hostCount: pinned host word used to poll the queue length; iterations: trace/shade rounds run
-cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations);
+// kernelEvents (nullable): callback that returns a (start, end) event pair to record around each
+// traversal launch
+typedef bool (*EventPairFn)(void* user, cudaEvent_t* start, cudaEvent_t* end);
+cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations,
+                                   EventPairFn kernelEvents = nullptr, void* user = nullptr);
 cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
 
 struct PostParams {

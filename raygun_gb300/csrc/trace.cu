@@ -1152,7 +1152,8 @@ static int persistent_grid(const void* fn, int threads, int smem) {
     return sms * (perSm > 0 ? perSm : 1);
 }
 
-cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations) {
+cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations,
+                                   EventPairFn kernelEvents, void* user) {
     static int gTrace[2] = {0, 0}, gShade = 0, gRaygen = 0;
     const int c = p.countVisits ? 1 : 0;
     if (!gTrace[c]) gTrace[c] = c ? persistent_grid((const void*)k_wf_trace<true>, kTraceThreads, 0)
@@ -1168,8 +1169,12 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
     const int kChunk = 4, kMaxIterations = 100000;
     for (;;) {
         for (int k = 0; k < kChunk; ++k, ++it) {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
+            if (e0) cudaEventRecord(e0, s);
             if (c) k_wf_trace<true><<<gTrace[c], kTraceThreads, 0, s>>>(p, q);
             else k_wf_trace<false><<<gTrace[c], kTraceThreads, 0, s>>>(p, q);
+            if (e1) cudaEventRecord(e1, s);
             k_wf_shade<<<gShade, 128, 0, s>>>(p, q);
             count_launch(2);
             q ^= 1;

@@ -22,6 +22,7 @@ ERRORS = {-1: "RG_ERR_INVALID_ARG", -2: "RG_ERR_CUDA", -3: "RG_ERR_OUT_OF_MEMORY
 RG_FLAG_DEBUG_IMAGES = 1
 RG_FLAG_COUNT_VISITS = 2
 RG_FLAG_MEGAKERNEL = 4
+RG_FLAG_KERNEL_TIMING = 8
 IMAGES = {"final": 0, "base": 1, "normal": 2, "rough": 3, "rough_transition": 4, "rough_colors_a": 5,
           "rough_colors_b": 6, "pre_fxaa": 7}
 
@@ -43,7 +44,8 @@ class Timings(ctypes.Structure):
     _fields_ = ([(k, ctypes.c_float) for k in ("asBuild", "rtTotal", "rtOnly", "postproc", "rough", "refit")]
                 + [("frames", ctypes.c_uint32)]
                 + [(k, ctypes.c_float) for k in ("asBuildSum", "rtTotalSum", "rtOnlySum", "postprocSum", "roughSum",
-                                                 "refitSum")])
+                                                 "refitSum", "traceKernel", "traceKernelSum")]
+                + [("traceLaunches", ctypes.c_uint32)])
 
 
 class Stats(ctypes.Structure):
