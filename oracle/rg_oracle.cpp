@@ -3,8 +3,11 @@
 // TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the smoke check and the
 // CPU-baseline leg of the benchmark call it; nothing in the product links or calls it.
 //
-// Parity unpinned: the reference has no tests, golden vectors or fixtures for this path, and its
-// own GPU path needs a Vulkan ray-tracing driver, so this restatement follows the shader source.
+// Pinned to the reference: the reference's own shader sources, compiled as C++ through a GLSL shim
+// (oracle/ref, built from the reference tree), produce the golden fixtures of tests/golden, and this
+// restatement reproduces them bit for bit (G-buffers, debug images, final frame, ray counts).  The
+// BVH, traversal and triangle test are the Vulkan driver's in the reference and have no reference
+// counterpart; both checkers share them from this file.
 //
 // It is a scalar C++ restatement of the reference's per-frame path:
 //   * LBVH over triangle / instance boxes (30-bit Morton, stable sort, Karras 2012 hierarchy,
@@ -29,7 +32,8 @@
 //   P6 RGBA16F stores round to nearest even
 //   P7 equal t -> smaller (instance, primitive)
 //   P8 clamp/min/max follow fminf/fmaxf (a NaN operand yields the other operand)
-//   P9 FXAA bilinear taps are computed in FP32: x = u*W - 0.5, weights (1-f, f), clamp to edge
+//   P9 FXAA taps: a coordinate equal to a texel centre ((i+0.5)/W in FP32) samples that texel,
+//      others are FP32 bilinear x = u*W - 0.5, weights (1-f, f); clamp to edge
 //
 // Built with -ffp-contract=off: every + - * / is a separately rounded IEEE operation, sqrt and /
 // are correctly rounded, so ray geometry is reproducible bit for bit.
@@ -827,7 +831,7 @@ struct Shader {
                 V3<T> dir = refract(WD, n, eta);
                 p.recDepth++;
                 p.curIOR = ior;
-                c.secondary++;
+                if (!(dir.x == T(0) && dir.y == T(0) && dir.z == T(0))) c.secondary++;  // only rays that traverse
                 trace(origin, tmin, dir, tmax, false, 0);
                 p.recDepth--;
                 refractColor = p.hitValue;
@@ -836,7 +840,7 @@ struct Shader {
                 V3<T> dir = refract(WD, n, eta);
                 p.recDepth++;
                 p.curIOR = T(1.0);
-                c.secondary++;
+                if (!(dir.x == T(0) && dir.y == T(0) && dir.z == T(0))) c.secondary++;
                 trace(origin, tmin, dir, tmax, false, 0);
                 p.recDepth--;
                 V3<T> tm = mix(V3<T>(T(1)), diffuse, std::log(T(1) + hitT));
@@ -1020,11 +1024,25 @@ struct Fxaa {
         y = std::min(std::max(y, 0), (int)im.H - 1);
         return im.at(x, y);
     }
-    void bilinear(float u, float v, float* o) const {  // P9
-        float fx = u * (float)im.W - 0.5f, fy = v * (float)im.H - 0.5f;
-        float x0 = std::floor(fx), y0 = std::floor(fy);
-        float ax = fx - x0, ay = fy - y0;
-        int ix = (int)x0, iy = (int)y0;
+    // P9: a coordinate equal to a texel centre as the shader computes it ((i + 0.5) / size in FP32)
+    // samples that texel; any other coordinate is FP32 bilinear x = u*size - 0.5, weights (1-f, f)
+    static void axis(float u, int size, int& i0, float& f) {
+        int c = (int)std::floor(u * (float)size);
+        if (u == ((float)c + 0.5f) / (float)size) {
+            i0 = c;
+            f = 0.0f;
+            return;
+        }
+        float fx = u * (float)size - 0.5f;
+        float x0 = std::floor(fx);
+        f = fx - x0;
+        i0 = (int)x0;
+    }
+    void bilinear(float u, float v, float* o) const {
+        int ix, iy;
+        float ax, ay;
+        axis(u, (int)im.W, ix, ax);
+        axis(v, (int)im.H, iy, ay);
         const float *t00 = texel(ix, iy), *t10 = texel(ix + 1, iy), *t01 = texel(ix, iy + 1), *t11 = texel(ix + 1, iy + 1);
         for (int k = 0; k < 4; ++k) {
             float top = t00[k] * (1.0f - ax) + t10[k] * ax;

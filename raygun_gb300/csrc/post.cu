@@ -180,14 +180,24 @@ struct Tex {
         const __half* h = reinterpret_cast<const __half*>(img + (size_t)y * W + x);
         return __half2float(__ldg(h + 1));
     }
-    // FP32 bilinear, clamp to edge: x = u*W - 0.5, weights (1-f, f)
+    // a coordinate equal to a texel centre ((i + 0.5) / size in FP32) samples that texel, as the
+    // hardware's subtexel grid does; any other coordinate is FP32 bilinear x = u*size - 0.5 with
+    // weights (1-f, f); clamp to edge
+    __device__ __forceinline__ static void axis(float u, int size, int& i0, float& f) {
+        int c = (int)floorf(u * (float)size);
+        if (u == ((float)c + 0.5f) / (float)size) {
+            i0 = c;
+            f = 0.0f;
+            return;
+        }
+        float fx = u * (float)size - 0.5f;
+        float x0 = floorf(fx);
+        f = fx - x0;
+        i0 = (int)x0;
+    }
     __device__ __forceinline__ void coords(float u, float v, int& ix, int& iy, float& ax, float& ay) const {
-        float fx = u * (float)W - 0.5f, fy = v * (float)H - 0.5f;
-        float x0 = floorf(fx), y0 = floorf(fy);
-        ax = fx - x0;
-        ay = fy - y0;
-        ix = (int)x0;
-        iy = (int)y0;
+        axis(u, W, ix, ax);
+        axis(v, H, iy, ay);
     }
     __device__ __forceinline__ float lumaAt(float u, float v) const {
         int ix, iy;

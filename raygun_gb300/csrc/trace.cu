@@ -586,7 +586,7 @@ __device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const
                     cur.kind = R_G_REFR_B;
                 }
                 p.recDepth++;
-                cnt.secondary++;
+                if (!(dir.x == 0.0f && dir.y == 0.0f && dir.z == 0.0f)) cnt.secondary++;  // only rays that traverse
                 frames[fsp++] = cur;
                 ray.o = cur.origin; ray.d = dir; ray.tmin = 0.01f; ray.tmax = 1000.0f; ray.missIndex = 0; ray.masked = false;
                 newRay = true;
