@@ -44,7 +44,32 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= t for f in _inputs())
 
 
+FACADE_SRC = os.path.join(HERE, "host", "raygun.cpp")
+FACADE_LIB = os.path.join(HERE, "librgfacade.so")
+FACADE_HDR = os.path.join(INCLUDE, "rg", "raygun.hpp")
+
+
+def build_facade(force: bool = False) -> str:
+    """The C++ facade (include/rg/raygun.hpp) as librgfacade.so, linked to librgcuda.so."""
+    deps = [FACADE_SRC, FACADE_HDR, os.path.join(INCLUDE, "rgcuda.h"), LIB]
+    if not force and os.path.exists(FACADE_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(FACADE_LIB) for d in deps):
+        return FACADE_LIB
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", INCLUDE, "-o", FACADE_LIB + ".tmp", FACADE_SRC,
+           "-L", HERE, "-lrgcuda", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"facade build failed:\n{r.stderr}")
+    os.replace(FACADE_LIB + ".tmp", FACADE_LIB)
+    return FACADE_LIB
+
+
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
+    lib = _build_cuda(force, verbose, extra_flags)
+    build_facade(force)
+    return lib
+
+
+def _build_cuda(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if not force and up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
