@@ -152,6 +152,12 @@ using TravStack = LocalStack;
 #ifndef RG_WF_MIN_BLOCKS
 #define RG_WF_MIN_BLOCKS 7
 #endif
+#ifndef RG_TAIL_RAYS
+#define RG_TAIL_RAYS 65536
+#endif
+#ifndef RG_POLL_ROUNDS
+#define RG_POLL_ROUNDS 4
+#endif
 
 // Resumable traversal of one ray: trav_begin sets it up, each trav_step processes one node or one
 // leaf (a 4-wide record tests up to four grandchildren of a BVH2 node and descends into the nearest
@@ -1099,6 +1105,60 @@ __global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
     }
 }
 
+// Tail of the wavefront loop: once few paths remain, one launch finishes every remaining path --
+// each thread traces and shades its path's remaining sequence back to back -- instead of one
+// (trace, shade) launch pair per remaining round.
+__global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, int q) {
+    RG_DECLARE_STACK(stk);
+    const WavefrontBuffers& wf = P.wf;
+    const DevScene& sc = P.scene;
+    const rg_ubo& U = P.ubo;
+    const V3 L = v3(U.lightDir[0], U.lightDir[1], U.lightDir[2]);
+    const int maxRec = U.maxRecursions;
+    const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
+    RayCounts cnt = {0, 0, 0, 0};
+    VisitCounts vc = {0, 0, 0};
+    Frame* framesBase = static_cast<Frame*>(wf.frames);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t path = wf.qPath[q][i];
+        const float4 o = wf.qO[q][i], d = wf.qD[q][i];
+        const int2 meta = wf.meta[path];
+        int fsp = meta.x;
+        RayReq ray;
+        ray.o = v3(o.x, o.y, o.z);
+        ray.tmin = o.w;
+        ray.d = v3(d.x, d.y, d.z);
+        ray.tmax = d.w;
+        ray.missIndex = meta.y;
+        ray.masked = false;
+        Payload p;
+        load_payload(wf.payload + 4 * (size_t)path, p);
+        Frame* frames = framesBase + (size_t)path * kMaxFrames;
+        Frame cur;
+        for (;;) {
+            Hit h;
+            h.hit = false;
+            if (!ray.masked) h = closest_hit<false>(sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, stk, vc);
+            if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) break;
+        }
+        float4* so = P.samples + 3 * (size_t)path;
+        so[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
+        so[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
+        so[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
+    }
+    unsigned long long c[6] = {cnt.shadow, cnt.secondary, cnt.masked, vc.nodes, vc.tris, vc.overflow};
+    const int slot[6] = {1, 2, 3, 4, 5, 6};
+    const unsigned lane = threadIdx.x & 31;
+    for (int k = 0; k < 6; ++k) {
+        unsigned long long v = c[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+        if (lane == 0 && v) {
+            atomicAdd(P.counters + slot[k], v);
+            atomicAdd(P.counters + 8 + slot[k], v);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(const DevScene sc, const float* __restrict__ rays, uint32_t n,
                                                                float* __restrict__ tuv, uint32_t* __restrict__ ids) {
     RG_DECLARE_STACK(stk);
@@ -1165,8 +1225,13 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
     if (e != cudaSuccess) return e;
     k_wf_raygen<<<gRaygen, 256, 0, s>>>(p);
     count_launch();
+    static int gTail = 0;
+    if (!gTail) gTail = persistent_grid((const void*)k_wf_tail, kTraceThreads, 0);
+    // the pending-ray count below which the remaining paths finish in one k_wf_tail launch; the
+    // visit-counting build stays in the round loop (the tail kernel does not count visits)
+    const uint32_t tailBelow = c ? 0u : (uint32_t)RG_TAIL_RAYS;
     int q = 0, it = 0;
-    const int kChunk = 4, kMaxIterations = 100000;
+    const int kChunk = RG_POLL_ROUNDS, kMaxIterations = 100000;
     for (;;) {
         for (int k = 0; k < kChunk; ++k, ++it) {
             cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1183,6 +1248,11 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
         if ((e = cudaMemcpyAsync(hostCount, p.wf.counts + q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
         if (*hostCount == 0) break;
+        if (*hostCount < tailBelow) {
+            k_wf_tail<<<gTail, kTraceThreads, 0, s>>>(p, q);
+            count_launch();
+            break;
+        }
         if (it >= kMaxIterations) return cudaErrorLaunchTimeout;
     }
     if (iterations) *iterations = it;
