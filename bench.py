@@ -310,7 +310,7 @@ def run_ours(args):
     peak, peak_src = measured_peak_hbm()
     traffic, traffic_src = trace_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "k_wf_trace (all traversal launches of one frame)",
+                "traffic": traffic, "kernel": "k_wf_trace + k_wf_tail (all traversal launches of one frame; the tail launch also shades)",
                 "launches_per_frame": tm["traceLaunches"] / max(tm["frames"], 1), "peak_source": f"{peak_src} hbm_gbs",
                 "algorithmic_bytes_per_launch": bytes_launch, "bytes_per_ray": bytes_per_ray,
                 "node_visits_per_ray": cst["nodes"] / max(crays, 1), "tri_tests_per_ray": cst["tris"] / max(crays, 1),

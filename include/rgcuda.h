@@ -106,7 +106,8 @@ typedef struct {
     float refit;     /* BLAS refits issued before the frame (not in the reference) */
     uint32_t frames; /* frames in the sums below */
     float asBuildSum, rtTotalSum, rtOnlySum, postprocSum, roughSum, refitSum;
-    float traceKernel, traceKernelSum; /* traversal kernels only (RG_FLAG_KERNEL_TIMING), within rtOnly */
+    float traceKernel, traceKernelSum; /* traversal launches only (RG_FLAG_KERNEL_TIMING), within rtOnly:
+                                          the round loop's k_wf_trace and the tail kernel */
     uint32_t traceLaunches;            /* traversal launches in traceKernelSum */
 } rg_timings;
 

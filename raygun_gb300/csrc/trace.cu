@@ -1249,7 +1249,11 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
         if (*hostCount == 0) break;
         if (*hostCount < tailBelow) {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
+            if (e0) cudaEventRecord(e0, s);
             k_wf_tail<<<gTail, kTraceThreads, 0, s>>>(p, q);
+            if (e1) cudaEventRecord(e1, s);
             count_launch();
             break;
         }
