@@ -63,6 +63,20 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_throughput(rays_local: float, ms_local: float, world: int, device=None):
+    """Whole-job rate of N independent replicas: rays summed over ranks / the slowest rank's time
+    (Mrays/s).  Every rank gets the same value; world == 1 needs no process group."""
+    if world == 1:
+        return rays_local / (ms_local * 1e-3) / 1e6, ms_local
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([rays_local], dtype=torch.float64, device=device)
+    m = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    return float(t.item()) / (float(m.item()) * 1e-3) / 1e6, float(m.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -226,22 +240,6 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum_over_ranks(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        return float(t.item())
-
     # ---------------- value: device-resident inputs ----------------
     ctx.set_flags(rgcuda.RG_FLAG_KERNEL_TIMING)  # events around every traversal launch
     f = 0
@@ -264,12 +262,10 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     launches = rgcuda.launch_count() - launches0
-    ms = max_over_ranks(e0.elapsed_time(e1))
     tot = ctx.total_stats()
     rays = tot["primary"] + tot["shadow"] + tot["secondary"]
     tm = ctx.timings()
-    all_rays = sum_over_ranks(rays)
-    value = all_rays / (ms * 1e-3) / 1e6
+    value, ms = replica_throughput(rays, e0.elapsed_time(e1), world, dev)
 
     ctx.set_flags(0)
 
@@ -288,10 +284,9 @@ def run_ours(args):
         f += 1
     e3.record(ext)
     barrier()
-    ms_e2e = max_over_ranks(e2.elapsed_time(e3))
     tot2 = ctx.total_stats()
-    rays2 = sum_over_ranks(tot2["primary"] + tot2["shadow"] + tot2["secondary"])
-    e2e = {"value": rays2 / (ms_e2e * 1e-3) / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d // K),
+    e2e_value, ms_e2e = replica_throughput(tot2["primary"] + tot2["shadow"] + tot2["secondary"], e2.elapsed_time(e3), world, dev)
+    e2e = {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d // K),
            "d2h_bytes_per_step": sc.height * sc.width * 16, "ms_per_step": ms_e2e / K}
 
     # ---------------- roofline of the trace kernel ----------------

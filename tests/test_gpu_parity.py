@@ -214,3 +214,22 @@ def test_hbm_budget_rejects(rg):
     with pytest.raises(rg.RgError) as e:
         ctx.set_resolution(1920, 1080)
     assert e.value.code == -6
+
+
+def test_material_live_edit(rg, orc):
+    """gpu/gpu_material.cpp:52-94 -> RenderSystem::updateModelBuffers: new material values reach the
+    next frame without touching the BVHs."""
+    sc = S.spheres_scene(n_spheres=10, width=80, height=45, num_samples=1, max_recursions=4, seed=11)
+    rt = rg.Raytracer(sc).prepare()
+    before = rt.render()
+    mats = sc.materials.copy()
+    mats["diffuse"][1:5] = [(1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0), (1.0, 1.0, 0.0)]
+    mats["reflectivity"][5] = 0.95
+    mats["transparency"][6], mats["ior"][6] = 0.98, 1.33
+    rt.ctx.update_materials(0, mats)
+    after = rt.render()
+    sc.materials = mats
+    o = orc.OracleScene(sc)
+    ob, on, orr, _ = o.render()
+    assert_image_close(after, orc.post(sc.ubo, ob, on, orr), "after material edit")
+    assert np.abs(after - before).max() > 0.1
