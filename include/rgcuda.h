@@ -198,6 +198,52 @@ rg_status rg_launch_count(uint64_t* out);
 /* The CUDA stream the context orders its work on (cudaStream_t). */
 rg_status rg_get_stream(rg_ctx* ctx, void** stream);
 
+/* ---- several scenes per context, batched rendering -------------------------------------------
+ * The reference renders one Scene per RenderSystem, whose per-scene GPU state is the model buffers,
+ * the BLASes and the TLAS (render/render_system.cpp:192-223, render/raytracer.cpp:54-85).  A scene
+ * slot is that state; a context holds any number of slots side by side in device memory.  Slot 0
+ * exists from rg_create.  rg_upload_geometry, rg_update_*, rg_build_blas, rg_refit_blas,
+ * rg_build_tlas*, rg_render, rg_trace_rays, rg_bvh_info and rg_instance_inverse act on the
+ * selected slot. */
+rg_status rg_scene_create(rg_ctx* ctx, uint32_t* out_scene);
+rg_status rg_scene_select(rg_ctx* ctx, uint32_t scene);
+/* Frees the slot's device memory.  The selected slot cannot be destroyed. */
+rg_status rg_scene_destroy(rg_ctx* ctx, uint32_t scene);
+/* Device memory held by the slot (model buffers, BLASes, TLAS), in bytes. */
+rg_status rg_scene_bytes(rg_ctx* ctx, uint32_t scene, uint64_t* out_bytes);
+
+/* One render of a batch: RenderSystem::render (render/render_system.cpp:88-162) of the scene in
+ * slot `scene` at width x height with this UBO; fxaa as for rg_render. */
+typedef struct rg_job {
+    uint32_t scene;
+    uint32_t width, height;
+    int32_t fxaa;
+    rg_ubo ubo;
+} rg_job;
+
+/* Launch shape of the batch loop's traversal kernel and the order it takes rays in. */
+enum { RG_SORT_NONE = 0, RG_SORT_OCTANT = 1, RG_SORT_MORTON = 2 };
+typedef struct rg_batch_tune {
+    int32_t threads;      /* block size: 64, 128 or 256 */
+    int32_t stack_depth;  /* traversal stack entries per thread: 16, 24, 32 or 48 */
+    int32_t sort_key;     /* RG_SORT_*: rays sorted per round by direction octant or origin Morton code */
+} rg_batch_tune;
+
+/* Renders every job: one wavefront loop traces the paths of all jobs together (path slots that
+ * finish take the next job's work), then each job's samples are resolved and run through the
+ * roughness, postprocess and FXAA passes into its own RGBA32F image.  Each image equals what
+ * rg_render of that job's scene, resolution and UBO produces.  rg_get_stats then counts the rays
+ * of the whole batch. */
+rg_status rg_render_batch(rg_ctx* ctx, const rg_job* jobs, uint32_t n);
+/* Device pointer of job `job`'s RGBA32F image of the last batch (width*height*4 floats). */
+rg_status rg_batch_framebuffer(rg_ctx* ctx, uint32_t job, float** d_rgba);
+/* Job `job`'s image of the last batch to host memory; waits for the batch. */
+rg_status rg_batch_download(rg_ctx* ctx, uint32_t job, float* host_rgba);
+rg_status rg_set_batch_tune(rg_ctx* ctx, const rg_batch_tune* tune);
+rg_status rg_get_batch_tune(rg_ctx* ctx, rg_batch_tune* out);
+/* Path slots of the batch loop (default 2^23; about 1.6 KB of device memory each). */
+rg_status rg_set_batch_slots(rg_ctx* ctx, uint32_t slots);
+
 /* ---- parity / inspection entry points (no reference counterpart: the Vulkan driver's BVHs are
  * opaque) ---- */
 /* LBVH of a BLAS (blas) or of the TLAS (blas = 0xFFFFFFFF): Morton codes per primitive, sorted

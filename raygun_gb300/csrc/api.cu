@@ -5,6 +5,7 @@
 // allocations, the pipeline and descriptor sets become kernel parameters, image barriers become
 // stream order, and the profiler's timestamp queries (raygun/profiler.cpp:55-105) become CUDA
 // events around the same five ranges.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -62,22 +63,28 @@ namespace rg {
 std::atomic<uint64_t> g_launches{0};
 }
 
+// one scene slot: model buffers, BLASes and TLAS (render_system.cpp:192-223, raytracer.cpp:54-85)
+struct SceneState {
+    DevBuf vertices, indices, materials;
+    uint32_t nv = 0, ni = 0, nm = 0;
+    std::vector<BlasRec> blas;
+    DevBuf blasTable;
+    DevBuf instIn, instDev;
+    BvhSet tlas;
+    uint32_t nInst = 0;
+    bool tlasReady = false;
+};
+
 struct rg_ctx {
     int device = 0;
     uint32_t flags = 0;
     uint64_t budget = 0, allocated = 0;
     cudaStream_t stream = nullptr;
     std::string err;
-    // geometry (render_system.cpp:192-223)
-    DevBuf vertices, indices, materials;
-    uint32_t nv = 0, ni = 0, nm = 0;
-    std::vector<BlasRec> blas;
-    DevBuf blasTable;
-    // TLAS
-    DevBuf instIn, instDev;
-    BvhSet tlas;
-    uint32_t nInst = 0;
-    bool tlasReady = false;
+    // scene slots; sc = the selected one (geometry / BLAS / TLAS calls act on it)
+    std::vector<SceneState*> scenes;
+    SceneState* sc = nullptr;
+    uint32_t scId = 0;
     // shared sort scratch
     DevBuf keysA, keysB, valsA, valsB, blockHist, bounds;
     // images (raytracer.cpp:173-195)
@@ -89,8 +96,15 @@ struct rg_ctx {
     DevBuf samples, workCounter;               // per-sample payload sums, persistent-kernel work counter
     // wavefront path state
     DevBuf wfPayload, wfMeta, wfFrames, wfQO0, wfQO1, wfQD0, wfQD1, wfQP0, wfQP1, wfHitTUV, wfHitInst, wfCounts;
-    uint32_t* hostCount = nullptr;             // pinned word for polling the queue length
+    uint32_t* hostCount = nullptr;             // pinned words for polling the queue length and work counter
     int lastIterations = 0;
+    // batch rendering: job table, per-slot job / sample index, ray-sort scratch, per-job images
+    DevBuf jobTable, slotJob, slotSample, sortKeys, sortPerm, sortHist;
+    DevBuf bBase, bNormal, bRough, bFinal, bFxaa, batchFb;
+    std::vector<size_t> batchOffset;           // per job: first pixel in batchFb
+    std::vector<uint32_t> batchW, batchH;
+    uint32_t batchSlots = 1u << 23;            // path slots of the batch loop (path state ~1.6 KB each)
+    TraceTune tune;
     std::vector<FrameEvents*> evPool, evPending;
     FrameEvents* evCur = nullptr;  // ranges recorded since the last frame
     rg_timings lastTimings{};
@@ -202,14 +216,14 @@ LbvhBuffers buffers(rg_ctx* c, const BvhSet& s) {
 const float* root_box(const BvhSet& s) { return s.n > 1 ? s.nodeBoxes.as<float>() : s.primBoxes.as<float>(); }
 
 rg_status upload_blas_entry(rg_ctx* c, uint32_t b) {
-    BlasRec& r = c->blas[b];
+    BlasRec& r = c->sc->blas[b];
     DevBlas e;
     std::memset(&e, 0, sizeof(e));
     e.nodes = r.bvh.nodes.as<BvhNode>();
     e.wide = r.bvh.wide.as<WideNode>();
     e.tris = r.tris.as<float4>();
     e.n = r.bvh.n;
-    DevBlas* d = c->blasTable.as<DevBlas>() + b;
+    DevBlas* d = c->sc->blasTable.as<DevBlas>() + b;
     CK(cudaMemcpyAsync(d, &e, sizeof(DevBlas), cudaMemcpyHostToDevice, c->stream));
     if (r.bvh.n > 0) CK(cudaMemcpyAsync(d->root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
     return RG_OK;
@@ -244,37 +258,93 @@ rg_status cur_events(rg_ctx* c, FrameEvents** out) {
     return RG_OK;
 }
 
-DevScene scene_of(rg_ctx* c) {
+DevScene scene_of(const SceneState& st) {
     DevScene s;
-    s.blas = c->blasTable.as<DevBlas>();
-    s.inst = c->instDev.as<DevInstance>();
-    s.tlasNodes = c->tlas.nodes.as<BvhNode>();
-    s.tlasWide = c->tlas.wide.as<WideNode>();
-    s.tlasOrder = c->tlas.order.as<uint32_t>();
-    s.tlasN = c->nInst;
+    s.blas = st.blasTable.as<DevBlas>();
+    s.inst = st.instDev.as<DevInstance>();
+    s.tlasNodes = st.tlas.nodes.as<BvhNode>();
+    s.tlasWide = st.tlas.wide.as<WideNode>();
+    s.tlasOrder = st.tlas.order.as<uint32_t>();
+    s.tlasN = st.nInst;
     s.pad = 0;
-    s.tlasRoot = root_box(c->tlas);
-    s.vertices = c->vertices.as<rg_vertex>();
-    s.indices = c->indices.as<uint32_t>();
-    s.materials = c->materials.as<rg_material>();
+    s.tlasRoot = root_box(st.tlas);
+    s.vertices = st.vertices.as<rg_vertex>();
+    s.indices = st.indices.as<uint32_t>();
+    s.materials = st.materials.as<rg_material>();
     return s;
 }
 
 rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
-    c->nInst = n;
-    c->tlasReady = false;
-    TRY(ensure(c, c->instDev, sizeof(DevInstance) * (size_t)(n ? n : 1)));
-    TRY(ensure_bvh(c, c->tlas, n));
+    c->sc->nInst = n;
+    c->sc->tlasReady = false;
+    TRY(ensure(c, c->sc->instDev, sizeof(DevInstance) * (size_t)(n ? n : 1)));
+    TRY(ensure_bvh(c, c->sc->tlas, n));
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
     CK(cudaEventRecord(fe->ev[EV_AS0], c->stream));
-    CK(setup_instances(c->instIn.as<rg_instance>(), n, c->blasTable.as<DevBlas>(), (uint32_t)c->blas.size(),
-                       c->instDev.as<DevInstance>(), c->tlas.primBoxes.as<float>(), c->stream));
-    CK(lbvh_build(buffers(c, c->tlas), c->stream));
-    CK(wide_records(buffers(c, c->tlas), c->tlas.wide.as<WideNode>(), c->stream));
+    CK(setup_instances(c->sc->instIn.as<rg_instance>(), n, c->sc->blasTable.as<DevBlas>(), (uint32_t)c->sc->blas.size(),
+                       c->sc->instDev.as<DevInstance>(), c->sc->tlas.primBoxes.as<float>(), c->stream));
+    CK(lbvh_build(buffers(c, c->sc->tlas), c->stream));
+    CK(wide_records(buffers(c, c->sc->tlas), c->sc->tlas.wide.as<WideNode>(), c->stream));
     CK(cudaEventRecord(fe->ev[EV_AS1], c->stream));
     fe->hasAs = true;
-    c->tlasReady = true;
+    c->sc->tlasReady = true;
+    return RG_OK;
+}
+
+void release_bvh(rg_ctx* c, BvhSet& s) {
+    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags, &s.wide};
+    for (DevBuf* b : bb) release(c, *b);
+}
+
+void release_scene(rg_ctx* c, SceneState& st) {
+    DevBuf* bufs[] = {&st.vertices, &st.indices, &st.materials, &st.blasTable, &st.instIn, &st.instDev};
+    for (DevBuf* b : bufs) release(c, *b);
+    release_bvh(c, st.tlas);
+    for (auto& r : st.blas) {
+        release_bvh(c, r.bvh);
+        release(c, r.tris);
+    }
+    st.blas.clear();
+}
+
+uint64_t scene_bytes(const SceneState& st) {
+    auto bvh = [](const BvhSet& s) {
+        return s.primBoxes.cap + s.morton.cap + s.order.cap + s.left.cap + s.right.cap + s.nodeBoxes.cap + s.nodes.cap +
+               s.parents.cap + s.flags.cap + s.wide.cap;
+    };
+    uint64_t b = st.vertices.cap + st.indices.cap + st.materials.cap + st.blasTable.cap + st.instIn.cap + st.instDev.cap + bvh(st.tlas);
+    for (const auto& r : st.blas) b += bvh(r.bvh) + r.tris.cap;
+    return b;
+}
+
+// path state of the wavefront loop for `paths` path slots
+rg_status ensure_wavefront(rg_ctx* c, size_t paths, WavefrontBuffers& w) {
+    const size_t P = paths ? paths : 1;
+    TRY(ensure(c, c->wfPayload, 64 * P));
+    TRY(ensure(c, c->wfMeta, 8 * P));
+    TRY(ensure(c, c->wfFrames, 144ull * kMaxFrames * P));
+    TRY(ensure(c, c->wfQO0, 16 * P));
+    TRY(ensure(c, c->wfQO1, 16 * P));
+    TRY(ensure(c, c->wfQD0, 16 * P));
+    TRY(ensure(c, c->wfQD1, 16 * P));
+    TRY(ensure(c, c->wfQP0, 4 * P));
+    TRY(ensure(c, c->wfQP1, 4 * P));
+    TRY(ensure(c, c->wfHitTUV, 16 * P));
+    TRY(ensure(c, c->wfHitInst, 4 * P));
+    TRY(ensure(c, c->wfCounts, 16));
+    w.payload = c->wfPayload.as<float4>();
+    w.meta = c->wfMeta.as<int2>();
+    w.frames = c->wfFrames.p;
+    w.qO[0] = c->wfQO0.as<float4>();
+    w.qO[1] = c->wfQO1.as<float4>();
+    w.qD[0] = c->wfQD0.as<float4>();
+    w.qD[1] = c->wfQD1.as<float4>();
+    w.qPath[0] = c->wfQP0.as<uint32_t>();
+    w.qPath[1] = c->wfQP1.as<uint32_t>();
+    w.hitTUV = c->wfHitTUV.as<float4>();
+    w.hitInst = c->wfHitInst.as<uint32_t>();
+    w.counts = c->wfCounts.as<uint32_t>();
     return RG_OK;
 }
 
@@ -301,12 +371,14 @@ rg_status rg_create(rg_ctx** out, const rg_device_opts* opts) {
         delete c;
         return RG_ERR_CUDA;
     }
+    c->scenes.push_back(new SceneState());
+    c->sc = c->scenes[0];
     if (ensure(c, c->counters, 16 * sizeof(unsigned long long)) != RG_OK) {
         delete c;
         return RG_ERR_OUT_OF_MEMORY;
     }
     cudaMemsetAsync(c->counters.p, 0, 128, c->stream);
-    if (cudaHostAlloc(&c->hostCount, sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
+    if (cudaHostAlloc(&c->hostCount, 4 * sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
         rg_destroy(c);
         return RG_ERR_OUT_OF_MEMORY;
     }
@@ -318,21 +390,18 @@ rg_status rg_destroy(rg_ctx* c) {
     if (!c) return RG_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->vertices, &c->indices, &c->materials, &c->blasTable, &c->instIn, &c->instDev, &c->keysA, &c->keysB,
-                      &c->valsA, &c->valsB, &c->blockHist, &c->bounds, &c->base, &c->normal, &c->rough, &c->finalImg,
-                      &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC, &c->tmpD,
-                      &c->samples, &c->workCounter, &c->wfPayload, &c->wfMeta, &c->wfFrames, &c->wfQO0, &c->wfQO1,
-                      &c->wfQD0, &c->wfQD1, &c->wfQP0, &c->wfQP1, &c->wfHitTUV, &c->wfHitInst, &c->wfCounts};
+    DevBuf* bufs[] = {&c->keysA, &c->keysB, &c->valsA, &c->valsB, &c->blockHist, &c->bounds, &c->base, &c->normal, &c->rough,
+                      &c->finalImg, &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC,
+                      &c->tmpD, &c->samples, &c->workCounter, &c->wfPayload, &c->wfMeta, &c->wfFrames, &c->wfQO0, &c->wfQO1,
+                      &c->wfQD0, &c->wfQD1, &c->wfQP0, &c->wfQP1, &c->wfHitTUV, &c->wfHitInst, &c->wfCounts, &c->jobTable,
+                      &c->slotJob, &c->slotSample, &c->sortKeys, &c->sortPerm, &c->sortHist, &c->bBase, &c->bNormal, &c->bRough,
+                      &c->bFinal, &c->bFxaa, &c->batchFb};
     for (DevBuf* b : bufs) release(c, *b);
-    auto relBvh = [&](BvhSet& s) {
-        DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags, &s.wide};
-        for (DevBuf* b : bb) release(c, *b);
-    };
-    relBvh(c->tlas);
-    for (auto& r : c->blas) {
-        relBvh(r.bvh);
-        release(c, r.tris);
-    }
+    for (SceneState* st : c->scenes)
+        if (st) {
+            release_scene(c, *st);
+            delete st;
+        }
     std::vector<FrameEvents*> all = c->evPool;
     all.insert(all.end(), c->evPending.begin(), c->evPending.end());
     if (c->evCur) all.push_back(c->evCur);
@@ -360,92 +429,92 @@ rg_status rg_upload_geometry(rg_ctx* c, const rg_vertex* v, uint32_t nv, const u
     for (uint32_t k = 0; k < ni; ++k)
         if (idx[k] >= nv) return fail(c, RG_ERR_INVALID_ARG, "index " + std::to_string(k) + " out of range");
     TRY(set_device(c));
-    TRY(ensure(c, c->vertices, sizeof(rg_vertex) * (size_t)nv));
-    TRY(ensure(c, c->indices, 4ull * ni));
-    TRY(ensure(c, c->materials, sizeof(rg_material) * (size_t)nm));
-    if (nv) CK(cudaMemcpyAsync(c->vertices.p, v, sizeof(rg_vertex) * (size_t)nv, cudaMemcpyHostToDevice, c->stream));
-    if (ni) CK(cudaMemcpyAsync(c->indices.p, idx, 4ull * ni, cudaMemcpyHostToDevice, c->stream));
-    if (nm) CK(cudaMemcpyAsync(c->materials.p, m, sizeof(rg_material) * (size_t)nm, cudaMemcpyHostToDevice, c->stream));
-    c->nv = nv;
-    c->ni = ni;
-    c->nm = nm;
+    TRY(ensure(c, c->sc->vertices, sizeof(rg_vertex) * (size_t)nv));
+    TRY(ensure(c, c->sc->indices, 4ull * ni));
+    TRY(ensure(c, c->sc->materials, sizeof(rg_material) * (size_t)nm));
+    if (nv) CK(cudaMemcpyAsync(c->sc->vertices.p, v, sizeof(rg_vertex) * (size_t)nv, cudaMemcpyHostToDevice, c->stream));
+    if (ni) CK(cudaMemcpyAsync(c->sc->indices.p, idx, 4ull * ni, cudaMemcpyHostToDevice, c->stream));
+    if (nm) CK(cudaMemcpyAsync(c->sc->materials.p, m, sizeof(rg_material) * (size_t)nm, cudaMemcpyHostToDevice, c->stream));
+    c->sc->nv = nv;
+    c->sc->ni = ni;
+    c->sc->nm = nm;
     return RG_OK;
 }
 
 rg_status rg_update_vertices(rg_ctx* c, uint32_t first, const rg_vertex* v, uint32_t n) {
-    if (!c || (n && !v) || (uint64_t)first + n > c->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
+    if (!c || (n && !v) || (uint64_t)first + n > c->sc->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
     TRY(set_device(c));
-    if (n) CK(cudaMemcpyAsync(c->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    if (n) CK(cudaMemcpyAsync(c->sc->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     return RG_OK;
 }
 
 rg_status rg_update_vertices_device(rg_ctx* c, uint32_t first, const rg_vertex* v, uint32_t n) {
-    if (!c || (n && !v) || (uint64_t)first + n > c->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
+    if (!c || (n && !v) || (uint64_t)first + n > c->sc->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
     TRY(set_device(c));
-    if (n) CK(cudaMemcpyAsync(c->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+    if (n) CK(cudaMemcpyAsync(c->sc->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
     return RG_OK;
 }
 
 rg_status rg_update_materials(rg_ctx* c, uint32_t first, const rg_material* m, uint32_t n) {
-    if (!c || (n && !m) || (uint64_t)first + n > c->nm) return fail(c, RG_ERR_INVALID_ARG, "material range outside the uploaded buffer");
+    if (!c || (n && !m) || (uint64_t)first + n > c->sc->nm) return fail(c, RG_ERR_INVALID_ARG, "material range outside the uploaded buffer");
     for (uint32_t k = 0; k < n; ++k)
         if (m[k].rayConsumption < 1 || m[k].rayConsumption > 5) return fail(c, RG_ERR_INVALID_ARG, "material rayConsumption outside 1..5");
     TRY(set_device(c));
-    if (n) CK(cudaMemcpyAsync(c->materials.as<rg_material>() + first, m, sizeof(rg_material) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    if (n) CK(cudaMemcpyAsync(c->sc->materials.as<rg_material>() + first, m, sizeof(rg_material) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     return RG_OK;
 }
 
 rg_status rg_build_blas(rg_ctx* c, uint32_t vOff, uint32_t iOff, uint32_t triCount, uint32_t* out) {
     if (!c || !out) return RG_ERR_INVALID_ARG;
-    if ((uint64_t)iOff + 3ull * triCount > c->ni) return fail(c, RG_ERR_INVALID_ARG, "triangle range outside the index buffer");
+    if ((uint64_t)iOff + 3ull * triCount > c->sc->ni) return fail(c, RG_ERR_INVALID_ARG, "triangle range outside the index buffer");
     if (triCount >= 0x7FFFFFFFu) return fail(c, RG_ERR_INVALID_ARG, "too many triangles");
     TRY(set_device(c));
     // vertex references of this range must stay inside the vertex buffer (checked on the host copy
     // the caller passed at upload time would be cheaper, but the index buffer lives on the device)
-    uint32_t b = (uint32_t)c->blas.size();
-    c->blas.emplace_back();
-    BlasRec& r = c->blas.back();
+    uint32_t b = (uint32_t)c->sc->blas.size();
+    c->sc->blas.emplace_back();
+    BlasRec& r = c->sc->blas.back();
     r.vOff = vOff;
     r.iOff = iOff;
     TRY(ensure_bvh(c, r.bvh, triCount));
     TRY(ensure(c, r.tris, 48ull * (triCount ? triCount : 1)));
     if (triCount) {
-        CK(tri_boxes(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), vOff, iOff, triCount, r.bvh.primBoxes.as<float>(), c->stream));
+        CK(tri_boxes(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), vOff, iOff, triCount, r.bvh.primBoxes.as<float>(), c->stream));
         CK(lbvh_build(buffers(c, r.bvh), c->stream));
         CK(wide_records(buffers(c, r.bvh), r.bvh.wide.as<WideNode>(), c->stream));
-        CK(tri_records(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), vOff, iOff, r.bvh.order.as<uint32_t>(), triCount,
+        CK(tri_records(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), vOff, iOff, r.bvh.order.as<uint32_t>(), triCount,
                        r.tris.as<float4>(), c->stream));
     }
     // the BLAS table grows; copy the existing entries over
-    DevBuf old = c->blasTable;
-    c->blasTable = DevBuf{};
-    TRY(ensure(c, c->blasTable, sizeof(DevBlas) * c->blas.size()));
+    DevBuf old = c->sc->blasTable;
+    c->sc->blasTable = DevBuf{};
+    TRY(ensure(c, c->sc->blasTable, sizeof(DevBlas) * c->sc->blas.size()));
     if (old.p) {
-        CK(cudaMemcpyAsync(c->blasTable.p, old.p, sizeof(DevBlas) * b, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->sc->blasTable.p, old.p, sizeof(DevBlas) * b, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         release(c, old);
     }
     TRY(upload_blas_entry(c, b));
     *out = b;
-    c->tlasReady = false;  // instances point at the BLAS table, which moved
+    c->sc->tlasReady = false;  // instances point at the BLAS table, which moved
     return RG_OK;
 }
 
 rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
-    if (!c || b >= c->blas.size()) return fail(c, RG_ERR_INVALID_ARG, "unknown BLAS");
+    if (!c || b >= c->sc->blas.size()) return fail(c, RG_ERR_INVALID_ARG, "unknown BLAS");
     TRY(set_device(c));
-    BlasRec& r = c->blas[b];
+    BlasRec& r = c->sc->blas[b];
     uint32_t n = r.bvh.n;
     if (!n) return RG_OK;
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
     if (!fe->hasRefit) CK(cudaEventRecord(fe->ev[EV_REFIT0], c->stream));
-    CK(tri_boxes(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, n, r.bvh.primBoxes.as<float>(), c->stream));
+    CK(tri_boxes(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), r.vOff, r.iOff, n, r.bvh.primBoxes.as<float>(), c->stream));
     CK(lbvh_refit(buffers(c, r.bvh), c->stream));
     CK(wide_records(buffers(c, r.bvh), r.bvh.wide.as<WideNode>(), c->stream));
-    CK(tri_records(c->vertices.as<rg_vertex>(), c->indices.as<uint32_t>(), r.vOff, r.iOff, r.bvh.order.as<uint32_t>(), n,
+    CK(tri_records(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), r.vOff, r.iOff, r.bvh.order.as<uint32_t>(), n,
                    r.tris.as<float4>(), c->stream));
-    CK(cudaMemcpyAsync(c->blasTable.as<DevBlas>()[b].root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->sc->blasTable.as<DevBlas>()[b].root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaEventRecord(fe->ev[EV_REFIT1], c->stream));
     fe->hasRefit = true;
     return RG_OK;
@@ -454,16 +523,16 @@ rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
 rg_status rg_build_tlas(rg_ctx* c, const rg_instance* inst, uint32_t n) {
     if (!c || (n && !inst)) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
-    TRY(ensure(c, c->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
-    if (n) CK(cudaMemcpyAsync(c->instIn.p, inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    TRY(ensure(c, c->sc->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
+    if (n) CK(cudaMemcpyAsync(c->sc->instIn.p, inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     return build_tlas_from_device_instances(c, n);
 }
 
 rg_status rg_build_tlas_device(rg_ctx* c, const rg_instance* d_inst, uint32_t n) {
     if (!c || (n && !d_inst)) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
-    TRY(ensure(c, c->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
-    if (n) CK(cudaMemcpyAsync(c->instIn.p, d_inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+    TRY(ensure(c, c->sc->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
+    if (n) CK(cudaMemcpyAsync(c->sc->instIn.p, d_inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
     return build_tlas_from_device_instances(c, n);
 }
 
@@ -533,13 +602,13 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     if (!c) return RG_ERR_INVALID_ARG;
     TRY(check_ubo(c, ubo));
     if (!c->W) return fail(c, RG_ERR_NOT_READY, "rg_set_resolution was not called");
-    if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS (call rg_build_tlas after the last rg_build_blas)");
+    if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS (call rg_build_tlas after the last rg_build_blas)");
     TRY(set_device(c));
     TRY(ensure(c, c->samples, 48ull * c->W * c->H * (uint32_t)ubo->numSamples));
     TRY(ensure(c, c->workCounter, 16));
     TraceParams tp;
     std::memset(&tp, 0, sizeof(tp));
-    tp.scene = scene_of(c);
+    tp.scene = scene_of(*c->sc);
     tp.ubo = *ubo;
     tp.W = c->W;
     tp.H = c->H;
@@ -551,34 +620,7 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     tp.samples = c->samples.as<float4>();
     tp.workCounter = c->workCounter.as<uint32_t>();
     const bool mega = (c->flags & RG_FLAG_MEGAKERNEL) != 0;
-    if (!mega) {
-        const size_t P = (size_t)c->W * c->H * (uint32_t)ubo->numSamples;
-        TRY(ensure(c, c->wfPayload, 64 * P));
-        TRY(ensure(c, c->wfMeta, 8 * P));
-        TRY(ensure(c, c->wfFrames, 144ull * kMaxFrames * P));
-        TRY(ensure(c, c->wfQO0, 16 * P));
-        TRY(ensure(c, c->wfQO1, 16 * P));
-        TRY(ensure(c, c->wfQD0, 16 * P));
-        TRY(ensure(c, c->wfQD1, 16 * P));
-        TRY(ensure(c, c->wfQP0, 4 * P));
-        TRY(ensure(c, c->wfQP1, 4 * P));
-        TRY(ensure(c, c->wfHitTUV, 16 * P));
-        TRY(ensure(c, c->wfHitInst, 4 * P));
-        TRY(ensure(c, c->wfCounts, 16));
-        WavefrontBuffers& w = tp.wf;
-        w.payload = c->wfPayload.as<float4>();
-        w.meta = c->wfMeta.as<int2>();
-        w.frames = c->wfFrames.p;
-        w.qO[0] = c->wfQO0.as<float4>();
-        w.qO[1] = c->wfQO1.as<float4>();
-        w.qD[0] = c->wfQD0.as<float4>();
-        w.qD[1] = c->wfQD1.as<float4>();
-        w.qPath[0] = c->wfQP0.as<uint32_t>();
-        w.qPath[1] = c->wfQP1.as<uint32_t>();
-        w.hitTUV = c->wfHitTUV.as<float4>();
-        w.hitInst = c->wfHitInst.as<uint32_t>();
-        w.counts = c->wfCounts.as<uint32_t>();
-    }
+    if (!mega) TRY(ensure_wavefront(c, (size_t)c->W * c->H * (uint32_t)ubo->numSamples, tp.wf));
     CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
@@ -774,10 +816,10 @@ rg_status rg_bvh_info(rg_ctx* c, uint32_t b, uint32_t* n_out, uint32_t* morton, 
     if (!c) return RG_ERR_INVALID_ARG;
     const BvhSet* s = nullptr;
     if (b == 0xFFFFFFFFu) {
-        if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
-        s = &c->tlas;
-    } else if (b < c->blas.size()) {
-        s = &c->blas[b].bvh;
+        if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+        s = &c->sc->tlas;
+    } else if (b < c->sc->blas.size()) {
+        s = &c->sc->blas[b].bvh;
     } else {
         return fail(c, RG_ERR_INVALID_ARG, "unknown BLAS");
     }
@@ -788,12 +830,12 @@ rg_status rg_bvh_info(rg_ctx* c, uint32_t b, uint32_t* n_out, uint32_t* morton, 
 
 rg_status rg_instance_inverse(rg_ctx* c, float* out) {
     if (!c || !out) return RG_ERR_INVALID_ARG;
-    if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+    if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
     TRY(set_device(c));
-    std::vector<DevInstance> h(c->nInst);
-    if (c->nInst) CK(cudaMemcpyAsync(h.data(), c->instDev.p, sizeof(DevInstance) * c->nInst, cudaMemcpyDeviceToHost, c->stream));
+    std::vector<DevInstance> h(c->sc->nInst);
+    if (c->sc->nInst) CK(cudaMemcpyAsync(h.data(), c->sc->instDev.p, sizeof(DevInstance) * c->sc->nInst, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    for (uint32_t i = 0; i < c->nInst; ++i)
+    for (uint32_t i = 0; i < c->sc->nInst; ++i)
         for (int r = 0; r < 3; ++r) {
             out[12 * i + 4 * r + 0] = h[i].inv[r].x;
             out[12 * i + 4 * r + 1] = h[i].inv[r].y;
@@ -805,14 +847,14 @@ rg_status rg_instance_inverse(rg_ctx* c, float* out) {
 
 rg_status rg_trace_rays(rg_ctx* c, const float* rays, uint32_t n, float* tuv, uint32_t* ids) {
     if (!c || (n && (!rays || !tuv || !ids))) return RG_ERR_INVALID_ARG;
-    if (!c->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+    if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
     if (!n) return RG_OK;
     TRY(set_device(c));
     TRY(ensure(c, c->tmpA, 32ull * n));
     TRY(ensure(c, c->tmpC, 12ull * n));
     TRY(ensure(c, c->tmpD, 8ull * n));
     CK(cudaMemcpyAsync(c->tmpA.p, rays, 32ull * n, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_trace_rays(scene_of(c), c->tmpA.as<float>(), n, c->tmpC.as<float>(), c->tmpD.as<uint32_t>(), c->stream));
+    CK(launch_trace_rays(scene_of(*c->sc), c->tmpA.as<float>(), n, c->tmpC.as<float>(), c->tmpD.as<uint32_t>(), c->stream));
     CK(cudaMemcpyAsync(tuv, c->tmpC.p, 12ull * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(ids, c->tmpD.p, 8ull * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -835,6 +877,209 @@ rg_status rg_lbvh_build_host(rg_ctx* c, const float* boxes, uint32_t n, uint32_t
     cudaStreamSynchronize(c->stream);
     for (DevBuf* b : bb) release(c, *b);
     return st;
+}
+
+}  // extern "C"
+
+// ---- scene slots and batched rendering ------------------------------------------------------------
+extern "C" {
+
+rg_status rg_scene_create(rg_ctx* c, uint32_t* out) {
+    if (!c || !out) return RG_ERR_INVALID_ARG;
+    for (uint32_t k = 0; k < c->scenes.size(); ++k)
+        if (!c->scenes[k]) {
+            c->scenes[k] = new SceneState();
+            *out = k;
+            return RG_OK;
+        }
+    c->scenes.push_back(new SceneState());
+    *out = (uint32_t)c->scenes.size() - 1;
+    return RG_OK;
+}
+
+rg_status rg_scene_select(rg_ctx* c, uint32_t id) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    if (id >= c->scenes.size() || !c->scenes[id]) return fail(c, RG_ERR_INVALID_ARG, "unknown scene " + std::to_string(id));
+    c->sc = c->scenes[id];
+    c->scId = id;
+    return RG_OK;
+}
+
+rg_status rg_scene_destroy(rg_ctx* c, uint32_t id) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    if (id >= c->scenes.size() || !c->scenes[id]) return fail(c, RG_ERR_INVALID_ARG, "unknown scene " + std::to_string(id));
+    if (id == c->scId) return fail(c, RG_ERR_INVALID_ARG, "the selected scene cannot be destroyed");
+    TRY(set_device(c));
+    CK(cudaStreamSynchronize(c->stream));  // no queued work may still read the slot
+    release_scene(c, *c->scenes[id]);
+    delete c->scenes[id];
+    c->scenes[id] = nullptr;
+    return RG_OK;
+}
+
+rg_status rg_scene_bytes(rg_ctx* c, uint32_t id, uint64_t* out) {
+    if (!c || !out) return RG_ERR_INVALID_ARG;
+    if (id >= c->scenes.size() || !c->scenes[id]) return fail(c, RG_ERR_INVALID_ARG, "unknown scene " + std::to_string(id));
+    *out = scene_bytes(*c->scenes[id]);
+    return RG_OK;
+}
+
+rg_status rg_set_batch_tune(rg_ctx* c, const rg_batch_tune* t) {
+    if (!c || !t) return RG_ERR_INVALID_ARG;
+    TraceTune tt;
+    tt.threads = t->threads;
+    tt.depth = t->stack_depth;
+    tt.sortKey = t->sort_key;
+    if (!tune_supported(tt)) return fail(c, RG_ERR_INVALID_ARG, "unsupported batch tune (threads 64/128/256, depth 16/24/32/48, sort 0..2)");
+    c->tune = tt;
+    return RG_OK;
+}
+
+rg_status rg_get_batch_tune(rg_ctx* c, rg_batch_tune* t) {
+    if (!c || !t) return RG_ERR_INVALID_ARG;
+    t->threads = c->tune.threads;
+    t->stack_depth = c->tune.depth;
+    t->sort_key = c->tune.sortKey;
+    return RG_OK;
+}
+
+rg_status rg_set_batch_slots(rg_ctx* c, uint32_t slots) {
+    if (!c || slots < 1024) return fail(c, RG_ERR_INVALID_ARG, "batch path slots must be >= 1024");
+    c->batchSlots = slots;
+    return RG_OK;
+}
+
+rg_status rg_render_batch(rg_ctx* c, const rg_job* jobs, uint32_t n) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    if (!jobs || n == 0) return fail(c, RG_ERR_INVALID_ARG, "empty batch");
+    std::vector<JobDesc> jd(n);
+    uint64_t work = 0, samples = 0, pixels = 0, maxPixels = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        const rg_job& in = jobs[j];
+        if (in.scene >= c->scenes.size() || !c->scenes[in.scene])
+            return fail(c, RG_ERR_INVALID_ARG, "job " + std::to_string(j) + ": unknown scene");
+        const SceneState& st = *c->scenes[in.scene];
+        if (!st.tlasReady) return fail(c, RG_ERR_NOT_READY, "job " + std::to_string(j) + ": scene has no TLAS");
+        if (in.width == 0 || in.height == 0 || in.width > 16384 || in.height > 16384)
+            return fail(c, RG_ERR_INVALID_ARG, "job " + std::to_string(j) + ": resolution must be 1..16384");
+        TRY(check_ubo(c, &in.ubo));
+        const uint32_t S = (uint32_t)in.ubo.numSamples;
+        const uint32_t tilesX = (in.width + 7) / 8, tilesY = (in.height + 3) / 4;
+        const uint64_t jobWork = (uint64_t)tilesX * tilesY * 32 * S;
+        const uint64_t jobPixels = (uint64_t)in.width * in.height;
+        JobDesc& d = jd[j];
+        std::memset(&d, 0, sizeof(d));
+        d.scene = scene_of(st);
+        d.ubo = in.ubo;
+        d.W = in.width;
+        d.H = in.height;
+        d.S = S;
+        d.tilesX = tilesX;
+        d.workBase = (uint32_t)work;
+        d.workCount = (uint32_t)jobWork;
+        d.sampleBase = (uint32_t)samples;
+        work += jobWork;
+        samples += jobPixels * S;
+        pixels += jobPixels;
+        if (jobPixels > maxPixels) maxPixels = jobPixels;
+        if (work >= (1ull << 31) || samples >= (1ull << 31))
+            return fail(c, RG_ERR_TOO_LARGE, "batch too large: at most 2^31 samples per batch");
+    }
+    TRY(set_device(c));
+    const uint32_t slots = (uint32_t)std::min<uint64_t>(work, c->batchSlots);
+    TraceParams tp;
+    std::memset(&tp, 0, sizeof(tp));
+    TRY(ensure_wavefront(c, slots, tp.wf));
+    TRY(ensure(c, c->samples, 48ull * samples));
+    TRY(ensure(c, c->workCounter, 16));
+    TRY(ensure(c, c->slotJob, 4ull * slots));
+    TRY(ensure(c, c->slotSample, 4ull * slots));
+    TRY(ensure(c, c->jobTable, sizeof(JobDesc) * n));
+    SortScratch sort{};
+    if (c->tune.sortKey != RG_SORT_NONE) {
+        TRY(ensure(c, c->sortKeys, 4ull * slots));
+        TRY(ensure(c, c->sortPerm, 4ull * slots));
+        TRY(ensure(c, c->sortHist, 8192 * 4));
+        sort.keysA = c->sortKeys.as<uint32_t>();
+        sort.valsA = c->sortPerm.as<uint32_t>();
+        sort.hist = c->sortHist.as<uint32_t>();
+    }
+    TRY(ensure(c, c->bBase, 8 * maxPixels));
+    TRY(ensure(c, c->bNormal, 8 * maxPixels));
+    TRY(ensure(c, c->bRough, 8 * maxPixels));
+    TRY(ensure(c, c->bFinal, 8 * maxPixels));
+    TRY(ensure(c, c->bFxaa, 8 * maxPixels));
+    TRY(ensure(c, c->batchFb, 16 * pixels));
+    CK(cudaMemcpyAsync(c->jobTable.p, jd.data(), sizeof(JobDesc) * n, cudaMemcpyHostToDevice, c->stream));
+    tp.counters = c->counters.as<unsigned long long>();
+    tp.countVisits = (c->flags & RG_FLAG_COUNT_VISITS) ? 1 : 0;
+    tp.samples = c->samples.as<float4>();
+    tp.workCounter = c->workCounter.as<uint32_t>();
+    tp.jobs = c->jobTable.as<JobDesc>();
+    tp.njobs = n;
+    tp.totalWork = (uint32_t)work;
+    tp.slots = slots;
+    tp.slotJob = c->slotJob.as<uint32_t>();
+    tp.slotSample = c->slotSample.as<uint32_t>();
+    CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+    FrameEvents* fe;
+    TRY(cur_events(c, &fe));
+    CK(cudaEventRecord(fe->ev[EV_RT0], c->stream));
+    if (c->flags & RG_FLAG_KERNEL_TIMING)
+        CK(launch_trace_batch(tp, c->tune, sort, c->stream, c->hostCount, &c->lastIterations, next_kernel_events, fe));
+    else
+        CK(launch_trace_batch(tp, c->tune, sort, c->stream, c->hostCount, &c->lastIterations));
+    CK(cudaEventRecord(fe->ev[EV_POST0], c->stream));
+    c->batchOffset.assign(n, 0);
+    c->batchW.assign(n, 0);
+    c->batchH.assign(n, 0);
+    size_t off = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        const JobDesc& d = jd[j];
+        CK(launch_resolve_job(c->samples.as<float4>(), d, c->bBase.as<uint2>(), c->bNormal.as<uint2>(), c->bRough.as<uint2>(), c->stream));
+        PostParams pp;
+        std::memset(&pp, 0, sizeof(pp));
+        pp.W = d.W;
+        pp.H = d.H;
+        pp.base = c->bBase.as<uint2>();
+        pp.normal = c->bNormal.as<uint2>();
+        pp.rough = c->bRough.as<uint2>();
+        pp.finalImg = c->bFinal.as<uint2>();
+        pp.fxaaOut = c->bFxaa.as<uint2>();
+        pp.framebuffer = c->batchFb.as<float4>() + off;
+        for (int k = 0; k < 4; ++k) pp.fade[k] = d.ubo.fadeColor[k];
+        pp.showAlpha = d.ubo.showAlpha ? 1 : 0;
+        pp.fxaa = jobs[j].fxaa ? 1 : 0;
+        CK(launch_rough_post(pp, c->stream));
+        CK(launch_fxaa(pp, c->stream));
+        c->batchOffset[j] = off;
+        c->batchW[j] = d.W;
+        c->batchH[j] = d.H;
+        off += (size_t)d.W * d.H;
+    }
+    CK(cudaEventRecord(fe->ev[EV_ROUGH1], c->stream));
+    CK(cudaEventRecord(fe->ev[EV_POST1], c->stream));
+    fe->hasFrame = true;
+    c->evPending.push_back(fe);
+    c->evCur = nullptr;
+    return RG_OK;
+}
+
+rg_status rg_batch_framebuffer(rg_ctx* c, uint32_t job, float** d) {
+    if (!c || !d) return RG_ERR_INVALID_ARG;
+    if (job >= c->batchOffset.size()) return fail(c, RG_ERR_INVALID_ARG, "no such job in the last batch");
+    *d = reinterpret_cast<float*>(c->batchFb.as<float4>() + c->batchOffset[job]);
+    return RG_OK;
+}
+
+rg_status rg_batch_download(rg_ctx* c, uint32_t job, float* host) {
+    if (!c || !host) return RG_ERR_INVALID_ARG;
+    if (job >= c->batchOffset.size()) return fail(c, RG_ERR_INVALID_ARG, "no such job in the last batch");
+    TRY(set_device(c));
+    CK(cudaMemcpyAsync(host, c->batchFb.as<float4>() + c->batchOffset[job], 16ull * c->batchW[job] * c->batchH[job],
+                       cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
 }
 
 }  // extern "C"

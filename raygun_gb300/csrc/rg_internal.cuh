@@ -159,6 +159,19 @@ struct WavefrontBuffers {
     uint32_t* counts;  // [0], [1] queue lengths, [2] trace work counter
 };
 
+// one render job of a batch: a scene, its UBO and its image size.  Work items of the batch are
+// numbered job after job; job j owns [workBase, workBase + workCount) and writes its per-sample
+// payload sums to samples[sampleBase + (y * W + x) * S + s].
+struct JobDesc {
+    DevScene scene;
+    rg_ubo ubo;
+    uint32_t W, H, S, tilesX;
+    uint32_t workBase;    // first work item (work items: 8x4 pixel tiles x 32 pixels x S samples)
+    uint32_t workCount;
+    uint32_t sampleBase;  // first per-sample slot in TraceParams::samples
+    uint32_t pad;
+};
+
 struct TraceParams {
     DevScene scene;
     rg_ubo ubo;
@@ -171,6 +184,17 @@ struct TraceParams {
     uint32_t* workCounter;         // work-item counter of the persistent kernel
     int countVisits;
     WavefrontBuffers wf;
+    // batch form of the wavefront loop (launch_trace_batch): the job table in device memory, the
+    // batch's work-item count, and per path slot the job and the output sample index.  A slot whose
+    // path finished takes the next work item (path regeneration), so `slots` bounds the path state.
+    const JobDesc* jobs;
+    uint32_t njobs;
+    uint32_t totalWork;
+    uint32_t slots;
+    uint32_t pad2;
+    uint32_t* slotJob;
+    uint32_t* slotSample;
+    const uint32_t* perm;  // nullable: order in which the trace kernel takes the queue's rays
 };
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
 // hostCount: pinned host word used to poll the queue length; iterations: trace/shade rounds run
@@ -179,6 +203,23 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
 typedef bool (*EventPairFn)(void* user, cudaEvent_t* start, cudaEvent_t* end);
 cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations,
                                    EventPairFn kernelEvents = nullptr, void* user = nullptr);
+// traversal launch shape of the batch loop: block size {64,128,256}, stack entries {16,24,32,48},
+// ray-sort key applied to each queue before it is traced
+struct TraceTune {
+    int threads = 128, depth = 48, sortKey = RG_SORT_NONE;
+};
+bool tune_supported(const TraceTune& t);
+// scratch of the ray sort (each of the first three: `slots` words; hist: sort_block_count(slots)*256)
+struct SortScratch {
+    uint32_t *keysA, *keysB, *valsA, *valsB, *hist;
+};
+// the wavefront loop over every job of p.jobs (raygen with regeneration, trace/shade rounds, tail);
+// hostWords: two pinned words (queue length, work counter) polled every few rounds
+cudaError_t launch_trace_batch(const TraceParams& p, const TraceTune& tune, const SortScratch& sort, cudaStream_t s,
+                               uint32_t* hostWords, int* iterations, EventPairFn kernelEvents = nullptr, void* user = nullptr);
+// raygen.rgen:36-38 for one job of a batch: average its samples into RGBA16F G-buffers
+cudaError_t launch_resolve_job(const float4* samples, const JobDesc& hostJob, uint2* base, uint2* normal, uint2* rough,
+                               cudaStream_t s);
 cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
 
 struct PostParams {

@@ -123,31 +123,34 @@ constexpr int kTraceThreads = 128;
 #endif
 
 // per-thread traversal stack in shared memory, laid out [depth][thread] so that the 32 lanes of a
-// warp touching the same depth hit 32 different banks
-struct SmemStack {
+// warp touching the same depth hit 32 different banks.  THREADS = block size, DEPTH = entries.
+template <int THREADS, int DEPTH>
+struct SmemStackT {
+    static constexpr int kDepth = DEPTH;
     uint32_t* base;  // &stack[0][threadIdx.x]
-    __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i * kTraceThreads]; }
+    __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i * THREADS]; }
 };
 // the same stack in (L1-cached) local memory
 #ifndef RG_STACK_SMEM
 #define RG_STACK_SMEM 1
 #endif
-#if !RG_STACK_SMEM
-struct LocalStack {
+template <int DEPTH>
+struct LocalStackT {
+    static constexpr int kDepth = DEPTH;
     uint32_t* base;
     __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i]; }
 };
-#endif
+#define RG_DECLARE_SMEM_STACK(name, THREADS, DEPTH)      \
+    __shared__ uint32_t name##_mem[DEPTH][THREADS];      \
+    const SmemStackT<THREADS, DEPTH> name{&name##_mem[0][threadIdx.x]}
 #if RG_STACK_SMEM
-#define RG_DECLARE_STACK(name)                                  \
-    __shared__ uint32_t name##_mem[kTraversalStack][kTraceThreads]; \
-    const SmemStack name{&name##_mem[0][threadIdx.x]}
-using TravStack = SmemStack;
+#define RG_DECLARE_STACK(name) RG_DECLARE_SMEM_STACK(name, kTraceThreads, kTraversalStack)
+using TravStack = SmemStackT<kTraceThreads, kTraversalStack>;
 #else
 #define RG_DECLARE_STACK(name)                 \
     uint32_t name##_mem[kTraversalStack];      \
-    const LocalStack name{name##_mem}
-using TravStack = LocalStack;
+    const LocalStackT<kTraversalStack> name{name##_mem}
+using TravStack = LocalStackT<kTraversalStack>;
 #endif
 #ifndef RG_WF_MIN_BLOCKS
 #define RG_WF_MIN_BLOCKS 7
@@ -198,8 +201,8 @@ __device__ __forceinline__ void trav_begin(Trav& T, const DevScene& sc, float ox
     T.active = true;
 }
 
-template <bool COUNT>
-__device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const TravStack& stack, VisitCounts& vc) {
+template <bool COUNT, class STACK>
+__device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STACK& stack, VisitCounts& vc) {
     const uint32_t ref = T.ref;
     const float tmin = T.tmin;
     if (!(ref & kLeaf)) {
@@ -226,7 +229,7 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const Tra
 #pragma unroll
             for (int j = 3; j >= 1; --j)
                 if (t[j] != INFINITY) {
-                    if (T.sp < kTraversalStack) stack[T.sp++] = r[j];
+                    if (T.sp < STACK::kDepth) stack[T.sp++] = r[j];
                     else vc.overflow++;
                 }
             T.ref = r[0];
@@ -255,7 +258,7 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const Tra
                 ray_pre(orr, qx, qy, qz, ex, ey, ez);
                 const float* rb = bl->root;
                 if (bn > 0 && slab(orr, __ldg(rb + 0), __ldg(rb + 3), __ldg(rb + 1), __ldg(rb + 4), __ldg(rb + 2), __ldg(rb + 5), tmin, T.h.t) != INFINITY) {
-                    if (T.sp < kTraversalStack) {
+                    if (T.sp < STACK::kDepth) {
                         stack[T.sp++] = kMarker;
                         T.r = orr;
                         T.nodes = bl->wide;
@@ -287,9 +290,9 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const Tra
     }
 }
 
-template <bool COUNT>
+template <bool COUNT, class STACK>
 __device__ Hit closest_hit(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
-                           const TravStack& stack, VisitCounts& vc) {
+                           const STACK& stack, VisitCounts& vc) {
     Trav T;
     trav_begin(T, sc, ox, oy, oz, dx, dy, dz, tmin, tmax);
     while (T.active) trav_step<COUNT>(T, sc, stack, vc);
@@ -834,14 +837,9 @@ __global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(co
     }
 }
 
-// raygen.h:116 + raygen.rgen:36-38: average the samples (in sample order) into the three RGBA16F
-// G-buffer images; normal.w = log(sum of depths) * 0.25 / S
-__global__ void k_resolve(const TraceParams P) {
-    const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= P.W || y >= P.H) return;
-    const uint32_t S = (uint32_t)P.ubo.numSamples;
-    const size_t pix = (size_t)y * P.W + x;
-    const float4* s = P.samples + 3 * pix * S;
+// raygen.h:116 + raygen.rgen:36-38: average one pixel's S samples (in sample order) into the three
+// RGBA16F G-buffer images; normal.w = log(sum of depths) * 0.25 / S
+__device__ __forceinline__ void resolve_pixel(const float4* s, uint32_t S, size_t pix, uint2* base, uint2* normal, uint2* rough) {
     float4 a = s[0], b = s[1], c = s[2];
     for (uint32_t k = 1; k < S; ++k) {
         const float4 a2 = s[3 * k], b2 = s[3 * k + 1], c2 = s[3 * k + 2];
@@ -850,9 +848,26 @@ __global__ void k_resolve(const TraceParams P) {
         c.x = c.x + c2.x; c.y = c.y + c2.y; c.z = c.z + c2.z; c.w = c.w + c2.w;
     }
     const float fs = (float)S;
-    P.base[pix] = pack_half4(a.x / fs, a.y / fs, a.z / fs, a.w / fs);
-    P.normal[pix] = pack_half4(b.x / fs, b.y / fs, b.z / fs, (logf(b.w) * 0.25f) / fs);
-    P.rough[pix] = pack_half4(c.x / fs, c.y / fs, c.z / fs, c.w / fs);
+    base[pix] = pack_half4(a.x / fs, a.y / fs, a.z / fs, a.w / fs);
+    normal[pix] = pack_half4(b.x / fs, b.y / fs, b.z / fs, (logf(b.w) * 0.25f) / fs);
+    rough[pix] = pack_half4(c.x / fs, c.y / fs, c.z / fs, c.w / fs);
+}
+
+__global__ void k_resolve(const TraceParams P) {
+    const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= P.W || y >= P.H) return;
+    const uint32_t S = (uint32_t)P.ubo.numSamples;
+    const size_t pix = (size_t)y * P.W + x;
+    resolve_pixel(P.samples + 3 * pix * S, S, pix, P.base, P.normal, P.rough);
+}
+
+// samples: the job's first sample (samples + 3 * sampleBase)
+__global__ void k_resolve_job(const float4* __restrict__ samples, uint32_t W, uint32_t H, uint32_t S, uint2* base, uint2* normal,
+                              uint2* rough) {
+    const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t pix = (size_t)y * W + x;
+    resolve_pixel(samples + 3 * pix * S, S, pix, base, normal, rough);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -920,6 +935,50 @@ __device__ __forceinline__ void flush_counts(const TraceParams& P, unsigned long
             }
 }
 
+// work item -> pixel and sample: work items enumerate 8x4 pixel tiles (row-major over the tile
+// grid), then the 32 pixels of a tile (row-major), then the samples of a pixel
+__device__ __forceinline__ bool decode_work(uint32_t id, uint32_t W, uint32_t H, uint32_t S, uint32_t tilesX, uint32_t& px,
+                                            uint32_t& py, uint32_t& sample) {
+    sample = id % S;
+    const uint32_t pid = id / S, tile = pid / (kTileW * kTileH), within = pid % (kTileW * kTileH);
+    px = (tile % tilesX) * kTileW + within % kTileW;
+    py = (tile / tilesX) * kTileH + within / kTileW;
+    return px < W && py < H;
+}
+
+// the job owning work item `id`: the last job whose workBase <= id (jobs are in work order)
+__device__ __forceinline__ uint32_t find_job(const JobDesc* __restrict__ jobs, uint32_t n, uint32_t id) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].workBase <= id) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// camera ray and fresh payload of work item `id` of a batch (raygen.h:84-102 with the job's UBO);
+// false when the item's pixel lies outside its image
+__device__ __forceinline__ bool batch_primary(const TraceParams& P, uint32_t id, uint32_t& job, uint32_t& sampleIdx, Payload& p,
+                                              RayReq& ray) {
+    job = find_job(P.jobs, P.njobs, id);
+    const JobDesc& J = P.jobs[job];
+    uint32_t px, py, s;
+    if (!decode_work(id - J.workBase, J.W, J.H, J.S, J.tilesX, px, py, s)) return false;
+    float org[4];
+    mul4(J.ubo.viewInverse, 0.0f, 0.0f, 0.0f, 1.0f, org);
+    const int aaRow = J.S < 8 ? (int)J.S : 8;
+    start_sample(J.ubo, v3(org[0], org[1], org[2]), px, py, J.W, J.H, (int)s, aaRow, p, ray);
+    sampleIdx = J.sampleBase + (py * J.W + px) * J.S + s;
+    return true;
+}
+
+__device__ __forceinline__ void store_sample(float4* so, const Payload& p) {
+    so[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
+    so[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
+    so[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
+}
+
 // raygen: one path per (pixel, sample) in 8x4-tile order; primary rays go to queue 0
 __global__ void __launch_bounds__(256) k_wf_raygen(const TraceParams P) {
     const WavefrontBuffers& wf = P.wf;
@@ -935,14 +994,7 @@ __global__ void __launch_bounds__(256) k_wf_raygen(const TraceParams P) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
         const uint32_t id = base + threadIdx.x;
         uint32_t px = 0, py = 0, sample = 0;
-        bool valid = false;
-        if (id < total) {
-            sample = id % S;
-            const uint32_t pid = id / S, tile = pid / (kTileW * kTileH), within = pid % (kTileW * kTileH);
-            px = (tile % tilesX) * kTileW + within % kTileW;
-            py = (tile / tilesX) * kTileH + within / kTileW;
-            valid = px < P.W && py < P.H;
-        }
+        const bool valid = id < total && decode_work(id, P.W, P.H, S, tilesX, px, py, sample);
         const uint32_t pos = warp_append(wf.counts + 0, valid);
         if (valid) {
             Payload p;
@@ -958,20 +1010,46 @@ __global__ void __launch_bounds__(256) k_wf_raygen(const TraceParams P) {
     flush_counts(P, c, 1);
 }
 
+// raygen of a batch: path slot k starts work item k (k < min(totalWork, slots)); the shade kernel
+// hands later work items to slots whose paths finished
+__global__ void __launch_bounds__(256) k_wfb_raygen(const TraceParams P) {
+    const WavefrontBuffers& wf = P.wf;
+    const uint32_t total = min(P.totalWork, P.slots);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *P.workCounter = total;
+    unsigned long long c[1] = {0};
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+        const uint32_t id = base + threadIdx.x;
+        Payload p;
+        RayReq ray;
+        uint32_t job = 0, si = 0;
+        const bool valid = id < total && batch_primary(P, id, job, si, p, ray);
+        const uint32_t pos = warp_append(wf.counts + 0, valid);
+        if (valid) {
+            store_payload(wf.payload + 4 * (size_t)id, p);
+            wf.meta[id] = make_int2(0, 0);
+            P.slotJob[id] = job;
+            P.slotSample[id] = si;
+            emit_ray(wf, 0, pos, id, ray);
+            c[0]++;
+        }
+    }
+    flush_counts(P, c, 1);
+}
+
 // closest hit of every ray of queue q.  Lanes whose ray finished take new rays from the queue (one
 // atomic per warp) as soon as RG_FETCH_THRESHOLD lanes of the warp are idle, so a warp does not wait
-// for its longest ray; between fetches every lane advances its ray by RG_TRACE_STEPS steps.
+// for its longest ray; between fetches every lane advances its ray by RG_WF_STEPS steps.  BATCH: the
+// ray's scene is its path's job's scene.  P.perm (nullable) gives the order the rays are taken in.
 #ifndef RG_FETCH_THRESHOLD
 #define RG_FETCH_THRESHOLD 8
 #endif
 #ifndef RG_WF_STEPS
 #define RG_WF_STEPS 8
 #endif
-template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads, RG_WF_MIN_BLOCKS) k_wf_trace(const TraceParams P, int q) {
-    RG_DECLARE_STACK(stk);
+template <bool COUNT, bool BATCH, int THREADS, int DEPTH>
+__global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k_wf_trace(const TraceParams P, int q) {
+    RG_DECLARE_SMEM_STACK(stk, THREADS, DEPTH);
     const WavefrontBuffers& wf = P.wf;
-    const DevScene& sc = P.scene;
     const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.counts[q ^ 1] = 0;  // the shade kernel appends there next
     const unsigned lane = threadIdx.x & 31;
@@ -980,6 +1058,8 @@ __global__ void __launch_bounds__(kTraceThreads, RG_WF_MIN_BLOCKS) k_wf_trace(co
     Trav T;
     T.active = false;
     uint32_t slot = 0;
+    const DevScene* scp = nullptr;  // BATCH: scene of the lane's ray
+#define RG_SC (BATCH ? *scp : P.scene)
     bool exhausted = false;
     for (;;) {
         const unsigned idle = __ballot_sync(0xFFFFFFFFu, !T.active);
@@ -992,12 +1072,14 @@ __global__ void __launch_bounds__(kTraceThreads, RG_WF_MIN_BLOCKS) k_wf_trace(co
                 if ((int)lane == leader) base = atomicAdd(wf.counts + 2, (uint32_t)__popc(needMask));
                 base = __shfl_sync(0xFFFFFFFFu, base, leader);
                 if (need) {
-                    slot = base + (uint32_t)__popc(needMask & ltmask);
-                    if (slot >= count) {
+                    const uint32_t k = base + (uint32_t)__popc(needMask & ltmask);
+                    if (k >= count) {
                         exhausted = true;
                     } else {
+                        slot = P.perm ? P.perm[k] : k;
+                        if (BATCH) scp = &P.jobs[P.slotJob[wf.qPath[q][slot]]].scene;
                         const float4 o = wf.qO[q][slot], d = wf.qD[q][slot];
-                        trav_begin(T, sc, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w);
+                        trav_begin(T, RG_SC, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w);
                         if (!T.active) {  // zero direction or the scene box missed
                             wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
                             wf.hitInst[slot] = 0xFFFFFFFFu;
@@ -1010,7 +1092,7 @@ __global__ void __launch_bounds__(kTraceThreads, RG_WF_MIN_BLOCKS) k_wf_trace(co
         if (T.active) {
 #pragma unroll 1
             for (int k = 0; k < RG_WF_STEPS; ++k) {
-                trav_step<COUNT>(T, sc, stk, vc);
+                trav_step<COUNT>(T, RG_SC, stk, vc);
                 if (!T.active) {
                     wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
                     wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;
@@ -1019,6 +1101,7 @@ __global__ void __launch_bounds__(kTraceThreads, RG_WF_MIN_BLOCKS) k_wf_trace(co
             }
         }
     }
+#undef RG_SC
     unsigned long long c[3] = {vc.nodes, vc.tris, vc.overflow};
     for (int k = 0; k < 3; ++k) {
         unsigned long long v = c[k];
@@ -1030,20 +1113,37 @@ __global__ void __launch_bounds__(kTraceThreads, RG_WF_MIN_BLOCKS) k_wf_trace(co
     }
 }
 
-// shading of every result of queue q; next rays go to queue q^1, finished samples to P.samples
+// shading of one path from a trace result up to its next traversed ray (false) or to the end of
+// its sample (true); mask-0 traces and zero directions run their miss shader right away
+__device__ __forceinline__ bool shade_until_trace(const DevScene& sc, const V3 L, const int maxRec, Hit h, Payload& p, RayReq& ray,
+                                                  Frame* frames, int& fsp, RayCounts& cnt) {
+    Frame cur;
+    for (;;) {
+        if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) return true;
+        if (ray.masked || (ray.d.x == 0.0f && ray.d.y == 0.0f && ray.d.z == 0.0f)) {
+            h.hit = false;
+            continue;
+        }
+        return false;
+    }
+}
+
+// shading of every result of queue q; next rays go to queue q^1, finished samples to P.samples.
+// BATCH: a slot whose path finished starts the batch's next work item in place.
+template <bool BATCH>
 __global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
     const WavefrontBuffers& wf = P.wf;
-    const DevScene& sc = P.scene;
-    const rg_ubo& U = P.ubo;
-    const V3 L = v3(U.lightDir[0], U.lightDir[1], U.lightDir[2]);
-    const int maxRec = U.maxRecursions;
+    const V3 L = v3(P.ubo.lightDir[0], P.ubo.lightDir[1], P.ubo.lightDir[2]);
+    const int maxRec = P.ubo.maxRecursions;
     const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.counts[2] = 0;  // the next trace kernel's work counter
+    const unsigned lane = threadIdx.x & 31;
     RayCounts cnt = {0, 0, 0, 0};
     Frame* framesBase = static_cast<Frame*>(wf.frames);
+    bool exhausted = false;
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
-        bool emit = false;
+        bool emit = false, regen = false;
         uint32_t path = 0;
         Payload p;
         RayReq ray;
@@ -1069,21 +1169,45 @@ __global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
             h.v = ht.z;
             h.prim = __float_as_uint(ht.w);
             Frame* frames = framesBase + (size_t)path * kMaxFrames;
-            Frame cur;
-            for (;;) {
-                if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) {
-                    float4* so = P.samples + 3 * (size_t)path;
-                    so[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
-                    so[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
-                    so[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
-                    break;
-                }
-                if (ray.masked || (ray.d.x == 0.0f && ray.d.y == 0.0f && ray.d.z == 0.0f)) {
-                    h.hit = false;  // no traversal: the trace's miss shader runs right away
-                    continue;
-                }
+            bool done;
+            if constexpr (BATCH) {
+                const JobDesc& J = P.jobs[P.slotJob[path]];
+                done = shade_until_trace(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, h,
+                                         p, ray, frames, fsp, cnt);
+            } else {
+                done = shade_until_trace(P.scene, L, maxRec, h, p, ray, frames, fsp, cnt);
+            }
+            if (done) {
+                store_sample(P.samples + 3 * (size_t)(BATCH ? P.slotSample[path] : path), p);
+                regen = BATCH;
+            } else {
                 emit = true;
-                break;
+            }
+        }
+        if constexpr (BATCH) {
+            // path regeneration: finished slots take the next work items (one atomic per warp and try)
+            for (;;) {
+                const bool need = regen && !exhausted;
+                const unsigned needMask = __ballot_sync(0xFFFFFFFFu, need);
+                if (!needMask) break;
+                const int leader = __ffs(needMask) - 1;
+                uint32_t b0 = 0;
+                if ((int)lane == leader) b0 = atomicAdd(P.workCounter, (uint32_t)__popc(needMask));
+                b0 = __shfl_sync(0xFFFFFFFFu, b0, leader);
+                if (need) {
+                    const uint32_t id = b0 + (uint32_t)__popc(needMask & ((1u << lane) - 1u));
+                    uint32_t job = 0, si = 0;
+                    if (id >= P.totalWork) {
+                        exhausted = true;
+                    } else if (batch_primary(P, id, job, si, p, ray)) {
+                        P.slotJob[path] = job;
+                        P.slotSample[path] = si;
+                        fsp = 0;
+                        regen = false;
+                        emit = true;
+                        cnt.primary++;
+                    }
+                }
             }
         }
         const uint32_t pos = warp_append(wf.counts + (q ^ 1), emit);
@@ -1093,28 +1217,32 @@ __global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
             wf.meta[path] = make_int2(fsp, ray.missIndex);
         }
     }
-    unsigned long long c[3] = {cnt.shadow, cnt.secondary, cnt.masked};
-    const unsigned lane = threadIdx.x & 31;
-    for (int k = 0; k < 3; ++k) {
-        unsigned long long v = c[k];
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
-        if (lane == 0 && v) {
-            atomicAdd(P.counters + 1 + k, v);
-            atomicAdd(P.counters + 9 + k, v);
-        }
+    unsigned long long c[4] = {cnt.primary, cnt.shadow, cnt.secondary, cnt.masked};
+    flush_counts(P, c, 4);
+}
+
+// the rest of one path, traced and shaded back to back
+template <class STACK>
+__device__ __forceinline__ void finish_path(const DevScene& sc, const V3 L, const int maxRec, RayReq& ray, Payload& p, Frame* frames,
+                                            int& fsp, const STACK& stk, VisitCounts& vc, RayCounts& cnt) {
+    Frame cur;
+    for (;;) {
+        Hit h;
+        h.hit = false;
+        if (!ray.masked) h = closest_hit<false>(sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, stk, vc);
+        if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) break;
     }
 }
 
 // Tail of the wavefront loop: once few paths remain, one launch finishes every remaining path --
 // each thread traces and shades its path's remaining sequence back to back -- instead of one
-// (trace, shade) launch pair per remaining round.
+// (trace, shade) launch pair per remaining round.  BATCH: only after the last work item was taken.
+template <bool BATCH>
 __global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, int q) {
     RG_DECLARE_STACK(stk);
     const WavefrontBuffers& wf = P.wf;
-    const DevScene& sc = P.scene;
-    const rg_ubo& U = P.ubo;
-    const V3 L = v3(U.lightDir[0], U.lightDir[1], U.lightDir[2]);
-    const int maxRec = U.maxRecursions;
+    const V3 L0 = v3(P.ubo.lightDir[0], P.ubo.lightDir[1], P.ubo.lightDir[2]);
+    const int maxRec0 = P.ubo.maxRecursions;
     const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
     RayCounts cnt = {0, 0, 0, 0};
     VisitCounts vc = {0, 0, 0};
@@ -1134,17 +1262,14 @@ __global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, 
         Payload p;
         load_payload(wf.payload + 4 * (size_t)path, p);
         Frame* frames = framesBase + (size_t)path * kMaxFrames;
-        Frame cur;
-        for (;;) {
-            Hit h;
-            h.hit = false;
-            if (!ray.masked) h = closest_hit<false>(sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, stk, vc);
-            if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) break;
+        if constexpr (BATCH) {
+            const JobDesc& J = P.jobs[P.slotJob[path]];
+            finish_path(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, ray, p, frames, fsp,
+                        stk, vc, cnt);
+        } else {
+            finish_path(P.scene, L0, maxRec0, ray, p, frames, fsp, stk, vc, cnt);
         }
-        float4* so = P.samples + 3 * (size_t)path;
-        so[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
-        so[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
-        so[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
+        store_sample(P.samples + 3 * (size_t)(BATCH ? P.slotSample[path] : path), p);
     }
     unsigned long long c[6] = {cnt.shadow, cnt.secondary, cnt.masked, vc.nodes, vc.tris, vc.overflow};
     const int slot[6] = {1, 2, 3, 4, 5, 6};
@@ -1156,6 +1281,102 @@ __global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, 
             atomicAdd(P.counters + slot[k], v);
             atomicAdd(P.counters + 8 + slot[k], v);
         }
+    }
+}
+
+// ---- ray sort of a queue (batch loop, optional) ------------------------------------------------
+// Bucket keys: direction octant (8 buckets) or the Morton code of the origin quantised to 16 cells
+// per axis of the scene's root box (4096 buckets).  The order within a bucket is arbitrary: every
+// ray's result is a function of the ray alone, so the sort changes which lane traces a ray, not
+// what it returns.
+template <int KEY>
+struct SortBuckets {
+    static constexpr int n = KEY == RG_SORT_OCTANT ? 8 : 4096;
+};
+
+template <bool BATCH, int KEY>
+__device__ __forceinline__ uint32_t ray_sort_key(const TraceParams& P, const float4 o, const float4 d, uint32_t path) {
+    if (KEY == RG_SORT_OCTANT) return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    const DevScene& sc = BATCH ? P.jobs[P.slotJob[path]].scene : P.scene;
+    if (sc.tlasN == 0) return 0u;
+    const float* b = sc.tlasRoot;
+    const float x = fminf(fmaxf((o.x - b[0]) / (b[3] - b[0]) * 16.0f, 0.0f), 15.0f);
+    const float y = fminf(fmaxf((o.y - b[1]) / (b[4] - b[1]) * 16.0f, 0.0f), 15.0f);
+    const float z = fminf(fmaxf((o.z - b[2]) / (b[5] - b[2]) * 16.0f, 0.0f), 15.0f);
+    return (expand10((uint32_t)x) << 2) | (expand10((uint32_t)y) << 1) | expand10((uint32_t)z);
+}
+
+// per block: histogram of the queue's keys in shared memory, added to the global bucket counts
+template <bool BATCH, int KEY>
+__global__ void __launch_bounds__(256) k_sort_count(const TraceParams P, int q, uint32_t* __restrict__ keys,
+                                                     uint32_t* __restrict__ buckets) {
+    constexpr int NB = SortBuckets<KEY>::n;
+    __shared__ uint32_t h[NB];
+    for (int i = threadIdx.x; i < NB; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const WavefrontBuffers& wf = P.wf;
+    const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t k = ray_sort_key<BATCH, KEY>(P, wf.qO[q][i], wf.qD[q][i], BATCH ? wf.qPath[q][i] : 0u);
+        keys[i] = k;
+        atomicAdd(&h[k], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NB; i += blockDim.x)
+        if (h[i]) atomicAdd(&buckets[i], h[i]);
+}
+
+// exclusive scan of the bucket counts into offsets (one block of 1024 threads); clears the counts
+template <int NB>
+__global__ void __launch_bounds__(1024) k_sort_offsets(uint32_t* __restrict__ buckets, uint32_t* __restrict__ offsets) {
+    constexpr int PER = (NB + 1023) / 1024;
+    __shared__ uint32_t part[1024];
+    uint32_t v[PER], sum = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int b = threadIdx.x * PER + k;
+        v[k] = b < NB ? buckets[b] : 0u;
+        sum += v[k];
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const uint32_t t = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int b = threadIdx.x * PER + k;
+        if (b < NB) {
+            offsets[b] = run;
+            buckets[b] = 0u;
+        }
+        run += v[k];
+    }
+}
+
+// perm[offsets[key]++] = ray: each block reserves one range per bucket, then fills it
+template <int KEY>
+__global__ void __launch_bounds__(256) k_sort_scatter(const TraceParams P, int q, const uint32_t* __restrict__ keys,
+                                                       uint32_t* __restrict__ offsets, uint32_t* __restrict__ perm) {
+    constexpr int NB = SortBuckets<KEY>::n;
+    __shared__ uint32_t h[NB], start[NB];
+    for (int i = threadIdx.x; i < NB; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const uint32_t count = *(volatile uint32_t*)(P.wf.counts + q);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) atomicAdd(&h[keys[i]], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < NB; i += blockDim.x) {
+        start[i] = h[i] ? atomicAdd(&offsets[i], h[i]) : 0u;
+        h[i] = 0;
+    }
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        perm[start[k] + atomicAdd(&h[k], 1u)] = i;
     }
 }
 
@@ -1212,21 +1433,54 @@ static int persistent_grid(const void* fn, int threads, int smem) {
     return sms * (perSm > 0 ? perSm : 1);
 }
 
+// persistent grid sizes, one per kernel (computed on first use)
+static int grid_of(const void* fn, int threads) {
+    static const void* fns[64];
+    static int grids[64];
+    static int n = 0;
+    for (int k = 0; k < n; ++k)
+        if (fns[k] == fn) return grids[k];
+    const int g = persistent_grid(fn, threads, 0);
+    if (g && n < 64) {
+        fns[n] = fn;
+        grids[n] = g;
+        ++n;
+    }
+    return g;
+}
+
+typedef void (*TraceKernel)(const TraceParams, int);
+
+// the traversal kernel of one launch shape
+static TraceKernel trace_kernel(bool batch, bool count, int threads, int depth) {
+    if (count) return batch ? k_wf_trace<true, true, kTraceThreads, kTraversalStack> : k_wf_trace<true, false, kTraceThreads, kTraversalStack>;
+    if (!batch) return k_wf_trace<false, false, kTraceThreads, kTraversalStack>;
+#define RG_TK(T, D) \
+    if (threads == T && depth == D) return k_wf_trace<false, true, T, D>;
+    RG_TK(64, 16) RG_TK(64, 24) RG_TK(64, 32) RG_TK(64, 48)
+    RG_TK(128, 16) RG_TK(128, 24) RG_TK(128, 32) RG_TK(128, 48)
+    RG_TK(256, 16) RG_TK(256, 24) RG_TK(256, 32) RG_TK(256, 48)
+#undef RG_TK
+    return nullptr;
+}
+
+bool tune_supported(const TraceTune& t) {
+    return trace_kernel(true, false, t.threads, t.depth) != nullptr && t.sortKey >= RG_SORT_NONE && t.sortKey <= RG_SORT_MORTON;
+}
+
 cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations,
                                    EventPairFn kernelEvents, void* user) {
-    static int gTrace[2] = {0, 0}, gShade = 0, gRaygen = 0;
     const int c = p.countVisits ? 1 : 0;
-    if (!gTrace[c]) gTrace[c] = c ? persistent_grid((const void*)k_wf_trace<true>, kTraceThreads, 0)
-                                  : persistent_grid((const void*)k_wf_trace<false>, kTraceThreads, 0);
-    if (!gShade) gShade = persistent_grid((const void*)k_wf_shade, 128, 0);
-    if (!gRaygen) gRaygen = persistent_grid((const void*)k_wf_raygen, 256, 0);
-    if (!gTrace[c] || !gShade || !gRaygen) return cudaErrorUnknown;
+    const TraceKernel trace = trace_kernel(false, c, kTraceThreads, kTraversalStack);
+    const int gTrace = grid_of((const void*)trace, kTraceThreads);
+    const int gShade = grid_of((const void*)k_wf_shade<false>, 128);
+    const int gRaygen = grid_of((const void*)k_wf_raygen, 256);
+    const int gTail = grid_of((const void*)k_wf_tail<false>, kTraceThreads);
+    if (!gTrace || !gShade || !gRaygen || !gTail) return cudaErrorUnknown;
     cudaError_t e = cudaMemsetAsync(p.wf.counts, 0, 4 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     k_wf_raygen<<<gRaygen, 256, 0, s>>>(p);
     count_launch();
-    static int gTail = 0;
-    if (!gTail) gTail = persistent_grid((const void*)k_wf_tail, kTraceThreads, 0);
     // the pending-ray count below which the remaining paths finish in one k_wf_tail launch; the
     // visit-counting build stays in the round loop (the tail kernel does not count visits)
     const uint32_t tailBelow = c ? 0u : (uint32_t)RG_TAIL_RAYS;
@@ -1237,10 +1491,9 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
             if (e0) cudaEventRecord(e0, s);
-            if (c) k_wf_trace<true><<<gTrace[c], kTraceThreads, 0, s>>>(p, q);
-            else k_wf_trace<false><<<gTrace[c], kTraceThreads, 0, s>>>(p, q);
+            trace<<<gTrace, kTraceThreads, 0, s>>>(p, q);
             if (e1) cudaEventRecord(e1, s);
-            k_wf_shade<<<gShade, 128, 0, s>>>(p, q);
+            k_wf_shade<false><<<gShade, 128, 0, s>>>(p, q);
             count_launch(2);
             q ^= 1;
         }
@@ -1252,7 +1505,7 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
             if (e0) cudaEventRecord(e0, s);
-            k_wf_tail<<<gTail, kTraceThreads, 0, s>>>(p, q);
+            k_wf_tail<false><<<gTail, kTraceThreads, 0, s>>>(p, q);
             if (e1) cudaEventRecord(e1, s);
             count_launch();
             break;
@@ -1262,6 +1515,83 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
     if (iterations) *iterations = it;
     dim3 grid((p.W + 31) / 32, (p.H + 7) / 8);
     k_resolve<<<grid, 256, 0, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// sort of queue q by the tune's key into p.perm (the scratch's valsA)
+static cudaError_t enqueue_sort(const TraceParams& p, int key, const SortScratch& sc, int grid, int q, cudaStream_t s) {
+    if (key == RG_SORT_OCTANT) {
+        k_sort_count<true, RG_SORT_OCTANT><<<grid, 256, 0, s>>>(p, q, sc.keysA, sc.hist);
+        k_sort_offsets<SortBuckets<RG_SORT_OCTANT>::n><<<1, 1024, 0, s>>>(sc.hist, sc.hist + 4096);
+        k_sort_scatter<RG_SORT_OCTANT><<<grid, 256, 0, s>>>(p, q, sc.keysA, sc.hist + 4096, sc.valsA);
+    } else {
+        k_sort_count<true, RG_SORT_MORTON><<<grid, 256, 0, s>>>(p, q, sc.keysA, sc.hist);
+        k_sort_offsets<SortBuckets<RG_SORT_MORTON>::n><<<1, 1024, 0, s>>>(sc.hist, sc.hist + 4096);
+        k_sort_scatter<RG_SORT_MORTON><<<grid, 256, 0, s>>>(p, q, sc.keysA, sc.hist + 4096, sc.valsA);
+    }
+    count_launch(3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_batch(const TraceParams& p0, const TraceTune& tune, const SortScratch& sort, cudaStream_t s,
+                               uint32_t* hostWords, int* iterations, EventPairFn kernelEvents, void* user) {
+    TraceParams p = p0;
+    const int c = p.countVisits ? 1 : 0;
+    const int threads = c ? kTraceThreads : tune.threads;
+    const TraceKernel trace = trace_kernel(true, c, threads, c ? kTraversalStack : tune.depth);
+    if (!trace || !tune_supported(tune)) return cudaErrorInvalidValue;
+    const int gTrace = grid_of((const void*)trace, threads);
+    const int gShade = grid_of((const void*)k_wf_shade<true>, 128);
+    const int gRaygen = grid_of((const void*)k_wfb_raygen, 256);
+    const int gTail = grid_of((const void*)k_wf_tail<true>, kTraceThreads);
+    const int gSort = grid_of((const void*)k_sort_scatter<RG_SORT_MORTON>, 256);
+    if (!gTrace || !gShade || !gRaygen || !gTail || !gSort) return cudaErrorUnknown;
+    const bool sorted = tune.sortKey != RG_SORT_NONE;
+    p.perm = sorted ? sort.valsA : nullptr;
+    cudaError_t e = cudaMemsetAsync(p.wf.counts, 0, 4 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    if (sorted && (e = cudaMemsetAsync(sort.hist, 0, 4096 * sizeof(uint32_t), s)) != cudaSuccess) return e;
+    k_wfb_raygen<<<gRaygen, 256, 0, s>>>(p);
+    count_launch();
+    const uint32_t tailBelow = c ? 0u : (uint32_t)RG_TAIL_RAYS;
+    int q = 0, it = 0;
+    const int kChunk = RG_POLL_ROUNDS, kMaxIterations = 100000;
+    for (;;) {
+        for (int k = 0; k < kChunk; ++k, ++it) {
+            if (sorted && (e = enqueue_sort(p, tune.sortKey, sort, gSort, q, s)) != cudaSuccess) return e;
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
+            if (e0) cudaEventRecord(e0, s);
+            trace<<<gTrace, threads, 0, s>>>(p, q);
+            if (e1) cudaEventRecord(e1, s);
+            k_wf_shade<true><<<gShade, 128, 0, s>>>(p, q);
+            count_launch(2);
+            q ^= 1;
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(hostWords, p.wf.counts + q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(hostWords + 1, p.workCounter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        if (hostWords[0] == 0) break;  // nothing queued: every path finished and no work item is left
+        if (hostWords[1] >= p.totalWork && hostWords[0] < tailBelow) {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
+            if (e0) cudaEventRecord(e0, s);
+            k_wf_tail<true><<<gTail, kTraceThreads, 0, s>>>(p, q);
+            if (e1) cudaEventRecord(e1, s);
+            count_launch();
+            break;
+        }
+        if (it >= kMaxIterations) return cudaErrorLaunchTimeout;
+    }
+    if (iterations) *iterations = it;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve_job(const float4* samples, const JobDesc& j, uint2* base, uint2* normal, uint2* rough, cudaStream_t s) {
+    dim3 grid((j.W + 31) / 32, (j.H + 7) / 8);
+    k_resolve_job<<<grid, 256, 0, s>>>(samples + 3 * (size_t)j.sampleBase, j.W, j.H, j.S, base, normal, rough);
     count_launch();
     return cudaGetLastError();
 }

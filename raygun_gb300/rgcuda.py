@@ -32,8 +32,14 @@ EXPORTS = [
     "rg_download", "rg_framebuffer_device", "rg_download_image", "rg_synchronize", "rg_get_timings", "rg_get_stats",
     "rg_get_stream", "rg_bvh_info", "rg_instance_inverse", "rg_trace_rays", "rg_post_only", "rg_lbvh_build_host",
     "rg_update_vertices_device", "rg_get_total_stats", "rg_reset_total_stats", "rg_set_flags", "rg_launch_count",
-    "rg_lbvh_build_device_noalloc",
+    "rg_lbvh_build_device_noalloc", "rg_scene_create", "rg_scene_select", "rg_scene_destroy", "rg_scene_bytes",
+    "rg_render_batch", "rg_batch_framebuffer", "rg_batch_download", "rg_set_batch_tune", "rg_get_batch_tune",
+    "rg_set_batch_slots",
 ]
+
+# rg_job (include/rgcuda.h): one render of a batch
+JOB = np.dtype([("scene", "<u4"), ("width", "<u4"), ("height", "<u4"), ("fxaa", "<i4"), ("ubo", scenes.UBO)])
+SORT_KEYS = {"none": 0, "octant": 1, "morton": 2}
 
 
 class DeviceOpts(ctypes.Structure):
@@ -51,6 +57,10 @@ class Timings(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("primary", "shadow", "secondary", "masked", "nodes", "tris",
                                                "stack_overflows", "iterations")]
+
+
+class BatchTune(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("stack_depth", ctypes.c_int32), ("sort_key", ctypes.c_int32)]
 
 
 class RgError(RuntimeError):
@@ -102,6 +112,16 @@ def load(path: str = LIB_PATH):
         "rg_set_flags": ([P, U32], I32),
         "rg_launch_count": ([ctypes.POINTER(ctypes.c_uint64)], I32),
         "rg_lbvh_build_device_noalloc": ([P, U32, P, P, P, P, P, P], I32),
+        "rg_scene_create": ([P, ctypes.POINTER(U32)], I32),
+        "rg_scene_select": ([P, U32], I32),
+        "rg_scene_destroy": ([P, U32], I32),
+        "rg_scene_bytes": ([P, U32, ctypes.POINTER(ctypes.c_uint64)], I32),
+        "rg_render_batch": ([P, P, U32], I32),
+        "rg_batch_framebuffer": ([P, U32, ctypes.POINTER(P)], I32),
+        "rg_batch_download": ([P, U32, P], I32),
+        "rg_set_batch_tune": ([P, ctypes.POINTER(BatchTune)], I32),
+        "rg_get_batch_tune": ([P, ctypes.POINTER(BatchTune)], I32),
+        "rg_set_batch_slots": ([P, U32], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -243,6 +263,53 @@ class Context:
         self._ck(self.L.rg_get_stream(self.h, ctypes.byref(p)))
         return p.value or 0
 
+    # -- scene slots and batched rendering
+    def scene_create(self) -> int:
+        out = ctypes.c_uint32()
+        self._ck(self.L.rg_scene_create(self.h, ctypes.byref(out)))
+        return out.value
+
+    def scene_select(self, scene: int):
+        self._ck(self.L.rg_scene_select(self.h, scene))
+
+    def scene_destroy(self, scene: int):
+        self._ck(self.L.rg_scene_destroy(self.h, scene))
+
+    def scene_bytes(self, scene: int) -> int:
+        out = ctypes.c_uint64()
+        self._ck(self.L.rg_scene_bytes(self.h, scene, ctypes.byref(out)))
+        return out.value
+
+    def render_batch(self, jobs):
+        j = np.ascontiguousarray(jobs, dtype=JOB)
+        self._ck(self.L.rg_render_batch(self.h, _p(j), len(j)))
+        self._batch = [(int(x["width"]), int(x["height"])) for x in j]
+
+    def batch_download(self, job: int, out=None):
+        w, h = self._batch[job] if 0 <= job < len(getattr(self, "_batch", [])) else (0, 0)
+        if out is None:
+            out = np.empty((h, w, 4), np.float32)
+        self._ck(self.L.rg_batch_download(self.h, job, _p(out)))
+        return out
+
+    def batch_framebuffer_ptr(self, job: int) -> int:
+        p = ctypes.c_void_p()
+        self._ck(self.L.rg_batch_framebuffer(self.h, job, ctypes.byref(p)))
+        return p.value
+
+    def set_batch_tune(self, threads=128, stack_depth=48, sort_key=0):
+        key = SORT_KEYS[sort_key] if isinstance(sort_key, str) else sort_key
+        t = BatchTune(threads, stack_depth, key)
+        self._ck(self.L.rg_set_batch_tune(self.h, ctypes.byref(t)))
+
+    def batch_tune(self) -> dict:
+        t = BatchTune()
+        self._ck(self.L.rg_get_batch_tune(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in BatchTune._fields_}
+
+    def set_batch_slots(self, slots: int):
+        self._ck(self.L.rg_set_batch_slots(self.h, slots))
+
     # -- parity / inspection
     def bvh(self, blas: int):
         b = 0xFFFFFFFF if blas < 0 else blas
@@ -321,3 +388,44 @@ class Raytracer:
     def render(self, ubo=None, fxaa=True):         # RenderSystem::render (headless)
         self.do_raytracing(ubo, fxaa)
         return self.ctx.download()
+
+
+def load_scene(ctx: Context, scene: scenes.Scene):
+    """setupModelBuffers + setupBottomLevelAS + setupTopLevelAS of `scene` into ctx's selected slot."""
+    ctx.upload_geometry(scene.vertices, scene.indices, scene.materials)
+    blas = [ctx.build_blas(int(m["vertexOffset"]), int(m["indexOffset"]), int(m["triCount"])) for m in scene.meshes]
+    inst = scene.instances.copy()
+    inst["blas"] = np.asarray(blas, np.uint32)[inst["blas"]]
+    ctx.build_tlas(inst)
+    return blas
+
+
+class BatchRenderer:
+    """Several scenes resident in one context, one scene slot each, rendered together by
+    rg_render_batch: each job is RenderSystem::render of one scene with its own camera, size,
+    samples and recursion depth."""
+
+    def __init__(self, scene_list, device=0, flags=0, hbm_budget_bytes=0):
+        self.ctx = Context(device, flags, hbm_budget_bytes)
+        self.scenes = list(scene_list)
+        self.slots = []
+        for k, sc in enumerate(self.scenes):
+            sid = 0 if k == 0 else self.ctx.scene_create()
+            self.ctx.scene_select(sid)
+            load_scene(self.ctx, sc)
+            self.slots.append(sid)
+        self.ctx.scene_select(0)
+
+    def jobs(self, fxaa=True) -> np.ndarray:
+        j = np.zeros(len(self.scenes), JOB)
+        for k, sc in enumerate(self.scenes):
+            j[k]["scene"] = self.slots[k]
+            j[k]["width"], j[k]["height"] = sc.width, sc.height
+            j[k]["fxaa"] = 1 if fxaa else 0
+            j[k]["ubo"] = sc.ubo[0] if sc.ubo.shape else sc.ubo
+        return j
+
+    def render(self, jobs=None, fxaa=True):
+        jobs = self.jobs(fxaa) if jobs is None else jobs
+        self.ctx.render_batch(jobs)
+        return [self.ctx.batch_download(k) for k in range(len(jobs))]

@@ -488,3 +488,116 @@ def _mesh_vertex_count(scene: Scene, b: int) -> int:
 
 def mesh_vertex_count(scene: Scene, b: int) -> int:
     return _mesh_vertex_count(scene, b)
+
+
+# ----------------------------------------------------------------------------- batched scenes
+
+C2_RESOLUTIONS = ((320, 180), (640, 360), (1280, 720), (1920, 1080))
+_MESH_CACHE: dict = {}
+
+
+def _catalog_mesh(kind: str) -> Mesh:
+    """The seed-free meshes of the game-frame set, built once per process."""
+    if kind not in _MESH_CACHE:
+        if kind.startswith("ico"):
+            _MESH_CACHE[kind] = icosphere(int(kind[3:]))
+        elif kind == "torus_a":
+            _MESH_CACHE[kind] = torus(64, 32, 1.0, 0.35)
+        else:
+            _MESH_CACHE[kind] = torus(64, 32, 1.0, 0.18)
+    return _MESH_CACHE[kind]
+
+
+C2_KINDS = ("ico3", "ico4", "ico5", "ico6", "torus_a", "torus_b", "heightfield")
+C2_KIND_TRIS = (1280, 5120, 20480, 81920, 4096, 4096, 130050)
+
+
+def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int, num_samples: int,
+                max_recursions: int, hf_n: int = 256) -> Scene:
+    """One scene of the batched workload, built from the game-frame meshes (icospheres subdiv 3-6,
+    the two 64x32 tori, 256x256 heightfields): instances are added until the instanced triangle
+    count reaches ``target_tris`` (to within the smallest mesh).
+
+    Draw order: per instance, the mesh kind (uniform over the kinds that still fit the remaining
+    budget; the smallest kind when none fits and the scene is still empty), then for a heightfield its
+    heights, then axis (2 draws), angle U[0,2pi), scale U[0.5,2], position (3 draws), material.
+    Objects spread over a square of half-size 12*sqrt(instances) at heights U[0.5,14]; heightfields
+    are terrain tiles (48 x 48 world units) laid on a grid under them.  The camera looks at the
+    centre from a distance proportional to the spread.
+    """
+    kinds_tris = dict(zip(C2_KINDS, C2_KIND_TRIS))
+    if hf_n != 256:
+        kinds_tris["heightfield"] = 2 * (hf_n - 1) ** 2
+    chosen = []
+    remaining = float(target_tris)
+    while True:
+        fits = [k for k in C2_KINDS if kinds_tris[k] <= remaining]
+        if not fits:
+            if chosen:
+                break
+            fits = [min(C2_KINDS, key=lambda k: kinds_tris[k])]
+        kind = fits[min(int(rng.uniform(1, 0, len(fits))[0]), len(fits) - 1)]
+        chosen.append(kind)
+        remaining -= kinds_tris[kind]
+    # one BLAS per distinct seed-free kind, one per heightfield instance (each has its own heights)
+    parts, blas_of = [], {}
+    n = len(chosen)
+    spread = 12.0 * math.sqrt(n)
+    inst = np.zeros(n, dtype=INSTANCE)
+    mats = np.zeros(n, dtype=MATERIAL)
+    hf_k = 0
+    grid = max(1, int(math.ceil(math.sqrt(sum(1 for k in chosen if k == "heightfield")))))
+    for i, kind in enumerate(chosen):
+        if kind == "heightfield":
+            parts.append((heightfield(rng, hf_n), None))
+            b = len(parts) - 1
+        else:
+            if kind not in blas_of:
+                parts.append((_catalog_mesh(kind), None))
+                blas_of[kind] = len(parts) - 1
+            b = blas_of[kind]
+        axis = _random_axis(rng)
+        angle = rng.uniform(1, 0, 2 * math.pi)[0]
+        scale = rng.uniform(1, 0.5, 2.0)[0]
+        p = np.array([rng.uniform(1, -spread, spread)[0], rng.uniform(1, 0.5, 14)[0], rng.uniform(1, -spread, spread)[0]])
+        mats[i] = random_materials(rng, 1)[0]
+        if kind == "heightfield":
+            gx, gz = hf_k % grid, hf_k // grid
+            m3 = np.eye(3) * (48.0 / (hf_n - 1))
+            p = np.array([-24.0 * grid + 48.0 * gx, -0.5, -24.0 * grid + 48.0 * gz])
+            hf_k += 1
+            mats[i] = _material(mats[i]["diffuse"], roughness=float(mats[i]["roughness"]), reflectivity=0.3, effect_id=1)
+        else:
+            m3 = _rot_axis_angle(axis, angle) * scale
+        t = np.zeros((3, 4))
+        t[:, :3], t[:, 3] = m3, p
+        inst[i]["transform"] = t.astype(np.float32)
+        inst[i]["blas"], inst[i]["mask"], inst[i]["materialBufferOffset"] = b, 0xFF, i
+    parts = [(m, np.zeros(len(m.positions), np.uint32)) for m, _ in parts]
+    eye = (0.0, 0.6 * spread + 8.0, -2.2 * spread - 10.0)
+    ubo = make_ubo(eye, (0, 2, 0), 60.0, width, height, (-0.4, -1.0, 0.3), num_samples, max_recursions)
+    return _finish(name, parts, mats, inst, ubo, width, height)
+
+
+def batch_scenes(n=64, seed=2, tri_range=(1e3, 4e6), resolutions=C2_RESOLUTIONS, samples=(1, 4), depths=(1, 6),
+                 hf_n=256) -> list:
+    """The batched-rendering workload: ``n`` independent scenes with triangle counts log-uniform in
+    ``tri_range``, resolution uniform over ``resolutions``, samples uniform in ``samples`` and
+    recursion depth uniform in ``depths`` (both inclusive).
+
+    Draw order per scene: log10(triangles), resolution index, samples, depth, then the scene's own
+    draws (batch_scene)."""
+    rng = Rng(seed)
+    lo, hi = math.log10(tri_range[0]), math.log10(tri_range[1])
+    out = []
+    for k in range(n):
+        target = 10.0 ** rng.uniform(1, lo, hi)[0]
+        w, h = resolutions[min(int(rng.uniform(1, 0, len(resolutions))[0]), len(resolutions) - 1)]
+        spp = samples[0] + min(int(rng.uniform(1, 0, samples[1] - samples[0] + 1)[0]), samples[1] - samples[0])
+        depth = depths[0] + min(int(rng.uniform(1, 0, depths[1] - depths[0] + 1)[0]), depths[1] - depths[0])
+        out.append(batch_scene(rng, f"batch{k:02d}", target, w, h, spp, depth, hf_n))
+    return out
+
+
+def c2_scenes() -> list:
+    return batch_scenes()

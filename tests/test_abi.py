@@ -59,3 +59,25 @@ def test_c1_scene_sizes():
     assert len(s.instances) == 1024
     assert 11_000_000 < s.instanced_tri_count < 13_000_000
     assert s.meshes["triCount"].tolist() == [1280, 5120, 20480, 81920, 4096, 4096, 130050, 130050]
+
+
+def test_batch_scene_generators():
+    from test_gpu_batch import mini_batch
+    scenes = mini_batch()
+    assert len({(s.width, s.height) for s in scenes}) >= 3
+    assert len({int(s.ubo["maxRecursions"][0]) for s in scenes}) >= 3
+    assert all(1 <= int(s.ubo["numSamples"][0]) <= 3 for s in scenes)
+    c2 = S.c2_scenes()
+    assert len(c2) == 64
+    assert {(s.width, s.height) for s in c2} <= set(S.C2_RESOLUTIONS)
+    assert {int(s.ubo["numSamples"][0]) for s in c2} == {1, 2, 3, 4}
+    assert {int(s.ubo["maxRecursions"][0]) for s in c2} == {1, 2, 3, 4, 5, 6}
+    tris = np.array([s.instanced_tri_count for s in c2])
+    assert tris.min() >= 1000 and tris.max() <= 4_000_000
+    assert np.median(np.log10(tris)) > 3.5  # log-uniform over [3, 6.6]
+    again = S.c2_scenes()
+    assert all(np.array_equal(a.instances, b.instances) for a, b in zip(c2, again))
+
+
+def test_job_layout(rg):
+    assert rg.JOB.itemsize == 208 and rg.JOB.fields["ubo"][1] == 16

@@ -1,0 +1,190 @@
+"""Batched rendering (rg_render_batch): several scenes resident in one context (one scene slot
+each), rendered by one wavefront loop in which finished path slots start the next job's work.
+
+* every job's image equals the single-scene render of the same scene, bit for bit (the same
+  kernels run on the same inputs; only the order rays are taken in changes), and so the oracle;
+* ray counts of the batch are the sum of the single renders' counts;
+* a small path pool (forced regeneration) and every traversal launch shape / ray-sort key of the
+  autotuner's grid give the same images;
+* the golden fixtures of the reference shaders, rendered as one batch, match their images;
+* misuse returns status codes.
+"""
+import numpy as np
+import pytest
+
+from raygun_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+RAY_KEYS = ("primary", "shadow", "secondary", "masked")
+
+
+def mini_batch(n=6, seed=7):
+    return S.batch_scenes(n=n, seed=seed, tri_range=(1e3, 6e4), resolutions=((40, 24), (64, 36), (96, 54), (33, 17)),
+                          samples=(1, 3), depths=(1, 6), hf_n=33)
+
+
+@pytest.fixture(scope="module")
+def batch(rg):
+    scenes = mini_batch()
+    singles, stats = [], []
+    for sc in scenes:
+        rt = rg.Raytracer(sc).prepare()
+        singles.append(rt.render())
+        stats.append(rt.ctx.stats())
+        rt.ctx.close()
+    return scenes, singles, stats
+
+
+def test_batch_equals_single_renders(rg, batch):
+    scenes, singles, stats = batch
+    br = rg.BatchRenderer(scenes)
+    imgs = br.render()
+    st = br.ctx.stats()
+    for k, (img, ref) in enumerate(zip(imgs, singles)):
+        assert img.shape == ref.shape
+        assert np.array_equal(img, ref), f"job {k}"
+    for key in RAY_KEYS:
+        assert st[key] == sum(s[key] for s in stats), key
+    assert st["stack_overflows"] == 0
+
+
+def test_path_regeneration_small_pool(rg, batch):
+    scenes, singles, _ = batch
+    br = rg.BatchRenderer(scenes)
+    br.ctx.set_batch_slots(1024)  # far fewer slots than samples: most slots run several paths
+    for k, (img, ref) in enumerate(zip(br.render(), singles)):
+        assert np.array_equal(img, ref), f"job {k}"
+
+
+@pytest.mark.parametrize("threads", [64, 128, 256])
+@pytest.mark.parametrize("depth", [16, 24, 32, 48])
+def test_launch_shapes(rg, batch, threads, depth):
+    scenes, singles, _ = batch
+    br = rg.BatchRenderer(scenes)
+    br.ctx.set_batch_tune(threads, depth, "none")
+    imgs = br.render()
+    assert br.ctx.stats()["stack_overflows"] == 0
+    for k, (img, ref) in enumerate(zip(imgs, singles)):
+        assert np.array_equal(img, ref), f"job {k} threads {threads} depth {depth}"
+
+
+@pytest.mark.parametrize("key", ["octant", "morton"])
+def test_ray_sort_keys(rg, batch, key):
+    scenes, singles, stats = batch
+    br = rg.BatchRenderer(scenes)
+    br.ctx.set_batch_tune(128, 32, key)
+    br.ctx.set_batch_slots(2048)
+    imgs = br.render()
+    st = br.ctx.stats()
+    for k, (img, ref) in enumerate(zip(imgs, singles)):
+        assert np.array_equal(img, ref), f"job {k} sort {key}"
+    for name in RAY_KEYS:
+        assert st[name] == sum(s[name] for s in stats), name
+
+
+def test_batch_vs_oracle(rg, orc):
+    from test_gpu_parity import assert_image_close
+    scenes = mini_batch(n=3, seed=11)
+    br = rg.BatchRenderer(scenes)
+    imgs = br.render()
+    st = br.ctx.stats()
+    total = {k: 0 for k in RAY_KEYS}
+    for sc, img in zip(scenes, imgs):
+        ob, on, orr, ost = orc.OracleScene(sc).render()
+        for k in RAY_KEYS:
+            total[k] += ost[k]
+        assert_image_close(img, orc.post(sc.ubo, ob, on, orr), sc.name)
+    for k in RAY_KEYS:
+        assert st[k] == total[k], k
+
+
+def test_golden_fixtures_as_one_batch(rg):
+    from test_golden import FIXTURES, load
+    from test_gpu_parity import assert_image_close
+    pairs = [load(p) for p in FIXTURES]
+    br = rg.BatchRenderer([sc for sc, _ in pairs])
+    imgs = br.render()
+    st = br.ctx.stats()
+    assert st["primary"] + st["shadow"] + st["secondary"] == sum(int(g["rays"][0]) for _, g in pairs)
+    for (sc, g), img in zip(pairs, imgs):
+        assert_image_close(img, g["final"], f"{sc.name} final (batched)")
+
+
+def test_same_scene_two_cameras(rg):
+    sc = S.spheres_scene(n_spheres=12, width=48, height=27, num_samples=2, max_recursions=3, seed=13)
+    moved = S.make_ubo((6, 4, -12), (0, 1, 0), 50.0, 40, 30, (-0.4, -1.0, 0.3), 1, 4)
+    rt = rg.Raytracer(sc).prepare()
+    ref_a = rt.render()
+    rt.ctx.set_resolution(40, 30)
+    ref_b = rt.render(moved)
+    br = rg.BatchRenderer([sc])
+    jobs = np.concatenate([br.jobs(), br.jobs()])
+    jobs[1]["width"], jobs[1]["height"], jobs[1]["ubo"] = 40, 30, moved[0]
+    br.ctx.render_batch(jobs)
+    assert np.array_equal(br.ctx.batch_download(0), ref_a)
+    assert np.array_equal(br.ctx.batch_download(1), ref_b)
+
+
+def test_scene_slots_are_independent(rg):
+    a = S.spheres_scene(n_spheres=8, width=32, height=18, num_samples=1, max_recursions=2, seed=21)
+    b = S.spheres_scene(n_spheres=20, width=32, height=18, num_samples=1, max_recursions=2, seed=22)
+    ctx = rg.Context()
+    ctx.set_resolution(32, 18)
+    rg.load_scene(ctx, a)
+    ctx.render(a.ubo)
+    first = ctx.download().copy()
+    sb = ctx.scene_create()
+    assert sb != 0
+    ctx.scene_select(sb)
+    rg.load_scene(ctx, b)
+    ctx.render(b.ubo)
+    img_b = ctx.download().copy()
+    assert not np.array_equal(first, img_b)
+    assert ctx.scene_bytes(sb) > 0
+    ctx.scene_select(0)
+    ctx.render(a.ubo)
+    assert np.array_equal(ctx.download(), first)
+    ctx.scene_destroy(sb)
+    with pytest.raises(rg.RgError):
+        ctx.scene_bytes(sb)
+    again = ctx.scene_create()  # a freed slot id is reused
+    assert again == sb
+
+
+def test_batch_errors(rg):
+    sc = S.spheres_scene(n_spheres=4, width=16, height=8, num_samples=1, max_recursions=1, seed=1)
+    br = rg.BatchRenderer([sc])
+    ctx = br.ctx
+    jobs = br.jobs()
+    bad = jobs.copy()
+    bad[0]["scene"] = 7
+    with pytest.raises(rg.RgError) as e:
+        ctx.render_batch(bad)
+    assert e.value.code == -1
+    empty_slot = ctx.scene_create()
+    bad = jobs.copy()
+    bad[0]["scene"] = empty_slot
+    with pytest.raises(rg.RgError) as e:
+        ctx.render_batch(bad)
+    assert e.value.code == -4  # no TLAS in that slot
+    bad = jobs.copy()
+    bad[0]["ubo"]["numSamples"] = 0
+    with pytest.raises(rg.RgError):
+        ctx.render_batch(bad)
+    bad = jobs.copy()
+    bad[0]["width"] = 0
+    with pytest.raises(rg.RgError):
+        ctx.render_batch(bad)
+    with pytest.raises(rg.RgError):
+        ctx.render_batch(jobs[:0])
+    with pytest.raises(rg.RgError):
+        ctx.set_batch_tune(96, 48, "none")
+    with pytest.raises(rg.RgError):
+        ctx.set_batch_tune(128, 20, "none")
+    with pytest.raises(rg.RgError):
+        ctx.scene_destroy(0)  # the selected slot
+    ctx.render_batch(jobs)
+    with pytest.raises(rg.RgError):
+        ctx.batch_download(1)
+    assert ctx.batch_download(0).shape == (8, 16, 4)
