@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=54, help="rows of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", default="1920x1080", help="WxH; smaller sizes are for profiling captures only")
+    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch"],
+                    help="game-frame: the 1080p 4x SSAA frame loop; batch: 64 independent scenes per step")
+    ap.add_argument("--no-tune", action="store_true", help="batch: skip the autotuner (default launch shape)")
+    ap.add_argument("--batch-scenes", type=int, default=64, help="batch: scenes per batch (profiling captures only)")
     return ap.parse_args()
 
 
@@ -336,6 +340,158 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+BATCH_WORKLOAD = "batched rendering: {n} independent scenes (instanced tris log-uniform 1k-4M from the game-frame meshes), " \
+                 "resolution uniform over 320x180/640x360/1280x720/1920x1080, 1-4 spp, depth 1-6; one CUDA-graph launch " \
+                 "per batch (device-side round loop), per-scene roughness + composite + FXAA"
+
+
+def run_batch(args):
+    import torch
+    from raygun_gb300 import build as rgbuild, rgcuda
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    rgbuild.build()
+    scenes = S.batch_scenes(n=args.batch_scenes)
+    br = rgcuda.BatchRenderer(scenes, device=local)
+    ctx = br.ctx
+    jobs = br.jobs()
+    K, W = args.steps, args.warmup
+    dev = torch.device("cuda", local)
+    ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    pixels = [sc.width * sc.height for sc in scenes]
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        ctx.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    tune, table = None, None
+    t_tune = time.perf_counter()
+    if not args.no_tune:
+        tune, table = ctx.autotune_batch(jobs, reps=1)
+    t_tune = time.perf_counter() - t_tune
+
+    # ---------------- value: scenes and job table resident, one graph launch per batch ----------------
+    for _ in range(W):
+        ctx.render_batch(jobs)
+    barrier()
+    ctx.timings()
+    ctx.reset_total_stats()
+    launches0 = rgcuda.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(ext)
+    for _ in range(K):
+        ctx.render_batch(jobs)
+    e1.record(ext)
+    barrier()
+    clk = clocks.stop()
+    launches = rgcuda.launch_count() - launches0
+    tot = ctx.total_stats()
+    rays = tot["primary"] + tot["shadow"] + tot["secondary"]
+    value, ms = replica_throughput(rays, e0.elapsed_time(e1), world, dev)
+
+    # ---------------- e2e: job table from host memory, every image read back to pinned host memory ----
+    fb_pin = torch.empty(sum(pixels) * 16, dtype=torch.uint8).pin_memory()
+    fb_host = fb_pin.numpy()
+    offs = np.concatenate([[0], np.cumsum(pixels)]) * 16
+
+    def step_host():
+        ctx.render_batch(jobs)
+        for k, sc in enumerate(scenes):
+            ctx.batch_download(k, fb_host[offs[k]:offs[k + 1]].view(np.float32).reshape(sc.height, sc.width, 4))
+
+    for _ in range(W):
+        step_host()
+    barrier()
+    ctx.reset_total_stats()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        step_host()
+    barrier()
+    dt = (time.perf_counter() - t0) * 1e3
+    tot2 = ctx.total_stats()
+    e2e_value, ms_e2e = replica_throughput(tot2["primary"] + tot2["shadow"] + tot2["secondary"], dt, world, dev)
+    e2e = {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(rgcuda.JOB.itemsize * len(jobs)),
+           "d2h_bytes_per_step": int(sum(pixels) * 16), "ms_per_step": ms_e2e / K,
+           "timing": "host wall clock around K batches, each followed by the read-back of every image (synchronous)"}
+
+    # ---------------- roofline of the traversal launches (host-polled loop with events) ----------------
+    ctx.set_flags(rgcuda.RG_FLAG_COUNT_VISITS)
+    ctx.render_batch(jobs)
+    barrier()
+    cst = ctx.stats()
+    ctx.set_flags(rgcuda.RG_FLAG_KERNEL_TIMING)
+    ctx.timings()
+    ctx.render_batch(jobs)
+    barrier()
+    tm = ctx.timings()
+    ctx.set_flags(0)
+    crays = cst["primary"] + cst["shadow"] + cst["secondary"]
+    bytes_batch = crays * BYTES_RAY + cst["nodes"] * BYTES_NODE + cst["tris"] * BYTES_TRI
+    trace_ms = tm["traceKernelSum"] / max(tm["frames"], 1)
+    achieved = bytes_batch / (trace_ms * 1e-3) / 1e9
+    peak, peak_src = measured_peak_hbm()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "k_wf_trace (batch form) + k_wf_tail: every traversal launch of one batch",
+                "launches_per_batch": tm["traceLaunches"] / max(tm["frames"], 1), "peak_source": f"{peak_src} hbm_gbs",
+                "algorithmic_bytes_per_batch": bytes_batch, "bytes_per_ray": bytes_batch / max(crays, 1),
+                "node_visits_per_ray": cst["nodes"] / max(crays, 1), "tri_tests_per_ray": cst["tris"] / max(crays, 1),
+                "trace_kernel_ms_per_batch": trace_ms}
+
+    out = {
+        "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded procedural scenes (no dataset)",
+        "config": {"workload": BATCH_WORKLOAD.format(n=len(scenes)), "scenes": len(scenes),
+                   "instanced_tris": int(sum(sc.instanced_tri_count for sc in scenes)),
+                   "unique_tris": int(sum(sc.tri_count for sc in scenes)), "pixels": int(sum(pixels)),
+                   "samples": int(sum(p * int(sc.ubo["numSamples"][0]) for p, sc in zip(pixels, scenes))),
+                   "l2": "inputs larger than L2 (path state and scene BVHs of the batch are several GB)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "batches_per_s": K / (ms * 1e-3), "rays_per_batch": rays / K,
+        "autotune": None if tune is None else {
+            "chosen": {"threads": tune["threads"], "stack_depth": tune["stack_depth"],
+                       "sort_key": {v: k for k, v in rgcuda.SORT_KEYS.items()}[tune["sort_key"]]},
+            "seconds": t_tune,
+            "ms_per_batch": {f"{t}x{d}/{k}": (None if v is None else round(v, 3)) for (t, d, k), v in table.items()}},
+        "e2e": e2e, "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_batch(scenes)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline_batch(scenes, every=1, row_step=1):
+    """The oracle on all host cores over a sample of the batch: every `every`-th scene, every
+    `row_step`-th row of each (default: the whole batch, a few seconds on 16 cores)."""
+    import oracle
+    nthreads = os.cpu_count() or 1
+    rays, dt, n = 0, 0.0, 0
+    for sc in scenes[::every]:
+        o = oracle.OracleScene(sc)
+        step = row_step
+        t = time.perf_counter()
+        _, _, _, st = o.render(rows=(0, sc.height), row_step=step, nthreads=nthreads)
+        dt += time.perf_counter() - t
+        rays += st["primary"] + st["shadow"] + st["secondary"]
+        n += 1
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "sample": f"{n} scenes (every {every}th), every {row_step}th row of each: {rays} rays in {dt:.2f} s (trace + shade)"}
+
+
 def cpu_baseline(orc_scene, sc, rows):
     """The oracle on all host cores over `rows` rows spread evenly over frame 0."""
     nthreads = os.cpu_count() or 1
@@ -395,6 +551,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -42,6 +42,7 @@ typedef struct {
 #define RG_FLAG_COUNT_VISITS 2u /* count BVH node / triangle visits (roofline accounting) */
 #define RG_FLAG_MEGAKERNEL 4u   /* trace + shade in one persistent kernel instead of the wavefront loop */
 #define RG_FLAG_KERNEL_TIMING 8u /* CUDA events around every traversal launch (rg_timings.traceKernel) */
+#define RG_FLAG_HOST_LOOP 16u    /* rg_render_batch: host-polled round loop instead of the CUDA graph */
 
 /* resources/shaders/vertex.def:3-7 (render/vertex.hpp:27-29): 32 B */
 typedef struct {
@@ -233,7 +234,10 @@ typedef struct rg_batch_tune {
  * finish take the next job's work), then each job's samples are resolved and run through the
  * roughness, postprocess and FXAA passes into its own RGBA32F image.  Each image equals what
  * rg_render of that job's scene, resolution and UBO produces.  rg_get_stats then counts the rays
- * of the whole batch. */
+ * of the whole batch.  The batch runs as one CUDA graph launch whose round loop is a device-side
+ * while node (re-captured only when the batch's shape changes: job sizes, samples, post options,
+ * tune); RG_FLAG_HOST_LOOP, RG_FLAG_KERNEL_TIMING and RG_FLAG_COUNT_VISITS use the host-polled
+ * loop instead.  In graph mode rg_timings.rtOnly covers the whole batch (post included). */
 rg_status rg_render_batch(rg_ctx* ctx, const rg_job* jobs, uint32_t n);
 /* Device pointer of job `job`'s RGBA32F image of the last batch (width*height*4 floats). */
 rg_status rg_batch_framebuffer(rg_ctx* ctx, uint32_t job, float** d_rgba);
@@ -243,6 +247,14 @@ rg_status rg_set_batch_tune(rg_ctx* ctx, const rg_batch_tune* tune);
 rg_status rg_get_batch_tune(rg_ctx* ctx, rg_batch_tune* out);
 /* Path slots of the batch loop (default 2^23; about 1.6 KB of device memory each). */
 rg_status rg_set_batch_slots(rg_ctx* ctx, uint32_t slots);
+/* Autotuner of the batch loop: renders the batch once (warm-up, capture) and then `reps` times
+ * with every launch shape of the grid threads {64,128,256} x stack depth {16,24,32,48} x sort key
+ * {none, octant, morton} (36 configurations, in that nesting order), keeps the fastest one whose
+ * render had no traversal-stack overflow (the results of every configuration are identical unless
+ * the stack overflows) and selects it.  ms_out (nullable, 36 floats): mean milliseconds per batch
+ * of each configuration, -1 where the stack overflowed.  No reference counterpart. */
+#define RG_AUTOTUNE_CONFIGS 36
+rg_status rg_autotune_batch(rg_ctx* ctx, const rg_job* jobs, uint32_t n, uint32_t reps, rg_batch_tune* best, float* ms_out);
 
 /* ---- parity / inspection entry points (no reference counterpart: the Vulkan driver's BVHs are
  * opaque) ---- */

@@ -105,6 +105,17 @@ struct rg_ctx {
     std::vector<uint32_t> batchW, batchH;
     uint32_t batchSlots = 1u << 23;            // path slots of the batch loop (path state ~1.6 KB each)
     TraceTune tune;
+    // graph form of the batch: second stream (loop body capture), instantiated graph and what it
+    // was captured for, loop words (device), launch accounting
+    cudaStream_t stream2 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    std::vector<uint8_t> graphKey;
+    DevBuf loopWords;
+    uint64_t graphFixedKernels = 0;
+    int graphBodyKernels = 0;
+    uint32_t bodyRunsSeen = 0;
+    bool graphPending = false;
     std::vector<FrameEvents*> evPool, evPending;
     FrameEvents* evCur = nullptr;  // ranges recorded since the last frame
     rg_timings lastTimings{};
@@ -153,6 +164,22 @@ rg_status ensure(rg_ctx* c, DevBuf& b, size_t bytes) {
     }
     b.cap = grow;
     c->allocated += grow;
+    return RG_OK;
+}
+
+// bookkeeping of finished batch-graph launches (call after the stream was synchronized): launch
+// accounting of the loop body runs, iteration count, the loop's iteration-limit flag
+rg_status settle_graph(rg_ctx* c) {
+    if (!c->graphPending) return RG_OK;
+    c->graphPending = false;
+    const uint32_t runs = c->hostCount[6];
+    count_launch((uint64_t)(runs - c->bodyRunsSeen) * (uint64_t)c->graphBodyKernels);
+    c->bodyRunsSeen = runs;
+    c->lastIterations = 2 * (int)c->hostCount[4];
+    if (c->hostCount[5]) {
+        CK(cudaMemsetAsync(c->loopWords.as<uint32_t>() + 1, 0, sizeof(uint32_t), c->stream));
+        return fail(c, RG_ERR_CUDA, "batch round loop stopped at its iteration limit");
+    }
     return RG_OK;
 }
 
@@ -378,7 +405,8 @@ rg_status rg_create(rg_ctx** out, const rg_device_opts* opts) {
         return RG_ERR_OUT_OF_MEMORY;
     }
     cudaMemsetAsync(c->counters.p, 0, 128, c->stream);
-    if (cudaHostAlloc(&c->hostCount, 4 * sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
+    if (cudaHostAlloc(&c->hostCount, 8 * sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
         rg_destroy(c);
         return RG_ERR_OUT_OF_MEMORY;
     }
@@ -411,6 +439,10 @@ rg_status rg_destroy(rg_ctx* c) {
         for (auto& e : f->kernel) cudaEventDestroy(e);
         delete f;
     }
+    if (c->graphExec) cudaGraphExecDestroy(c->graphExec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    release(c, c->loopWords);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->hostCount) cudaFreeHost(c->hostCount);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -661,6 +693,7 @@ rg_status rg_download(rg_ctx* c, float* host) {
     TRY(set_device(c));
     CK(cudaMemcpyAsync(host, c->fb.p, 16ull * c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    TRY(settle_graph(c));
     return RG_OK;
 }
 
@@ -699,6 +732,7 @@ rg_status rg_download_image(rg_ctx* c, int32_t which, float* host) {
     if (h16) CK(h16_to_f32(h16, c->tmpB.as<float4>(), px, c->stream));
     CK(cudaMemcpyAsync(host, c->tmpB.p, 16 * px, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    TRY(settle_graph(c));
     return RG_OK;
 }
 
@@ -706,6 +740,7 @@ rg_status rg_synchronize(rg_ctx* c) {
     if (!c) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
     CK(cudaStreamSynchronize(c->stream));
+    TRY(settle_graph(c));
     return RG_OK;
 }
 
@@ -713,6 +748,7 @@ rg_status rg_get_timings(rg_ctx* c, rg_timings* t) {
     if (!c || !t) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
     CK(cudaStreamSynchronize(c->stream));
+    TRY(settle_graph(c));
     auto el = [&](cudaEvent_t a, cudaEvent_t b) {
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
@@ -757,6 +793,7 @@ static rg_status read_stats(rg_ctx* c, rg_stats* s, int base) {
     unsigned long long v[16];
     CK(cudaMemcpyAsync(v, c->counters.p, 128, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    TRY(settle_graph(c));
     s->primary = v[base + 0];
     s->shadow = v[base + 1];
     s->secondary = v[base + 2];
@@ -880,6 +917,113 @@ rg_status rg_lbvh_build_host(rg_ctx* c, const float* boxes, uint32_t n, uint32_t
 }
 
 }  // extern "C"
+
+
+// ---- batch helpers ----------------------------------------------------------------------------------
+namespace {
+
+// per job: resolve of its samples, roughness + postprocess + FXAA into its slice of batchFb
+cudaError_t enqueue_batch_posts(rg_ctx* c, const JobDesc* jd, const rg_job* jobs, uint32_t n) {
+    for (uint32_t j = 0; j < n; ++j) {
+        const JobDesc& d = jd[j];
+        cudaError_t e = launch_resolve_job(c->samples.as<float4>(), d, c->bBase.as<uint2>(), c->bNormal.as<uint2>(),
+                                           c->bRough.as<uint2>(), c->stream);
+        if (e != cudaSuccess) return e;
+        PostParams pp;
+        std::memset(&pp, 0, sizeof(pp));
+        pp.W = d.W;
+        pp.H = d.H;
+        pp.base = c->bBase.as<uint2>();
+        pp.normal = c->bNormal.as<uint2>();
+        pp.rough = c->bRough.as<uint2>();
+        pp.finalImg = c->bFinal.as<uint2>();
+        pp.fxaaOut = c->bFxaa.as<uint2>();
+        pp.framebuffer = c->batchFb.as<float4>() + c->batchOffset[j];
+        for (int k = 0; k < 4; ++k) pp.fade[k] = d.ubo.fadeColor[k];
+        pp.showAlpha = d.ubo.showAlpha ? 1 : 0;
+        pp.fxaa = jobs[j].fxaa ? 1 : 0;
+        if ((e = launch_rough_post(pp, c->stream)) != cudaSuccess) return e;
+        if ((e = launch_fxaa(pp, c->stream)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <class T>
+void key_put(std::vector<uint8_t>& k, const T& v) {
+    const uint8_t* b = reinterpret_cast<const uint8_t*>(&v);
+    k.insert(k.end(), b, b + sizeof(T));
+}
+
+// what a captured batch graph depends on besides the job table's contents (scenes, cameras)
+std::vector<uint8_t> batch_graph_key(rg_ctx* c, const TraceParams& tp, const SortScratch& sort, const JobDesc* jd,
+                                     const rg_job* jobs, uint32_t n) {
+    std::vector<uint8_t> k;
+    key_put(k, tp);
+    key_put(k, c->tune);
+    key_put(k, sort);
+    const void* ptrs[] = {c->bBase.p, c->bNormal.p, c->bRough.p, c->bFinal.p, c->bFxaa.p, c->batchFb.p, c->loopWords.p,
+                          c->hostCount};
+    key_put(k, ptrs);
+    for (uint32_t j = 0; j < n; ++j) {
+        key_put(k, jd[j].W);
+        key_put(k, jd[j].H);
+        key_put(k, jd[j].S);
+        key_put(k, jd[j].sampleBase);
+        key_put(k, jd[j].ubo.fadeColor);
+        key_put(k, jd[j].ubo.showAlpha);
+        key_put(k, jobs[j].fxaa);
+        key_put(k, c->batchOffset[j]);
+    }
+    return k;
+}
+
+rg_status launch_batch_graph(rg_ctx* c, const TraceParams& tp, const SortScratch& sort, const JobDesc* jd, const rg_job* jobs,
+                             uint32_t n) {
+    if (!c->loopWords.p) {
+        TRY(ensure(c, c->loopWords, 16));
+        CK(cudaMemsetAsync(c->loopWords.p, 0, 16, c->stream));
+        c->bodyRunsSeen = 0;
+    }
+    std::vector<uint8_t> key = batch_graph_key(c, tp, sort, jd, jobs, n);
+    if (!c->graphExec || key != c->graphKey) {
+        if (c->graphExec) cudaGraphExecDestroy(c->graphExec);
+        if (c->graph) cudaGraphDestroy(c->graph);
+        c->graphExec = nullptr;
+        c->graph = nullptr;
+        c->graphKey.clear();
+        const uint64_t before = g_launches.load();
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+        cudaError_t e = capture_trace_batch(tp, c->tune, sort, c->stream, c->stream2, c->loopWords.as<uint32_t>());
+        const uint64_t postsBefore = g_launches.load();
+        if (e == cudaSuccess) e = enqueue_batch_posts(c, jd, jobs, n);
+        const uint64_t posts = g_launches.load() - postsBefore;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->hostCount + 4, c->loopWords.p, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+        g_launches.store(before);  // captured launches are counted when the graph runs
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return fail(c, RG_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        cudaError_t e3 = cudaGraphInstantiate(&c->graphExec, g, 0);
+        if (e3 != cudaSuccess) {
+            cudaGraphDestroy(g);
+            c->graphExec = nullptr;
+            return fail(c, RG_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e3));
+        }
+        c->graph = g;
+        c->graphKey = std::move(key);
+        c->graphFixedKernels = (uint64_t)batch_graph_kernels(c->tune, &c->graphBodyKernels) + posts;
+    }
+    CK(cudaGraphLaunch(c->graphExec, c->stream));
+    count_launch(c->graphFixedKernels);
+    c->graphPending = true;
+    return RG_OK;
+}
+
+}  // namespace
 
 // ---- scene slots and batched rendering ------------------------------------------------------------
 extern "C" {
@@ -1022,46 +1166,95 @@ rg_status rg_render_batch(rg_ctx* c, const rg_job* jobs, uint32_t n) {
     tp.slotJob = c->slotJob.as<uint32_t>();
     tp.slotSample = c->slotSample.as<uint32_t>();
     CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
-    FrameEvents* fe;
-    TRY(cur_events(c, &fe));
-    CK(cudaEventRecord(fe->ev[EV_RT0], c->stream));
-    if (c->flags & RG_FLAG_KERNEL_TIMING)
-        CK(launch_trace_batch(tp, c->tune, sort, c->stream, c->hostCount, &c->lastIterations, next_kernel_events, fe));
-    else
-        CK(launch_trace_batch(tp, c->tune, sort, c->stream, c->hostCount, &c->lastIterations));
-    CK(cudaEventRecord(fe->ev[EV_POST0], c->stream));
     c->batchOffset.assign(n, 0);
     c->batchW.assign(n, 0);
     c->batchH.assign(n, 0);
     size_t off = 0;
     for (uint32_t j = 0; j < n; ++j) {
-        const JobDesc& d = jd[j];
-        CK(launch_resolve_job(c->samples.as<float4>(), d, c->bBase.as<uint2>(), c->bNormal.as<uint2>(), c->bRough.as<uint2>(), c->stream));
-        PostParams pp;
-        std::memset(&pp, 0, sizeof(pp));
-        pp.W = d.W;
-        pp.H = d.H;
-        pp.base = c->bBase.as<uint2>();
-        pp.normal = c->bNormal.as<uint2>();
-        pp.rough = c->bRough.as<uint2>();
-        pp.finalImg = c->bFinal.as<uint2>();
-        pp.fxaaOut = c->bFxaa.as<uint2>();
-        pp.framebuffer = c->batchFb.as<float4>() + off;
-        for (int k = 0; k < 4; ++k) pp.fade[k] = d.ubo.fadeColor[k];
-        pp.showAlpha = d.ubo.showAlpha ? 1 : 0;
-        pp.fxaa = jobs[j].fxaa ? 1 : 0;
-        CK(launch_rough_post(pp, c->stream));
-        CK(launch_fxaa(pp, c->stream));
         c->batchOffset[j] = off;
-        c->batchW[j] = d.W;
-        c->batchH[j] = d.H;
-        off += (size_t)d.W * d.H;
+        c->batchW[j] = jd[j].W;
+        c->batchH[j] = jd[j].H;
+        off += (size_t)jd[j].W * jd[j].H;
+    }
+    FrameEvents* fe;
+    TRY(cur_events(c, &fe));
+    CK(cudaEventRecord(fe->ev[EV_RT0], c->stream));
+    const bool hostLoop = (c->flags & (RG_FLAG_HOST_LOOP | RG_FLAG_KERNEL_TIMING | RG_FLAG_COUNT_VISITS)) != 0;
+    if (hostLoop) {
+        if (c->flags & RG_FLAG_KERNEL_TIMING)
+            CK(launch_trace_batch(tp, c->tune, sort, c->stream, c->hostCount, &c->lastIterations, next_kernel_events, fe));
+        else
+            CK(launch_trace_batch(tp, c->tune, sort, c->stream, c->hostCount, &c->lastIterations));
+        CK(cudaEventRecord(fe->ev[EV_POST0], c->stream));
+        CK(enqueue_batch_posts(c, jd.data(), jobs, n));
+    } else {
+        TRY(launch_batch_graph(c, tp, sort, jd.data(), jobs, n));
+        CK(cudaEventRecord(fe->ev[EV_POST0], c->stream));
     }
     CK(cudaEventRecord(fe->ev[EV_ROUGH1], c->stream));
     CK(cudaEventRecord(fe->ev[EV_POST1], c->stream));
     fe->hasFrame = true;
     c->evPending.push_back(fe);
     c->evCur = nullptr;
+    return RG_OK;
+}
+
+rg_status rg_autotune_batch(rg_ctx* c, const rg_job* jobs, uint32_t n, uint32_t reps, rg_batch_tune* best, float* msOut) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    if (!jobs || n == 0 || reps == 0) return fail(c, RG_ERR_INVALID_ARG, "autotune needs jobs and reps >= 1");
+    TRY(set_device(c));
+    const int threads[3] = {64, 128, 256}, depths[4] = {16, 24, 32, 48}, keys[3] = {RG_SORT_NONE, RG_SORT_OCTANT, RG_SORT_MORTON};
+    const TraceTune saved = c->tune;
+    const uint32_t savedFlags = c->flags;
+    c->flags &= ~(uint32_t)(RG_FLAG_KERNEL_TIMING | RG_FLAG_COUNT_VISITS);  // time the production (graph) loop
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float bestMs = -1.0f;
+    TraceTune bestTune = saved;
+    rg_status st = RG_OK;
+    int idx = 0;
+    for (int ti = 0; ti < 3 && st == RG_OK; ++ti)
+        for (int di = 0; di < 4 && st == RG_OK; ++di)
+            for (int ki = 0; ki < 3 && st == RG_OK; ++ki, ++idx) {
+                c->tune.threads = threads[ti];
+                c->tune.depth = depths[di];
+                c->tune.sortKey = keys[ki];
+                float ms = -1.0f;
+                st = rg_render_batch(c, jobs, n);
+                rg_stats stats{};
+                if (st == RG_OK) st = read_stats(c, &stats, 0);
+                if (st == RG_OK && stats.stack_overflows == 0) {
+                    cudaError_t e = cudaEventRecord(e0, c->stream);
+                    for (uint32_t r = 0; r < reps && st == RG_OK && e == cudaSuccess; ++r) st = rg_render_batch(c, jobs, n);
+                    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    if (st == RG_OK) st = settle_graph(c);
+                    float el = 0.0f;
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&el, e0, e1);
+                    if (e != cudaSuccess && st == RG_OK) st = fail(c, RG_ERR_CUDA, cudaGetErrorString(e));
+                    ms = el / (float)reps;
+                    if (st == RG_OK && (bestMs < 0.0f || ms < bestMs)) {
+                        bestMs = ms;
+                        bestTune = c->tune;
+                    }
+                }
+                if (msOut) msOut[idx] = ms;
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->flags = savedFlags;
+    // the tuning renders are not frames of the caller's timeline
+    for (FrameEvents* f : c->evPending) c->evPool.push_back(f);
+    c->evPending.clear();
+    c->tune = st == RG_OK && bestMs >= 0.0f ? bestTune : saved;
+    if (st != RG_OK) return st;
+    if (bestMs < 0.0f) return fail(c, RG_ERR_STACK_OVERFLOW, "every configuration overflowed the traversal stack");
+    if (best) {
+        best->threads = c->tune.threads;
+        best->stack_depth = c->tune.depth;
+        best->sort_key = c->tune.sortKey;
+    }
     return RG_OK;
 }
 
@@ -1079,6 +1272,7 @@ rg_status rg_batch_download(rg_ctx* c, uint32_t job, float* host) {
     CK(cudaMemcpyAsync(host, c->batchFb.as<float4>() + c->batchOffset[job], 16ull * c->batchW[job] * c->batchH[job],
                        cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    TRY(settle_graph(c));
     return RG_OK;
 }
 

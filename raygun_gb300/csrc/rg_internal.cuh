@@ -217,6 +217,14 @@ struct SortScratch {
 // hostWords: two pinned words (queue length, work counter) polled every few rounds
 cudaError_t launch_trace_batch(const TraceParams& p, const TraceTune& tune, const SortScratch& sort, cudaStream_t s,
                                uint32_t* hostWords, int* iterations, EventPairFn kernelEvents = nullptr, void* user = nullptr);
+// graph form of launch_trace_batch, enqueued on stream s while it captures: prologue, a while node
+// (body captured on the idle stream s2: two trace/shade rounds and the device-side loop condition)
+// and the tail launch.  loopWords: 3 device words (body runs of the launch, sticky iteration-limit
+// flag, body runs in total), the last two zeroed by the caller once.
+cudaError_t capture_trace_batch(const TraceParams& p, const TraceTune& tune, const SortScratch& sort, cudaStream_t s,
+                                cudaStream_t s2, uint32_t* loopWords);
+// kernels of that graph outside the loop body; *perBody = kernels of one body run
+int batch_graph_kernels(const TraceTune& tune, int* perBody);
 // raygen.rgen:36-38 for one job of a batch: average its samples into RGBA16F G-buffers
 cudaError_t launch_resolve_job(const float4* samples, const JobDesc& hostJob, uint2* base, uint2* normal, uint2* rough,
                                cudaStream_t s);

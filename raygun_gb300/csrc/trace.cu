@@ -19,6 +19,8 @@
 // GLSL-undefined cases follow fixed policies: r/(tr+r) with tr+r == 0 -> 0; pow(x, n) with
 // integer n -> repeated multiply; a zero direction (refract at total internal reflection) -> no
 // traversal, miss shader; clamp/min/max treat a NaN operand as absent (fminf/fmaxf).
+#include <cstring>
+
 #include "rg_internal.cuh"
 
 namespace rg {
@@ -1586,6 +1588,78 @@ cudaError_t launch_trace_batch(const TraceParams& p0, const TraceTune& tune, con
         if (it >= kMaxIterations) return cudaErrorLaunchTimeout;
     }
     if (iterations) *iterations = it;
+    return cudaGetLastError();
+}
+
+// loop condition of the graph form: continue while rays are queued and either many are queued or
+// work items remain; stop (and flag) after maxIter body runs.  loop[0] = body runs, loop[1] = flag.
+__global__ void k_batch_continue(cudaGraphConditionalHandle h, const uint32_t* __restrict__ counts, const uint32_t* __restrict__ work,
+                                 uint32_t totalWork, uint32_t tailBelow, uint32_t maxIter, uint32_t* __restrict__ loop) {
+    const uint32_t c = *(volatile const uint32_t*)counts, it = loop[0] + 1u;
+    loop[0] = it;
+    loop[2] += 1u;  // body runs since the words were allocated (launch accounting)
+    bool more = c != 0u && (c >= tailBelow || *(volatile const uint32_t*)work < totalWork);
+    if (more && it >= maxIter) {
+        loop[1] = 1u;
+        more = false;
+    }
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+int batch_graph_kernels(const TraceTune& tune, int* perBody) {
+    const int round = 2 + (tune.sortKey != RG_SORT_NONE ? 3 : 0);
+    if (perBody) *perBody = 2 * round + 1;
+    return 2;  // raygen + tail
+}
+
+cudaError_t capture_trace_batch(const TraceParams& p0, const TraceTune& tune, const SortScratch& sort, cudaStream_t s,
+                                cudaStream_t s2, uint32_t* loopWords) {
+    TraceParams p = p0;
+    if (p.countVisits) return cudaErrorInvalidValue;  // the visit-counting build runs the host loop
+    const TraceKernel trace = trace_kernel(true, false, tune.threads, tune.depth);
+    if (!trace || !tune_supported(tune)) return cudaErrorInvalidValue;
+    const int gTrace = grid_of((const void*)trace, tune.threads);
+    const int gShade = grid_of((const void*)k_wf_shade<true>, 128);
+    const int gRaygen = grid_of((const void*)k_wfb_raygen, 256);
+    const int gTail = grid_of((const void*)k_wf_tail<true>, kTraceThreads);
+    const int gSort = grid_of((const void*)k_sort_scatter<RG_SORT_MORTON>, 256);
+    if (!gTrace || !gShade || !gRaygen || !gTail || !gSort) return cudaErrorUnknown;
+    const bool sorted = tune.sortKey != RG_SORT_NONE;
+    p.perm = sorted ? sort.valsA : nullptr;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(p.wf.counts, 0, 4 * sizeof(uint32_t), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(loopWords, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
+    if (sorted && (e = cudaMemsetAsync(sort.hist, 0, 4096 * sizeof(uint32_t), s)) != cudaSuccess) return e;
+    k_wfb_raygen<<<gRaygen, 256, 0, s>>>(p);
+    // while node after the prologue; its body is captured on s2
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if ((e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd)) != cudaSuccess) return e;
+    if (st != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureInvalidated;
+    cudaGraphConditionalHandle h;
+    if ((e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp)) != cudaSuccess) return e;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) != cudaSuccess) return e;
+    for (int q = 0; q < 2; ++q) {
+        if (sorted) enqueue_sort(p, tune.sortKey, sort, gSort, q, s2);
+        trace<<<gTrace, tune.threads, 0, s2>>>(p, q);
+        k_wf_shade<true><<<gShade, 128, 0, s2>>>(p, q);
+    }
+    k_batch_continue<<<1, 1, 0, s2>>>(h, p.wf.counts, p.workCounter, p.totalWork, (uint32_t)RG_TAIL_RAYS, 50000u, loopWords);
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(s2, &captured);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) != cudaSuccess) return e;
+    // after an even number of rounds the pending rays are in queue 0
+    k_wf_tail<true><<<gTail, kTraceThreads, 0, s>>>(p, 0);
     return cudaGetLastError();
 }
 

@@ -23,6 +23,7 @@ RG_FLAG_DEBUG_IMAGES = 1
 RG_FLAG_COUNT_VISITS = 2
 RG_FLAG_MEGAKERNEL = 4
 RG_FLAG_KERNEL_TIMING = 8
+RG_FLAG_HOST_LOOP = 16
 IMAGES = {"final": 0, "base": 1, "normal": 2, "rough": 3, "rough_transition": 4, "rough_colors_a": 5,
           "rough_colors_b": 6, "pre_fxaa": 7}
 
@@ -34,12 +35,18 @@ EXPORTS = [
     "rg_update_vertices_device", "rg_get_total_stats", "rg_reset_total_stats", "rg_set_flags", "rg_launch_count",
     "rg_lbvh_build_device_noalloc", "rg_scene_create", "rg_scene_select", "rg_scene_destroy", "rg_scene_bytes",
     "rg_render_batch", "rg_batch_framebuffer", "rg_batch_download", "rg_set_batch_tune", "rg_get_batch_tune",
-    "rg_set_batch_slots",
+    "rg_set_batch_slots", "rg_autotune_batch",
 ]
 
 # rg_job (include/rgcuda.h): one render of a batch
 JOB = np.dtype([("scene", "<u4"), ("width", "<u4"), ("height", "<u4"), ("fxaa", "<i4"), ("ubo", scenes.UBO)])
 SORT_KEYS = {"none": 0, "octant": 1, "morton": 2}
+AUTOTUNE_CONFIGS = 36
+
+
+def autotune_grid():
+    """Configurations of rg_autotune_batch in its order: (threads, stack depth, sort key name)."""
+    return [(t, d, k) for t in (64, 128, 256) for d in (16, 24, 32, 48) for k in ("none", "octant", "morton")]
 
 
 class DeviceOpts(ctypes.Structure):
@@ -122,6 +129,7 @@ def load(path: str = LIB_PATH):
         "rg_set_batch_tune": ([P, ctypes.POINTER(BatchTune)], I32),
         "rg_get_batch_tune": ([P, ctypes.POINTER(BatchTune)], I32),
         "rg_set_batch_slots": ([P, U32], I32),
+        "rg_autotune_batch": ([P, P, U32, U32, ctypes.POINTER(BatchTune), P], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -306,6 +314,19 @@ class Context:
         t = BatchTune()
         self._ck(self.L.rg_get_batch_tune(self.h, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in BatchTune._fields_}
+
+    def autotune_batch(self, jobs, reps=1):
+        """Selects the fastest traversal launch shape / ray-sort key for this batch; returns the
+        chosen tune and the table {(threads, depth, sort): ms or None (stack overflow)}."""
+        j = np.ascontiguousarray(jobs, dtype=JOB)
+        best = BatchTune()
+        ms = np.zeros(AUTOTUNE_CONFIGS, np.float32)
+        self._ck(self.L.rg_autotune_batch(self.h, _p(j), len(j), reps, ctypes.byref(best), _p(ms)))
+        self._batch = [(int(x["width"]), int(x["height"])) for x in j]
+        table = {}
+        for i, (t, d, k) in enumerate(autotune_grid()):
+            table[(t, d, k)] = None if ms[i] < 0 else float(ms[i])
+        return {k: getattr(best, k) for k, _ in BatchTune._fields_}, table
 
     def set_batch_slots(self, slots: int):
         self._ck(self.L.rg_set_batch_slots(self.h, slots))

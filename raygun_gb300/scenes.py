@@ -516,14 +516,15 @@ def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int
                 max_recursions: int, hf_n: int = 256) -> Scene:
     """One scene of the batched workload, built from the game-frame meshes (icospheres subdiv 3-6,
     the two 64x32 tori, 256x256 heightfields): instances are added until the instanced triangle
-    count reaches ``target_tris`` (to within the smallest mesh).
+    count reaches ``target_tris`` (to within the smallest mesh), over a ground quad (2 triangles,
+    floor material) so that every scene has a horizon.
 
     Draw order: per instance, the mesh kind (uniform over the kinds that still fit the remaining
     budget; the smallest kind when none fits and the scene is still empty), then for a heightfield its
     heights, then axis (2 draws), angle U[0,2pi), scale U[0.5,2], position (3 draws), material.
-    Objects spread over a square of half-size 12*sqrt(instances) at heights U[0.5,14]; heightfields
-    are terrain tiles (48 x 48 world units) laid on a grid under them.  The camera looks at the
-    centre from a distance proportional to the spread.
+    Objects spread over a square of half-size R = 3 sqrt(instances) + 6 at heights U[0.5,6];
+    heightfields are terrain tiles (48 x 48 world units) laid on a grid around the origin.  The
+    camera looks at the centre from (0, 0.5R + 6, -1.6R - 8) with a 60 degree vertical field of view.
     """
     kinds_tris = dict(zip(C2_KINDS, C2_KIND_TRIS))
     if hf_n != 256:
@@ -540,14 +541,16 @@ def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int
         chosen.append(kind)
         remaining -= kinds_tris[kind]
     # one BLAS per distinct seed-free kind, one per heightfield instance (each has its own heights)
-    parts, blas_of = [], {}
-    n = len(chosen)
-    spread = 12.0 * math.sqrt(n)
+    half = 3.0 * math.sqrt(len(chosen)) + 6.0
+    parts, blas_of = [(quad(1.6 * half + 30.0), None)], {}
+    n = len(chosen) + 1
     inst = np.zeros(n, dtype=INSTANCE)
     mats = np.zeros(n, dtype=MATERIAL)
+    inst[0] = identity_instance(0, 0)[0]
+    mats[0] = floor_material()[0]
     hf_k = 0
     grid = max(1, int(math.ceil(math.sqrt(sum(1 for k in chosen if k == "heightfield")))))
-    for i, kind in enumerate(chosen):
+    for i, kind in enumerate(chosen, start=1):
         if kind == "heightfield":
             parts.append((heightfield(rng, hf_n), None))
             b = len(parts) - 1
@@ -559,7 +562,7 @@ def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int
         axis = _random_axis(rng)
         angle = rng.uniform(1, 0, 2 * math.pi)[0]
         scale = rng.uniform(1, 0.5, 2.0)[0]
-        p = np.array([rng.uniform(1, -spread, spread)[0], rng.uniform(1, 0.5, 14)[0], rng.uniform(1, -spread, spread)[0]])
+        p = np.array([rng.uniform(1, -half, half)[0], rng.uniform(1, 0.5, 6.0)[0], rng.uniform(1, -half, half)[0]])
         mats[i] = random_materials(rng, 1)[0]
         if kind == "heightfield":
             gx, gz = hf_k % grid, hf_k // grid
@@ -574,8 +577,8 @@ def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int
         inst[i]["transform"] = t.astype(np.float32)
         inst[i]["blas"], inst[i]["mask"], inst[i]["materialBufferOffset"] = b, 0xFF, i
     parts = [(m, np.zeros(len(m.positions), np.uint32)) for m, _ in parts]
-    eye = (0.0, 0.6 * spread + 8.0, -2.2 * spread - 10.0)
-    ubo = make_ubo(eye, (0, 2, 0), 60.0, width, height, (-0.4, -1.0, 0.3), num_samples, max_recursions)
+    eye = (0.0, 0.5 * half + 6.0, -1.6 * half - 8.0)
+    ubo = make_ubo(eye, (0, 1, 0), 60.0, width, height, (-0.4, -1.0, 0.3), num_samples, max_recursions)
     return _finish(name, parts, mats, inst, ubo, width, height)
 
 

@@ -49,6 +49,41 @@ def test_batch_equals_single_renders(rg, batch):
     assert st["stack_overflows"] == 0
 
 
+def test_host_loop_equals_graph(rg, batch):
+    scenes, singles, stats = batch
+    br = rg.BatchRenderer(scenes, flags=rg.RG_FLAG_HOST_LOOP)
+    br.ctx.set_batch_slots(4096)
+    for k, (img, ref) in enumerate(zip(br.render(), singles)):
+        assert np.array_equal(img, ref), f"job {k}"
+    st = br.ctx.stats()
+    for key in RAY_KEYS:
+        assert st[key] == sum(s[key] for s in stats), key
+    assert st["iterations"] > 0
+
+
+def test_graph_replay_reads_new_cameras(rg, batch):
+    """The captured graph is replayed for a batch of the same shape: new cameras and scene contents
+    come through the job table without a new capture."""
+    scenes, singles, _ = batch
+    br = rg.BatchRenderer(scenes)
+    n0 = rg.launch_count()
+    assert all(np.array_equal(a, b) for a, b in zip(br.render(), singles))
+    n1 = rg.launch_count()
+    assert n1 - n0 > 3 * len(scenes)  # raygen, rounds, tail, per-job resolve / post / FXAA
+    jobs = br.jobs()
+    moved = []
+    for k, sc in enumerate(scenes):
+        u = S.make_ubo((3.0 + k, 9.0, -30.0), (0, 2, 0), 55.0, sc.width, sc.height, (-0.4, -1.0, 0.3),
+                       int(sc.ubo["numSamples"][0]), int(sc.ubo["maxRecursions"][0]))
+        jobs[k]["ubo"] = u[0]
+        moved.append(u)
+    br.ctx.render_batch(jobs)
+    for k, sc in enumerate(scenes):
+        rt = rg.Raytracer(sc).prepare()
+        assert np.array_equal(br.ctx.batch_download(k), rt.render(moved[k])), f"job {k}"
+        rt.ctx.close()
+
+
 def test_path_regeneration_small_pool(rg, batch):
     scenes, singles, _ = batch
     br = rg.BatchRenderer(scenes)
@@ -81,6 +116,20 @@ def test_ray_sort_keys(rg, batch, key):
         assert np.array_equal(img, ref), f"job {k} sort {key}"
     for name in RAY_KEYS:
         assert st[name] == sum(s[name] for s in stats), name
+
+
+def test_autotuner(rg, batch):
+    scenes, singles, _ = batch
+    br = rg.BatchRenderer(scenes)
+    best, table = br.ctx.autotune_batch(br.jobs(), reps=1)
+    assert len(table) == rg.AUTOTUNE_CONFIGS
+    timed = {k: v for k, v in table.items() if v is not None}
+    assert timed and all(v > 0 for v in timed.values())
+    key = (best["threads"], best["stack_depth"], {v: k for k, v in rg.SORT_KEYS.items()}[best["sort_key"]])
+    assert table[key] == min(timed.values())
+    assert br.ctx.batch_tune() == best
+    for k, (img, ref) in enumerate(zip(br.render(), singles)):
+        assert np.array_equal(img, ref), f"job {k} after autotune"
 
 
 def test_batch_vs_oracle(rg, orc):
