@@ -226,7 +226,7 @@ typedef struct rg_job {
 enum { RG_SORT_NONE = 0, RG_SORT_OCTANT = 1, RG_SORT_MORTON = 2 };
 typedef struct rg_batch_tune {
     int32_t threads;      /* block size: 64, 128 or 256 */
-    int32_t stack_depth;  /* traversal stack entries per thread: 16, 24, 32 or 48 */
+    int32_t stack_depth;  /* traversal stack entries per thread: 16, 24, 32 or 48 (48: up to 128 threads) */
     int32_t sort_key;     /* RG_SORT_*: rays sorted per round by direction octant or origin Morton code */
 } rg_batch_tune;
 
@@ -252,7 +252,8 @@ rg_status rg_set_batch_slots(rg_ctx* ctx, uint32_t slots);
  * {none, octant, morton} (36 configurations, in that nesting order), keeps the fastest one whose
  * render had no traversal-stack overflow (the results of every configuration are identical unless
  * the stack overflows) and selects it.  ms_out (nullable, 36 floats): mean milliseconds per batch
- * of each configuration, -1 where the stack overflowed.  No reference counterpart. */
+ * of each configuration, -1 where the stack overflowed or the shape is not built (256 threads with
+ * 48 entries exceeds a block's static shared memory).  No reference counterpart. */
 #define RG_AUTOTUNE_CONFIGS 36
 rg_status rg_autotune_batch(rg_ctx* ctx, const rg_job* jobs, uint32_t n, uint32_t reps, rg_batch_tune* best, float* ms_out);
 

@@ -69,7 +69,7 @@ struct SceneState {
     uint32_t nv = 0, ni = 0, nm = 0;
     std::vector<BlasRec> blas;
     DevBuf blasTable;
-    DevBuf instIn, instDev;
+    DevBuf instIn, instDev, tlasLeaves;
     BvhSet tlas;
     uint32_t nInst = 0;
     bool tlasReady = false;
@@ -291,7 +291,7 @@ DevScene scene_of(const SceneState& st) {
     s.inst = st.instDev.as<DevInstance>();
     s.tlasNodes = st.tlas.nodes.as<BvhNode>();
     s.tlasWide = st.tlas.wide.as<WideNode>();
-    s.tlasOrder = st.tlas.order.as<uint32_t>();
+    s.tlasLeaves = st.tlasLeaves.as<InstRec>();
     s.tlasN = st.nInst;
     s.pad = 0;
     s.tlasRoot = root_box(st.tlas);
@@ -305,6 +305,7 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
     c->sc->nInst = n;
     c->sc->tlasReady = false;
     TRY(ensure(c, c->sc->instDev, sizeof(DevInstance) * (size_t)(n ? n : 1)));
+    TRY(ensure(c, c->sc->tlasLeaves, sizeof(InstRec) * (size_t)(n ? n : 1)));
     TRY(ensure_bvh(c, c->sc->tlas, n));
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
@@ -313,6 +314,8 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
                        c->sc->instDev.as<DevInstance>(), c->sc->tlas.primBoxes.as<float>(), c->stream));
     CK(lbvh_build(buffers(c, c->sc->tlas), c->stream));
     CK(wide_records(buffers(c, c->sc->tlas), c->sc->tlas.wide.as<WideNode>(), c->stream));
+    CK(inst_records(c->sc->tlas.order.as<uint32_t>(), n, c->sc->instDev.as<DevInstance>(), c->sc->blasTable.as<DevBlas>(),
+                    c->sc->tlasLeaves.as<InstRec>(), c->stream));
     CK(cudaEventRecord(fe->ev[EV_AS1], c->stream));
     fe->hasAs = true;
     c->sc->tlasReady = true;
@@ -325,7 +328,7 @@ void release_bvh(rg_ctx* c, BvhSet& s) {
 }
 
 void release_scene(rg_ctx* c, SceneState& st) {
-    DevBuf* bufs[] = {&st.vertices, &st.indices, &st.materials, &st.blasTable, &st.instIn, &st.instDev};
+    DevBuf* bufs[] = {&st.vertices, &st.indices, &st.materials, &st.blasTable, &st.instIn, &st.instDev, &st.tlasLeaves};
     for (DevBuf* b : bufs) release(c, *b);
     release_bvh(c, st.tlas);
     for (auto& r : st.blas) {
@@ -340,7 +343,8 @@ uint64_t scene_bytes(const SceneState& st) {
         return s.primBoxes.cap + s.morton.cap + s.order.cap + s.left.cap + s.right.cap + s.nodeBoxes.cap + s.nodes.cap +
                s.parents.cap + s.flags.cap + s.wide.cap;
     };
-    uint64_t b = st.vertices.cap + st.indices.cap + st.materials.cap + st.blasTable.cap + st.instIn.cap + st.instDev.cap + bvh(st.tlas);
+    uint64_t b = st.vertices.cap + st.indices.cap + st.materials.cap + st.blasTable.cap + st.instIn.cap + st.instDev.cap +
+                 st.tlasLeaves.cap + bvh(st.tlas);
     for (const auto& r : st.blas) b += bvh(r.bvh) + r.tris.cap;
     return b;
 }
@@ -547,6 +551,9 @@ rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
     CK(tri_records(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), r.vOff, r.iOff, r.bvh.order.as<uint32_t>(), n,
                    r.tris.as<float4>(), c->stream));
     CK(cudaMemcpyAsync(c->sc->blasTable.as<DevBlas>()[b].root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->sc->tlasReady)  // the TLAS leaf records carry copies of the BLAS root boxes
+        CK(inst_records(c->sc->tlas.order.as<uint32_t>(), c->sc->nInst, c->sc->instDev.as<DevInstance>(),
+                        c->sc->blasTable.as<DevBlas>(), c->sc->tlasLeaves.as<InstRec>(), c->stream));
     CK(cudaEventRecord(fe->ev[EV_REFIT1], c->stream));
     fe->hasRefit = true;
     return RG_OK;
@@ -1221,6 +1228,10 @@ rg_status rg_autotune_batch(rg_ctx* c, const rg_job* jobs, uint32_t n, uint32_t 
                 c->tune.depth = depths[di];
                 c->tune.sortKey = keys[ki];
                 float ms = -1.0f;
+                if (!tune_supported(c->tune)) {
+                    if (msOut) msOut[idx] = ms;
+                    continue;
+                }
                 st = rg_render_batch(c, jobs, n);
                 rg_stats stats{};
                 if (st == RG_OK) st = read_stats(c, &stats, 0);

@@ -195,6 +195,32 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
     }
 }
 
+// TLAS leaf k: the instance at sorted position k with its inverse rows and its BLAS's root box
+// and record pointers copied in
+__global__ void k_inst_records(const uint32_t* __restrict__ order, uint32_t n, const DevInstance* __restrict__ inst,
+                               const DevBlas* __restrict__ blas, InstRec* __restrict__ out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t ii = order[k];
+    const DevInstance& d = inst[ii];
+    InstRec r;
+    r.inv[0] = d.inv[0];
+    r.inv[1] = d.inv[1];
+    r.inv[2] = d.inv[2];
+    r.lo = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0u));
+    r.hi = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(ii));
+    r.wide = nullptr;
+    r.tris = nullptr;
+    if (d.valid) {
+        const DevBlas& b = blas[d.blas];
+        r.lo = make_float4(b.root[0], b.root[1], b.root[2], __uint_as_float(b.n));
+        r.hi = make_float4(b.root[3], b.root[4], b.root[5], __uint_as_float(ii));
+        r.wide = b.wide;
+        r.tris = b.tris;
+    }
+    out[k] = r;
+}
+
 // ---- Karras 2012 hierarchy ----------------------------------------------------------------------
 __device__ inline int delta(const uint32_t* __restrict__ k, int n, int i, int j) {
     if (j < 0 || j >= n) return -1;
@@ -389,6 +415,14 @@ cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, 
                         float4* tris, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_tri_records<<<blocks(n, 256), 256, 0, s>>>(v, idx, vOff, iOff, order, n, tris);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t inst_records(const uint32_t* order, uint32_t n, const DevInstance* inst, const DevBlas* blas, InstRec* out,
+                         cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_inst_records<<<blocks(n, 128), 128, 0, s>>>(order, n, inst, blas, out);
     count_launch();
     return cudaGetLastError();
 }

@@ -67,12 +67,23 @@ struct __align__(16) DevInstance {
 };
 static_assert(sizeof(DevInstance) == 128, "instance");
 
+// TLAS leaf record, in leaf (sorted) order: what the traversal needs to enter an instance, in one
+// fetch of six independent 16-byte loads
+struct __align__(16) InstRec {
+    float4 inv[3];           // world -> object rows
+    float4 lo;               // BLAS root box lo xyz; w = BLAS triangle count bits (0: invalid or empty)
+    float4 hi;               // BLAS root box hi xyz; w = instance index bits
+    const WideNode* wide;    // the BLAS's 4-wide records
+    const float4* tris;      // its leaf-ordered triangles
+};
+static_assert(sizeof(InstRec) == 96, "instance record");
+
 struct DevScene {
     const DevBlas* blas;
     const DevInstance* inst;
     const BvhNode* tlasNodes;
     const WideNode* tlasWide;
-    const uint32_t* tlasOrder;  // sorted position -> instance
+    const InstRec* tlasLeaves;  // sorted position -> instance record
     uint32_t tlasN;
     uint32_t pad;
     const float* tlasRoot;      // root box (lo xyz, hi xyz), device memory
@@ -145,6 +156,9 @@ cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, 
                         float4* tris, cudaStream_t s);
 cudaError_t setup_instances(const rg_instance* in, uint32_t n, const DevBlas* blas, uint32_t nblas, DevInstance* out,
                             float* boxes, cudaStream_t s);
+// the TLAS leaf records (after the TLAS build; again after a BLAS refit, which moves root boxes)
+cudaError_t inst_records(const uint32_t* order, uint32_t n, const DevInstance* inst, const DevBlas* blas, InstRec* out,
+                         cudaStream_t s);
 
 // device buffers of the wavefront path (one path per pixel sample; P = paths)
 struct WavefrontBuffers {

@@ -54,6 +54,14 @@ __device__ __forceinline__ void ray_pre(Ray& r, float ox, float oy, float oz, fl
     r.Sz = 1.0f / dkz;
 }
 
+// the world-space ray at the TLAS level needs origin, direction and inverse direction only (no
+// triangle is tested there)
+__device__ __forceinline__ void ray_pre_world(Ray& r, float ox, float oy, float oz, float dx, float dy, float dz) {
+    r.ox = ox; r.oy = oy; r.oz = oz;
+    r.dx = dx; r.dy = dy; r.dz = dz;
+    r.ix = 1.0f / dx; r.iy = 1.0f / dy; r.iz = 1.0f / dz;
+}
+
 constexpr float kInflate = 1.0000004f;  // 1 + 2*gamma_3 (Ize 2013) rounded up
 
 // slab test of one box against [tmin, tbest]; returns entry distance or +inf
@@ -126,11 +134,16 @@ constexpr int kTraceThreads = 128;
 
 // per-thread traversal stack in shared memory, laid out [depth][thread] so that the 32 lanes of a
 // warp touching the same depth hit 32 different banks.  THREADS = block size, DEPTH = entries.
+// Beside it, nine floats per thread keep the world-space ray's origin, direction and inverse
+// direction while the ray is inside a BLAS, so leaving the BLAS restores them instead of
+// recomputing them.
 template <int THREADS, int DEPTH>
 struct SmemStackT {
     static constexpr int kDepth = DEPTH;
     uint32_t* base;  // &stack[0][threadIdx.x]
+    float* saved;    // &world[0][threadIdx.x]
     __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i * THREADS]; }
+    __device__ __forceinline__ float& w(int i) const { return saved[i * THREADS]; }
 };
 // the same stack in (L1-cached) local memory
 #ifndef RG_STACK_SMEM
@@ -140,18 +153,22 @@ template <int DEPTH>
 struct LocalStackT {
     static constexpr int kDepth = DEPTH;
     uint32_t* base;
+    float* saved;
     __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i]; }
+    __device__ __forceinline__ float& w(int i) const { return saved[i]; }
 };
 #define RG_DECLARE_SMEM_STACK(name, THREADS, DEPTH)      \
     __shared__ uint32_t name##_mem[DEPTH][THREADS];      \
-    const SmemStackT<THREADS, DEPTH> name{&name##_mem[0][threadIdx.x]}
+    __shared__ float name##_world[9][THREADS];           \
+    const SmemStackT<THREADS, DEPTH> name{&name##_mem[0][threadIdx.x], &name##_world[0][threadIdx.x]}
 #if RG_STACK_SMEM
 #define RG_DECLARE_STACK(name) RG_DECLARE_SMEM_STACK(name, kTraceThreads, kTraversalStack)
 using TravStack = SmemStackT<kTraceThreads, kTraversalStack>;
 #else
 #define RG_DECLARE_STACK(name)                 \
     uint32_t name##_mem[kTraversalStack];      \
-    const LocalStackT<kTraversalStack> name{name##_mem}
+    float name##_world[9];                     \
+    const LocalStackT<kTraversalStack> name{name##_mem, name##_world}
 using TravStack = LocalStackT<kTraversalStack>;
 #endif
 #ifndef RG_WF_MIN_BLOCKS
@@ -170,8 +187,8 @@ using TravStack = LocalStackT<kTraversalStack>;
 // behind a marker entry; a BLAS leaf runs the triangle test).  The
 // kernel interleaves trav_step with shading so that a lane whose ray finished does not idle.
 struct Trav {
-    float ox, oy, oz, dx, dy, dz, tmin;  // world-space ray
-    Ray r;                               // the ray of the current level (world or object space)
+    float tmin;
+    Ray r;  // the ray of the current level (world or object space); its shear terms are used in BLASes only
     Hit h;
     const WideNode* nodes;
     const float4* tris;
@@ -188,10 +205,8 @@ __device__ __forceinline__ void trav_begin(Trav& T, const DevScene& sc, float ox
     T.h.inst = T.h.prim = 0xFFFFFFFFu;
     T.active = false;
     if ((dx == 0.0f && dy == 0.0f && dz == 0.0f) || sc.tlasN == 0) return;
-    T.ox = ox; T.oy = oy; T.oz = oz;
-    T.dx = dx; T.dy = dy; T.dz = dz;
     T.tmin = tmin;
-    ray_pre(T.r, ox, oy, oz, dx, dy, dz);
+    ray_pre_world(T.r, ox, oy, oz, dx, dy, dz);
     if (sc.tlasN > 1 && slab(T.r, sc.tlasRoot[0], sc.tlasRoot[3], sc.tlasRoot[1], sc.tlasRoot[4], sc.tlasRoot[2], sc.tlasRoot[5], tmin, T.h.t) == INFINITY)
         return;
     T.sp = 0;
@@ -242,11 +257,12 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
         const float4* tp = T.tris + 3 * (size_t)(ref & ~kLeaf);
         tri_test(T.r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), tmin, T.inst, T.h);
     } else {
-        uint32_t ii = __ldg(sc.tlasOrder + (ref & ~kLeaf));
-        const DevInstance* in = sc.inst + ii;
-        if (__ldg(&in->valid)) {
-            const float ox = T.ox, oy = T.oy, oz = T.oz, dx = T.dx, dy = T.dy, dz = T.dz;
-            float4 i0 = __ldg(&in->inv[0]), i1 = __ldg(&in->inv[1]), i2 = __ldg(&in->inv[2]);
+        const InstRec* ir = sc.tlasLeaves + (ref & ~kLeaf);
+        const float4 i0 = __ldg(&ir->inv[0]), i1 = __ldg(&ir->inv[1]), i2 = __ldg(&ir->inv[2]);
+        const float4 lo = __ldg(&ir->lo), hi = __ldg(&ir->hi);
+        const uint32_t bn = __float_as_uint(lo.w);
+        if (bn > 0) {
+            const float ox = T.r.ox, oy = T.r.oy, oz = T.r.oz, dx = T.r.dx, dy = T.r.dy, dz = T.r.dz;  // world ray (TLAS level)
             float qx = ((i0.x * ox + i0.y * oy) + i0.z * oz) + i0.w;
             float qy = ((i1.x * ox + i1.y * oy) + i1.z * oz) + i1.w;
             float qz = ((i2.x * ox + i2.y * oy) + i2.z * oz) + i2.w;
@@ -254,18 +270,19 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
             float ey = (i1.x * dx + i1.y * dy) + i1.z * dz;
             float ez = (i2.x * dx + i2.y * dy) + i2.z * dz;
             if (!(ex == 0.0f && ey == 0.0f && ez == 0.0f)) {
-                const DevBlas* bl = sc.blas + __ldg(&in->blas);
-                uint32_t bn = __ldg(&bl->n);
                 Ray orr;
                 ray_pre(orr, qx, qy, qz, ex, ey, ez);
-                const float* rb = bl->root;
-                if (bn > 0 && slab(orr, __ldg(rb + 0), __ldg(rb + 3), __ldg(rb + 1), __ldg(rb + 4), __ldg(rb + 2), __ldg(rb + 5), tmin, T.h.t) != INFINITY) {
+                if (slab(orr, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, tmin, T.h.t) != INFINITY) {
                     if (T.sp < STACK::kDepth) {
+                        const ulonglong2 pp = __ldg(reinterpret_cast<const ulonglong2*>(&ir->wide));
+                        stack.w(0) = ox; stack.w(1) = oy; stack.w(2) = oz;
+                        stack.w(3) = dx; stack.w(4) = dy; stack.w(5) = dz;
+                        stack.w(6) = T.r.ix; stack.w(7) = T.r.iy; stack.w(8) = T.r.iz;
                         stack[T.sp++] = kMarker;
                         T.r = orr;
-                        T.nodes = bl->wide;
-                        T.tris = bl->tris;
-                        T.inst = ii;
+                        T.nodes = reinterpret_cast<const WideNode*>(pp.x);
+                        T.tris = reinterpret_cast<const float4*>(pp.y);
+                        T.inst = __float_as_uint(hi.w);
                         T.inBlas = true;
                         T.ref = bn == 1 ? kLeaf : 0u;
                         return;
@@ -288,7 +305,9 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
         }
         T.inBlas = false;
         T.nodes = sc.tlasWide;
-        ray_pre(T.r, T.ox, T.oy, T.oz, T.dx, T.dy, T.dz);
+        T.r.ox = stack.w(0); T.r.oy = stack.w(1); T.r.oz = stack.w(2);
+        T.r.dx = stack.w(3); T.r.dy = stack.w(4); T.r.dz = stack.w(5);
+        T.r.ix = stack.w(6); T.r.iy = stack.w(7); T.r.iz = stack.w(8);
     }
 }
 
@@ -1461,7 +1480,7 @@ static TraceKernel trace_kernel(bool batch, bool count, int threads, int depth) 
     if (threads == T && depth == D) return k_wf_trace<false, true, T, D>;
     RG_TK(64, 16) RG_TK(64, 24) RG_TK(64, 32) RG_TK(64, 48)
     RG_TK(128, 16) RG_TK(128, 24) RG_TK(128, 32) RG_TK(128, 48)
-    RG_TK(256, 16) RG_TK(256, 24) RG_TK(256, 32) RG_TK(256, 48)
+    RG_TK(256, 16) RG_TK(256, 24) RG_TK(256, 32)  // 256 x 48 exceeds the 48 KB of static shared memory
 #undef RG_TK
     return nullptr;
 }
