@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-rows", type=int, default=54, help="rows of the CPU-baseline sample")
+    ap.add_argument("--cpu-rows", type=int, default=0, help="rows per render of the CPU-baseline sample (0: full frames)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", default="1920x1080", help="WxH; smaller sizes are for profiling captures only")
     ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch"],
@@ -474,35 +474,41 @@ def run_batch(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline_batch(scenes, every=1, row_step=1):
-    """The oracle on all host cores over a sample of the batch: every `every`-th scene, every
-    `row_step`-th row of each (default: the whole batch, a few seconds on 16 cores)."""
+def cpu_baseline_batch(scenes, min_seconds=10.0, max_passes=10):
+    """The oracle on all host cores over the whole batch (every scene, every row), repeated until at
+    least `min_seconds` of CPU work."""
     import oracle
     nthreads = os.cpu_count() or 1
+    orcs = [oracle.OracleScene(sc) for sc in scenes]
     rays, dt, n = 0, 0.0, 0
-    for sc in scenes[::every]:
-        o = oracle.OracleScene(sc)
-        step = row_step
+    while n < max_passes and (n == 0 or dt < min_seconds):
+        for o, sc in zip(orcs, scenes):
+            t = time.perf_counter()
+            _, _, _, st = o.render(rows=(0, sc.height), row_step=1, nthreads=nthreads)
+            dt += time.perf_counter() - t
+            rays += st["primary"] + st["shadow"] + st["secondary"]
+        n += 1
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "sample": f"{n} passes over all {len(scenes)} scenes (every row): {rays} rays in {dt:.2f} s (trace + shade)"}
+
+
+def cpu_baseline(orc_scene, sc, rows, min_seconds=10.0, max_renders=20):
+    """The oracle on all host cores: full renders of frame 0 repeated until at least `min_seconds`
+    of CPU work (the frame takes ~2 s on 16 cores).  `rows` > 0 renders only that many rows spread
+    over the frame per render (a shorter sample, for quick runs)."""
+    nthreads = os.cpu_count() or 1
+    step = max(1, sc.height // rows) if rows > 0 else 1
+    rays, dt, n = 0, 0.0, 0
+    while n < max_renders and (n == 0 or dt < min_seconds):
         t = time.perf_counter()
-        _, _, _, st = o.render(rows=(0, sc.height), row_step=step, nthreads=nthreads)
+        _, _, _, st = orc_scene.render(rows=(0, sc.height), row_step=step, nthreads=nthreads)
         dt += time.perf_counter() - t
         rays += st["primary"] + st["shadow"] + st["secondary"]
         n += 1
+    nrows = (sc.height + step - 1) // step
+    what = "full frame 0" if step == 1 else f"every {step}th row of frame 0 ({nrows} rows)"
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
-            "sample": f"{n} scenes (every {every}th), every {row_step}th row of each: {rays} rays in {dt:.2f} s (trace + shade)"}
-
-
-def cpu_baseline(orc_scene, sc, rows):
-    """The oracle on all host cores over `rows` rows spread evenly over frame 0."""
-    nthreads = os.cpu_count() or 1
-    step = max(1, sc.height // rows)
-    t = time.perf_counter()
-    _, _, _, st = orc_scene.render(rows=(0, sc.height), row_step=step, nthreads=nthreads)
-    dt = time.perf_counter() - t
-    rays = st["primary"] + st["shadow"] + st["secondary"]
-    n = (sc.height + step - 1) // step
-    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
-            "sample": f"every {step}th row of frame 0 ({n} rows x {sc.width} px, {int(sc.ubo['numSamples'][0])} spp): "
+            "sample": f"{n} renders of the {what} ({sc.width} px wide, {int(sc.ubo['numSamples'][0])} spp): "
                       f"{rays} rays in {dt:.2f} s (trace + shade)"}
 
 

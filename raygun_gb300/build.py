@@ -44,17 +44,17 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= t for f in _inputs())
 
 
-FACADE_SRC = os.path.join(HERE, "host", "raygun.cpp")
+FACADE_SRCS = [os.path.join(HERE, "host", "raygun.cpp"), os.path.join(HERE, "host", "collada.cpp")]
 FACADE_LIB = os.path.join(HERE, "librgfacade.so")
-FACADE_HDR = os.path.join(INCLUDE, "rg", "raygun.hpp")
+FACADE_HDRS = [os.path.join(INCLUDE, "rg", "raygun.hpp"), os.path.join(INCLUDE, "rg", "collada.hpp")]
 
 
 def build_facade(force: bool = False) -> str:
     """The C++ facade (include/rg/raygun.hpp) as librgfacade.so, linked to librgcuda.so."""
-    deps = [FACADE_SRC, FACADE_HDR, os.path.join(INCLUDE, "rgcuda.h"), LIB]
+    deps = [*FACADE_SRCS, *FACADE_HDRS, os.path.join(INCLUDE, "rgcuda.h"), LIB]
     if not force and os.path.exists(FACADE_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(FACADE_LIB) for d in deps):
         return FACADE_LIB
-    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", INCLUDE, "-o", FACADE_LIB + ".tmp", FACADE_SRC,
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", INCLUDE, "-o", FACADE_LIB + ".tmp", *FACADE_SRCS,
            "-L", HERE, "-lrgcuda", "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
