@@ -56,8 +56,14 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="rows per render of the CPU-baseline sample (0: full frames)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", default="1920x1080", help="WxH; smaller sizes are for profiling captures only")
-    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch"],
-                    help="game-frame: the 1080p 4x SSAA frame loop; batch: 64 independent scenes per step")
+    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch", "serve"],
+                    help="game-frame: the 1080p 4x SSAA frame loop; batch: 64 independent scenes per step; "
+                         "serve: Poisson render requests through the render server")
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-rate", type=float, default=400.0, help="mean arrivals per second")
+    ap.add_argument("--serve-large", type=int, default=12, help="large terrain scenes in the catalog")
+    ap.add_argument("--serve-budget-gb", type=float, default=160.0)
+    ap.add_argument("--serve-graph", action="store_true", help="serve: CUDA-graph batches instead of the host loop")
     ap.add_argument("--no-tune", action="store_true", help="batch: skip the autotuner (default launch shape)")
     ap.add_argument("--batch-scenes", type=int, default=64, help="batch: scenes per batch (profiling captures only)")
     return ap.parse_args()
@@ -474,6 +480,84 @@ def run_batch(args):
         dist.destroy_process_group()
 
 
+SERVE_WORKLOAD = "serving loop: Poisson arrivals at {rate:g} req/s, {n} requests; scenes of the batched-rendering " \
+                 "distribution ({small} scenes) or, with probability 0.05, large terrain scenes ({large} scenes of " \
+                 "10-60 tessellated 1M-triangle heightfields) at 320x180..3840x2160 and 1-8 spp; LRU scene residency " \
+                 "under a {budget:g} GB HBM budget; waiting requests batched per step; every image read back"
+
+
+def run_serve(args):
+    import torch
+    from raygun_gb300 import build as rgbuild, rgcuda, serving as V
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    rgbuild.build()
+    small = S.batch_scenes(n=64, seed=4)
+    catalog = {f"b{k:02d}": sc for k, sc in enumerate(small)}
+    rng = S.Rng(44)
+    large_keys = []
+    for k in range(args.serve_large):
+        fields = 10 + min(int(rng.uniform(1, 0, 51)[0]), 50)
+        key = f"t{k:02d}"
+        catalog[key] = S.terrain_scene(rng, key, fields, 1920, 1080, 1, 3)
+        large_keys.append(key)
+    budget = int(args.serve_budget_gb * 1e9)
+    ctx = rgcuda.Context(device=local, hbm_budget_bytes=budget,
+                         flags=0 if args.serve_graph else rgcuda.RG_FLAG_HOST_LOOP)
+    srv = V.RenderServer(ctx, catalog, budget)
+    reqs = V.poisson_requests(args.serve_requests, args.serve_rate, 4, [(k, catalog[k]) for k in catalog if k[0] == "b"],
+                              [(k, catalog[k]) for k in large_keys])
+    # a server that has been running: the working buffers of a large batch exist and the catalog is
+    # resident as far as the budget allows (catalog order)
+    warm = V.poisson_requests(96, args.serve_rate, 40, [(k, catalog[k]) for k in catalog if k[0] == "b"],
+                              [(k, catalog[k]) for k in large_keys], large_fraction=0.2)
+    for r in warm:
+        r.arrival = 0.0
+    t0 = time.perf_counter()
+    V.run_open_loop(srv, warm)
+    reserve = max(srv._working_held(), 24 << 30)
+    for key in catalog:
+        if srv.res.resident_bytes() + srv.res.footprint(key) + reserve > budget:
+            break
+        srv.res.ensure(key)
+    t_warm = time.perf_counter() - t0
+    srv.rays, srv.batches, srv.batch_sizes = 0, 0, []
+    ev0, up0 = srv.res.evictions, srv.res.uploads
+    launches0 = rgcuda.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    results, wall = V.run_open_loop(srv, reqs)
+    clk = clocks.stop()
+    summary = V.summarize(results, wall, srv.rays)
+    ok = [r for r in results if r.ok]
+    byid = {r.id: r for r in reqs}
+    d2h = sum(byid[r.id].width * byid[r.id].height * 16 for r in ok)
+    out = {
+        "metric": "Mrays/s", "value": summary["mrays_per_s"], "unit": "Mrays/s", "n_gpus": world,
+        "steps": srv.batches, "warmup": 1, "ms_per_step": summary["seconds"] * 1e3 / max(srv.batches, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded procedural scenes and arrivals (no dataset)",
+        "config": {"workload": SERVE_WORKLOAD.format(rate=args.serve_rate, n=args.serve_requests, small=len(small),
+                                                     large=len(large_keys), budget=args.serve_budget_gb),
+                   "catalog_scenes": len(catalog),
+                   "catalog_instanced_tris": int(sum(sc.instanced_tri_count for sc in catalog.values())),
+                   "catalog_unique_tris": int(sum(int(sc.meshes["triCount"].astype(np.int64).sum()) for sc in catalog.values())),
+                   "batch_mode": "graph" if args.serve_graph else "host loop",
+                   "l2": "inputs larger than L2", "parallelism": "single GPU"},
+        "serving": {**summary, "batches": srv.batches, "mean_batch": float(np.mean(srv.batch_sizes)) if srv.batch_sizes else 0.0,
+                    "evictions": srv.res.evictions - ev0, "uploads": srv.res.uploads - up0,
+                    "resident_scenes_at_start": len(srv.res.slots), "warmup_seconds": t_warm},
+        "e2e": {"value": summary["mrays_per_s"], "unit": "Mrays/s",
+                "h2d_bytes_per_step": int(rgcuda.JOB.itemsize * len(ok) / max(srv.batches, 1)),
+                "d2h_bytes_per_step": int(d2h / max(srv.batches, 1)),
+                "timing": "wall clock from the first arrival to the last completion; requests arrive in real time"},
+        "roofline": None, "clocks": clk, "gpu_launches": int(rgcuda.launch_count() - launches0),
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def cpu_baseline_batch(scenes, min_seconds=10.0, max_passes=10):
     """The oracle on all host cores over the whole batch (every scene, every row), repeated until at
     least `min_seconds` of CPU work."""
@@ -559,6 +643,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

@@ -245,6 +245,9 @@ rg_status rg_batch_framebuffer(rg_ctx* ctx, uint32_t job, float** d_rgba);
 rg_status rg_batch_download(rg_ctx* ctx, uint32_t job, float* host_rgba);
 rg_status rg_set_batch_tune(rg_ctx* ctx, const rg_batch_tune* tune);
 rg_status rg_get_batch_tune(rg_ctx* ctx, rg_batch_tune* out);
+/* Device memory the context holds (all scene slots, images, path state, scratch) and its budget
+ * (rg_device_opts.hbm_budget_bytes, 0 = none), in bytes. */
+rg_status rg_get_memory(rg_ctx* ctx, uint64_t* allocated_bytes, uint64_t* budget_bytes);
 /* Path slots of the batch loop (default 2^23; about 1.6 KB of device memory each). */
 rg_status rg_set_batch_slots(rg_ctx* ctx, uint32_t slots);
 /* Autotuner of the batch loop: renders the batch once (warm-up, capture) and then `reps` times

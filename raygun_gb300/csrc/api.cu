@@ -1094,6 +1094,13 @@ rg_status rg_get_batch_tune(rg_ctx* c, rg_batch_tune* t) {
     return RG_OK;
 }
 
+rg_status rg_get_memory(rg_ctx* c, uint64_t* allocated, uint64_t* budget) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    if (allocated) *allocated = c->allocated;
+    if (budget) *budget = c->budget;
+    return RG_OK;
+}
+
 rg_status rg_set_batch_slots(rg_ctx* c, uint32_t slots) {
     if (!c || slots < 1024) return fail(c, RG_ERR_INVALID_ARG, "batch path slots must be >= 1024");
     c->batchSlots = slots;

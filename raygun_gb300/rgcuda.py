@@ -35,7 +35,7 @@ EXPORTS = [
     "rg_update_vertices_device", "rg_get_total_stats", "rg_reset_total_stats", "rg_set_flags", "rg_launch_count",
     "rg_lbvh_build_device_noalloc", "rg_scene_create", "rg_scene_select", "rg_scene_destroy", "rg_scene_bytes",
     "rg_render_batch", "rg_batch_framebuffer", "rg_batch_download", "rg_set_batch_tune", "rg_get_batch_tune",
-    "rg_set_batch_slots", "rg_autotune_batch",
+    "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory",
 ]
 
 # rg_job (include/rgcuda.h): one render of a batch
@@ -130,6 +130,7 @@ def load(path: str = LIB_PATH):
         "rg_get_batch_tune": ([P, ctypes.POINTER(BatchTune)], I32),
         "rg_set_batch_slots": ([P, U32], I32),
         "rg_autotune_batch": ([P, P, U32, U32, ctypes.POINTER(BatchTune), P], I32),
+        "rg_get_memory": ([P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -327,6 +328,12 @@ class Context:
         for i, (t, d, k) in enumerate(autotune_grid()):
             table[(t, d, k)] = None if ms[i] < 0 else float(ms[i])
         return {k: getattr(best, k) for k, _ in BatchTune._fields_}, table
+
+    def memory(self):
+        """(allocated bytes, budget bytes) of this context."""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._ck(self.L.rg_get_memory(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def set_batch_slots(self, slots: int):
         self._ck(self.L.rg_set_batch_slots(self.h, slots))

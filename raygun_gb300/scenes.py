@@ -604,3 +604,86 @@ def batch_scenes(n=64, seed=2, tri_range=(1e3, 4e6), resolutions=C2_RESOLUTIONS,
 
 def c2_scenes() -> list:
     return batch_scenes()
+
+
+# ----------------------------------------------------------------------------- large terrain scenes
+
+SERVE_RESOLUTIONS = C2_RESOLUTIONS + ((3840, 2160),)
+_FIELD_CACHE: dict = {}
+
+
+def _terrain_field(k: int, hf_n: int) -> Mesh:
+    """Distinct base heightfield k (seed 4000 + k), built once per process."""
+    key = (k, hf_n)
+    if key not in _FIELD_CACHE:
+        _FIELD_CACHE[key] = heightfield(Rng(4000 + k), hf_n)
+    return _FIELD_CACHE[key]
+
+
+def terrain_scene(rng: Rng, name: str, fields: int, width: int, height: int, num_samples: int, max_recursions: int,
+                  hf_n: int = 708, distinct: int = 4, objects: int = 256) -> Scene:
+    """A large scene: ``fields`` tessellated heightfield tiles of 2(hf_n-1)^2 triangles each (~1M at
+    hf_n = 708), each its own BLAS, laid on a square grid of 48 x 48 world-unit tiles, plus
+    ``objects`` instances of the game-frame meshes above them.  The tiles' vertex data comes from
+    ``distinct`` base heightfields (tile k uses base k mod distinct): BLASes are built per tile, so
+    device memory grows with ``fields`` while host memory does not.
+
+    Draw order: per tile, diffuse (3 draws) and roughness; then per object the kind index, axis
+    (2 draws), angle, scale U[0.5,2], position (3 draws), material (random_materials)."""
+    base = [_terrain_field(k, hf_n) for k in range(min(distinct, fields))]
+    kinds = [_catalog_mesh(k) for k in ("ico3", "ico4", "ico5", "ico6", "torus_a", "torus_b")]
+    parts = [(m, np.zeros(len(m.positions), np.uint32)) for m in base + kinds]
+    proto = _finish(name, parts, np.zeros(1, dtype=MATERIAL), np.zeros(0, dtype=INSTANCE), None, width, height)
+    meshes = list(proto.meshes)
+    tile_mesh = []
+    for f in range(fields):
+        if f < len(base):
+            tile_mesh.append(f)
+        else:
+            meshes.append(proto.meshes[f % len(base)])
+            tile_mesh.append(len(meshes) - 1)
+    meshes = np.array(meshes, dtype=MESH)
+    grid = max(1, int(math.ceil(math.sqrt(fields))))
+    half = 24.0 * grid
+    n = fields + objects
+    inst = np.zeros(n, dtype=INSTANCE)
+    mats = np.zeros(n, dtype=MATERIAL)
+    scale = 48.0 / (hf_n - 1)
+    for f in range(fields):
+        diffuse = rng.uniform(3, 0.4, 1.0)
+        rough = rng.uniform(1, 0.0, 0.5)[0]
+        t = np.zeros((3, 4))
+        t[:, :3] = np.eye(3) * scale
+        t[:, 3] = (-half + 24.0 + 48.0 * (f % grid), -0.5, -half + 24.0 + 48.0 * (f // grid))
+        inst[f]["transform"] = t.astype(np.float32)
+        inst[f]["blas"], inst[f]["mask"], inst[f]["materialBufferOffset"] = tile_mesh[f], 0xFF, f
+        mats[f] = _material(diffuse, roughness=float(rough), reflectivity=0.3, effect_id=1)[0]
+    for i in range(fields, n):
+        kind = min(int(rng.uniform(1, 0, len(kinds))[0]), len(kinds) - 1)
+        axis = _random_axis(rng)
+        angle = rng.uniform(1, 0, 2 * math.pi)[0]
+        sc_ = rng.uniform(1, 0.5, 2.0)[0]
+        p = np.array([rng.uniform(1, -half, half)[0], rng.uniform(1, 0.5, 6.0)[0], rng.uniform(1, -half, half)[0]])
+        mats[i] = random_materials(rng, 1)[0]
+        t = np.zeros((3, 4))
+        t[:, :3], t[:, 3] = _rot_axis_angle(axis, angle) * sc_, p
+        inst[i]["transform"] = t.astype(np.float32)
+        inst[i]["blas"], inst[i]["mask"], inst[i]["materialBufferOffset"] = len(base) + kind, 0xFF, i
+    inst["vertexBufferOffset"] = meshes["vertexOffset"][inst["blas"]]
+    inst["indexBufferOffset"] = meshes["indexOffset"][inst["blas"]]
+    eye = (0.0, 0.35 * half + 10.0, -0.9 * half - 10.0)
+    ubo = make_ubo(eye, (0, 0, 0), 60.0, width, height, (-0.4, -1.0, 0.3), num_samples, max_recursions)
+    return Scene(name, proto.vertices, proto.indices, mats, meshes, inst, ubo, width, height)
+
+
+def reframe(scene: Scene, width: int, height: int, num_samples: int, max_recursions: int) -> np.ndarray:
+    """The scene's camera at another image size / sample count / depth: same view, projection of the
+    new aspect ratio."""
+    u = scene.ubo.copy()
+    vi = u["viewInverse"][0]
+    fov = 60.0
+    ubo = make_ubo((0, 0, 0), (0, 0, 1), fov, width, height, tuple(u["lightDir"][0]), num_samples, max_recursions)
+    ubo["viewInverse"] = vi
+    for k in ("clearColor", "time", "showAlpha", "fadeColor"):
+        ubo[k] = u[k]
+    return ubo
