@@ -133,7 +133,8 @@ enum {
     RG_IMAGE_ROUGH_TRANSITION = 4,
     RG_IMAGE_ROUGH_COLORS_A = 5,
     RG_IMAGE_ROUGH_COLORS_B = 6,
-    RG_IMAGE_PRE_FXAA = 7
+    RG_IMAGE_PRE_FXAA = 7,
+    RG_IMAGE_FILTER_OUT = 8  /* the learned filter's prediction of the last frame (RGB; rg_set_filter) */
 };
 
 /* Replaces Raytracer::Raytracer (render/raytracer.cpp:38-52) and the device parts of
@@ -245,6 +246,42 @@ rg_status rg_batch_framebuffer(rg_ctx* ctx, uint32_t job, float** d_rgba);
 rg_status rg_batch_download(rg_ctx* ctx, uint32_t job, float* host_rgba);
 rg_status rg_set_batch_tune(rg_ctx* ctx, const rg_batch_tune* tune);
 rg_status rg_get_batch_tune(rg_ctx* ctx, rg_batch_tune* out);
+/* ---- learned roughness filter -------------------------------------------------------------------
+ * A 5-layer 3x3 convolutional network (12-32-64-64-32-3 channels, ReLU, layer-1 output added to the
+ * input of layer 5, BF16 weights and activations, FP32 accumulation on the tensor cores) that
+ * predicts the rough-reflection radiance the composite mixes in (postprocess.comp:28-50), in place of
+ * the screen-space roughness approximation (rough_prepare.comp + rough_blur_h/v,
+ * raytracer.cpp:112-122).  No reference counterpart beyond the passes it replaces.
+ * Parameters: per layer W[out][in][3][3] then b[out], FP32, real channel counts. */
+typedef struct rg_filter rg_filter;
+#define RG_FILTER_PARAMS 78243u
+rg_status rg_filter_create(rg_ctx* ctx, uint64_t seed, rg_filter** out);  /* He-normal weights; ctx's device and stream */
+rg_status rg_filter_destroy(rg_filter* f);
+const char* rg_filter_last_error(const rg_filter* f);
+rg_status rg_filter_get_params(rg_filter* f, float* host, uint32_t n);
+rg_status rg_filter_set_params(rg_filter* f, const float* host, uint32_t n);  /* also resets the Adam state */
+/* gradients of the last rg_filter_train_step, in the parameter layout */
+rg_status rg_filter_get_grads(rg_filter* f, float* host, uint32_t n);
+/* the network on `batch` images of height x width (device memory): d_input [batch][height][width][16]
+ * BF16 (channels 12..15 zero), d_out [batch][height][width][4] FP32 (RGB used) */
+rg_status rg_filter_forward(rg_filter* f, const void* d_input, uint32_t batch, uint32_t height, uint32_t width, float* d_out);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) on the mean squared error against d_target
+ * [batch][height][width][4] FP32 (RGB used); lr 0 computes the gradients only.  *loss_out: the loss
+ * before the step */
+rg_status rg_filter_train_step(rg_filter* f, const void* d_input, const float* d_target, uint32_t batch, uint32_t height, uint32_t width,
+                               float lr, float* loss_out);
+/* the filter input of the context's last frame, d_out [H][W][16] BF16: rough RGB, normal, log-scaled
+ * linear depth, roughness term (rough.a), base colour, reflect contribution */
+rg_status rg_filter_input(rg_ctx* ctx, void* d_out);
+/* the rough RGB of the context's last frame, d_out [H][W][4] FP32 (training target of a glossy frame) */
+rg_status rg_filter_target(rg_ctx* ctx, float* d_out);
+/* frames of this context use the filter in place of the roughness passes (NULL: the plain passes) */
+rg_status rg_set_filter(rg_ctx* ctx, rg_filter* f);
+/* glossy reference shading (training targets; 0 = off, the default): at each sample's primary hit
+ * the reflection and refraction directions are drawn around their mirror directions from a GGX lobe
+ * of the material roughness (alpha = roughness^2), seeded per pixel sample from `seed` */
+rg_status rg_set_glossy(rg_ctx* ctx, uint32_t seed);
+
 /* Device memory the context holds (all scene slots, images, path state, scratch) and its budget
  * (rg_device_opts.hbm_budget_bytes, 0 = none), in bytes. */
 rg_status rg_get_memory(rg_ctx* ctx, uint64_t* allocated_bytes, uint64_t* budget_bytes);

@@ -116,6 +116,11 @@ struct rg_ctx {
     int graphBodyKernels = 0;
     uint32_t bodyRunsSeen = 0;
     bool graphPending = false;
+    // learned roughness filter used by the frames (nullable), glossy reference shading seed (0 = off),
+    // samples of the last frame
+    rg_filter* filter = nullptr;
+    uint32_t glossySeed = 0;
+    uint32_t lastSamples = 1;
     std::vector<FrameEvents*> evPool, evPending;
     FrameEvents* evCur = nullptr;  // ranges recorded since the last frame
     rg_timings lastTimings{};
@@ -618,7 +623,11 @@ static rg_status run_post(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
     CK(cudaEventRecord(fe->ev[EV_POST0], c->stream));
-    CK(launch_rough_post(pp, c->stream));
+    if (c->filter)  // the learned filter in place of the roughness passes, then the same FXAA
+        CK(filter_frame(c->filter, pp.base, pp.normal, pp.rough, c->W, c->H, (float)c->lastSamples, pp.fade, pp.showAlpha, pp.finalImg,
+                        c->stream));
+    else
+        CK(launch_rough_post(pp, c->stream));
     CK(cudaEventRecord(fe->ev[EV_ROUGH1], c->stream));
     CK(launch_fxaa(pp, c->stream));
     CK(cudaEventRecord(fe->ev[EV_POST1], c->stream));
@@ -658,6 +667,8 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     tp.countVisits = (c->flags & RG_FLAG_COUNT_VISITS) ? 1 : 0;
     tp.samples = c->samples.as<float4>();
     tp.workCounter = c->workCounter.as<uint32_t>();
+    tp.glossySeed = c->glossySeed;
+    c->lastSamples = (uint32_t)ubo->numSamples;
     const bool mega = (c->flags & RG_FLAG_MEGAKERNEL) != 0;
     if (!mega) TRY(ensure_wavefront(c, (size_t)c->W * c->H * (uint32_t)ubo->numSamples, tp.wf));
     CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
@@ -724,6 +735,10 @@ rg_status rg_download_image(rg_ctx* c, int32_t which, float* host) {
         case RG_IMAGE_NORMAL: h16 = c->normal.as<uint2>(); break;
         case RG_IMAGE_ROUGH: h16 = c->rough.as<uint2>(); break;
         case RG_IMAGE_PRE_FXAA: h16 = c->finalImg.as<uint2>(); break;
+        case RG_IMAGE_FILTER_OUT:
+            if (!c->filter) return fail(c, RG_ERR_NOT_READY, "no learned filter set (rg_set_filter)");
+            CK(cudaMemcpyAsync(c->tmpB.p, filter_prediction(c->filter), 16 * px, cudaMemcpyDeviceToDevice, c->stream));
+            break;
         case RG_IMAGE_ROUGH_COLORS_A:
         case RG_IMAGE_ROUGH_COLORS_B:
         case RG_IMAGE_ROUGH_TRANSITION:
@@ -1291,6 +1306,40 @@ rg_status rg_batch_download(rg_ctx* c, uint32_t job, float* host) {
                        cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     TRY(settle_graph(c));
+    return RG_OK;
+}
+
+}  // extern "C"
+
+// ---- learned roughness filter: frame inputs / targets, selection, glossy reference shading ---------
+extern "C" {
+
+rg_status rg_filter_input(rg_ctx* c, void* d_out) {
+    if (!c || !d_out) return RG_ERR_INVALID_ARG;
+    if (!c->haveFrame) return fail(c, RG_ERR_NOT_READY, "no frame rendered");
+    TRY(set_device(c));
+    CK(filter_gbuffer(c->base.as<uint2>(), c->normal.as<uint2>(), c->rough.as<uint2>(), (size_t)c->W * c->H, (float)c->lastSamples, d_out,
+                      c->stream));
+    return RG_OK;
+}
+
+rg_status rg_filter_target(rg_ctx* c, float* d_out) {
+    if (!c || !d_out) return RG_ERR_INVALID_ARG;
+    if (!c->haveFrame) return fail(c, RG_ERR_NOT_READY, "no frame rendered");
+    TRY(set_device(c));
+    CK(filter_target(c->rough.as<uint2>(), (size_t)c->W * c->H, reinterpret_cast<float4*>(d_out), c->stream));
+    return RG_OK;
+}
+
+rg_status rg_set_filter(rg_ctx* c, rg_filter* f) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    c->filter = f;
+    return RG_OK;
+}
+
+rg_status rg_set_glossy(rg_ctx* c, uint32_t seed) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    c->glossySeed = seed;
     return RG_OK;
 }
 

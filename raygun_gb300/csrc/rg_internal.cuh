@@ -6,6 +6,7 @@
 // out as fmaf() where they are wanted.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -209,6 +210,7 @@ struct TraceParams {
     uint32_t* slotJob;
     uint32_t* slotSample;
     const uint32_t* perm;  // nullable: order in which the trace kernel takes the queue's rays
+    uint32_t glossySeed;   // 0: the reference's mirror shading; else glossy reference shading (seed)
 };
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
 // hostCount: pinned host word used to poll the queue length; iterations: trace/shade rounds run
@@ -243,6 +245,41 @@ int batch_graph_kernels(const TraceTune& tune, int* perBody);
 cudaError_t launch_resolve_job(const float4* samples, const JobDesc& hostJob, uint2* base, uint2* normal, uint2* rough,
                                cudaStream_t s);
 cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
+
+// ---- learned roughness filter (filter.cu) ----
+// one 3x3 convolution: y = epilogue(conv(x [+ x2], w) + bias); NHWC BF16 activations
+struct FilterConvArgs {
+    const __nv_bfloat16* x;     // [B][H][W][CIN]
+    const __nv_bfloat16* x2;    // nullable, added to x
+    const __nv_bfloat16* w;     // packed [9][CIN/8][COUT][8] (K = tap * CIN + ci, rows = output channels)
+    const float* bias;          // nullable [COUT]
+    const __nv_bfloat16* add;   // nullable [B][H][W][COUT], added after the activation
+    const __nv_bfloat16* mask;  // nullable [B][H][W][COUT]: ym = value where mask > 0, else 0
+    __nv_bfloat16* y;           // nullable [B][H][W][COUT]
+    __nv_bfloat16* ym;          // nullable [B][H][W][COUT]
+    float* yf;                  // nullable [B][H][W][4]: channels 0..3 in FP32
+    int B, H, W, relu;
+    int* status;                // set when a tensor-core completion wait gave up
+};
+cudaError_t filter_conv(int cin, int cout, const FilterConvArgs& a, cudaStream_t s);
+int filter_dw_ctas();
+cudaError_t filter_dw(int cin, int cout, const void* x, const void* x2, const void* g, int B, int H, int W, float* partial, int ctas,
+                      int* status, cudaStream_t s);
+cudaError_t filter_pack(const float* W, int coutReal, int cinReal, int cin, int cout, int transposed, void* out, cudaStream_t s);
+cudaError_t filter_dw_reduce(const float* partial, int ctas, int cout, int cin, int coutReal, int cinReal, float* dW, cudaStream_t s);
+cudaError_t filter_bias_grad(const void* g, size_t P, int C, int cReal, float* partial, int blocks, float* db, cudaStream_t s);
+cudaError_t filter_loss(const float4* out, const float4* target, size_t P, float scale, void* g, float* partial, int blocks, cudaStream_t s);
+cudaError_t filter_adam(float* w, const float* grad, float* m, float* v, int n, float lr, float b1, float b2, float eps, float c1,
+                        float c2, cudaStream_t s);
+cudaError_t filter_gbuffer(const uint2* base, const uint2* normal, const uint2* rough, size_t P, float samples, void* out, cudaStream_t s);
+cudaError_t filter_composite(const uint2* base, const float4* pred, size_t P, const float fade[4], int showAlpha, uint2* finalImg,
+                             cudaStream_t s);
+cudaError_t filter_target(const uint2* rough, size_t P, float4* out, cudaStream_t s);
+cudaError_t filter_bias_pad(const float* b, int cReal, int c, float* out, cudaStream_t s);
+// the filter on one frame (G-buffers -> input -> network -> composite into finalImg); filter_api.cu
+cudaError_t filter_frame(rg_filter* f, const uint2* base, const uint2* normal, const uint2* rough, uint32_t W, uint32_t H, float samples,
+                         const float fade[4], int showAlpha, uint2* finalImg, cudaStream_t s);
+const float4* filter_prediction(const rg_filter* f);  // [P] of the last frame: RGB, w unused
 
 struct PostParams {
     uint32_t W, H;

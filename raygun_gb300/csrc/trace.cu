@@ -364,6 +364,7 @@ struct Payload {  // payload.h:29-39
     float roughA;
     float depth, curIOR, refDepth;
     int rayType, recDepth;
+    uint32_t seed;  // glossy reference shading: per-sample random seed (0: mirror shading); not in payload.h
 };
 
 // resume codes of a paused closest-hit invocation
@@ -458,6 +459,27 @@ struct RayReq {
 struct RayCounts {
     unsigned long long primary, shadow, secondary, masked;
 };
+
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t v) {  // PCG-RXS-M-XS (O'Neill 2014) output permutation
+    const uint32_t st = v * 747796405u + 2891336453u;
+    const uint32_t w = ((st >> ((st >> 28u) + 4u)) ^ st) * 277803737u;
+    return (w >> 22u) ^ w;
+}
+
+// Glossy reference shading: a GGX microfacet normal (Walter et al. 2007, alpha = roughness^2) drawn
+// around n from two uniforms of the sample's seed and stream k
+__device__ __forceinline__ V3 ggx_normal(V3 n, float roughness, uint32_t seed, uint32_t k) {
+    const uint32_t h1 = pcg_hash(seed * 2654435761u + k), h2 = pcg_hash(h1 ^ 0x9E3779B9u);
+    const float u1 = (float)(h1 >> 8) * (1.0f / 16777216.0f), u2 = (float)(h2 >> 8) * (1.0f / 16777216.0f);
+    const float a = roughness * roughness;
+    const float tan2 = a * a * u1 / fmaxf(1.0f - u1, 1e-7f);
+    const float cosT = rsqrtf(1.0f + tan2), sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
+    const float phi = 6.28318530718f * u2;
+    // orthonormal basis around n (Duff et al. 2017)
+    const float sg = copysignf(1.0f, n.z), aa = -1.0f / (sg + n.z), bb = n.x * n.y * aa;
+    const V3 t = v3(1.0f + sg * n.x * n.x * aa, sg * bb, -sg * n.x), b = v3(bb, sg + n.y * n.y * aa, -n.y);
+    return normalize(t * (sinT * cosf(phi)) + b * (sinT * sinf(phi)) + n * cosT);
+}
 
 // One step of the closest-hit / miss state machine: consume the result `h` of the pending trace and
 // run the paused invocations on the frame stack until the next trace is needed (returns true, `ray`
@@ -591,6 +613,10 @@ __device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const
         } else if (ph == PH_G_REFLECT) {  // :206-221
             if (p.recDepth < maxRec && cur.reflectivity > 0.0f) {
                 V3 dir = reflect(cur.D, cur.n);
+                if (p.seed && p.recDepth == 0 && cur.roughness > 0.0f) {  // glossy reference shading
+                    const V3 g = reflect(cur.D, ggx_normal(cur.n, cur.roughness, p.seed, 1u));
+                    if (dot(g, cur.n) > 0.0f) dir = g;
+                }
                 p.recDepth += cur.rayConsumption;
                 p.refDepth = p.refDepth + cur.t;
                 cnt.secondary++;
@@ -604,14 +630,24 @@ __device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const
         } else if (ph == PH_G_REFRACT) {  // :223-251
             if (p.recDepth < maxRec && cur.transparency > 0.0f) {
                 V3 dir;
+                const bool glossy = p.seed && p.recDepth == 0 && cur.roughness > 0.0f;
+                const V3 mn = glossy ? ggx_normal(cur.n, cur.roughness, p.seed, 2u) : cur.n;
                 if (cur.front) {
                     float eta = p.curIOR / cur.ior;
                     dir = refract(cur.D, cur.n, eta);
+                    if (glossy) {  // glossy reference shading: refraction through the sampled microfacet
+                        const V3 g = refract(cur.D, mn, eta);
+                        if (!(g.x == 0.0f && g.y == 0.0f && g.z == 0.0f)) dir = g;
+                    }
                     p.curIOR = cur.ior;
                     cur.kind = R_G_REFR_F;
                 } else {
                     float eta = cur.ior / 1.0f;
                     dir = refract(cur.D, cur.n, eta);
+                    if (glossy) {
+                        const V3 g = refract(cur.D, mn, eta);
+                        if (!(g.x == 0.0f && g.y == 0.0f && g.z == 0.0f)) dir = g;
+                    }
                     p.curIOR = 1.0f;
                     cur.kind = R_G_REFR_B;
                 }
@@ -701,7 +737,7 @@ __device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const
 
 // raygen.h:84-102: camera ray of one sample and the payload initialisation
 __device__ __forceinline__ void start_sample(const rg_ubo& U, const V3 camO, uint32_t px, uint32_t py, uint32_t W, uint32_t H,
-                                             int sample, int aaRow, Payload& p, RayReq& ray) {
+                                             int sample, int aaRow, Payload& p, RayReq& ray, uint32_t glossySeed = 0u) {
     float pcx = ((float)px + 0.5f) + kAA[aaRow][sample & 7][0];
     float pcy = ((float)py + 0.5f) + kAA[aaRow][sample & 7][1];
     float ux = pcx / (float)W, uy = pcy / (float)H;
@@ -726,6 +762,7 @@ __device__ __forceinline__ void start_sample(const rg_ubo& U, const V3 camO, uin
     p.rayType = RT_GENERIC;
     p.recDepth = 0;
     p.reflectContribution = 0.0f;
+    p.seed = glossySeed ? ((pcg_hash(glossySeed ^ pcg_hash(px + pcg_hash(py + pcg_hash((uint32_t)sample)))) & 0xFFFFFFu) | 1u) : 0u;
 }
 
 #ifndef RG_TRACE_STEPS
@@ -823,7 +860,7 @@ __global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(co
                         px = (tile % tilesX) * kTileW + within % kTileW;
                         py = (tile / tilesX) * kTileH + within / kTileW;
                         if (px < P.W && py < P.H) {
-                            start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray);
+                            start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray, P.glossySeed);
                             cnt.primary++;
                             fsp = 0;
                             state = begin_ray(T, sc, ray);
@@ -918,7 +955,7 @@ __device__ __forceinline__ void store_payload(float4* dst, const Payload& p) {
     dst[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
     dst[1] = make_float4(p.normal.x, p.normal.y, p.normal.z, p.depth);
     dst[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
-    dst[3] = make_float4(p.curIOR, p.refDepth, __int_as_float(p.rayType), __int_as_float(p.recDepth));
+    dst[3] = make_float4(p.curIOR, p.refDepth, __uint_as_float((uint32_t)p.rayType | (p.seed << 8)), __int_as_float(p.recDepth));
 }
 
 __device__ __forceinline__ void load_payload(const float4* src, Payload& p) {
@@ -931,7 +968,8 @@ __device__ __forceinline__ void load_payload(const float4* src, Payload& p) {
     p.roughA = c.w;
     p.curIOR = d.x;
     p.refDepth = d.y;
-    p.rayType = __float_as_int(d.z);
+    p.rayType = (int)(__float_as_uint(d.z) & 0xFFu);
+    p.seed = __float_as_uint(d.z) >> 8;
     p.recDepth = __float_as_int(d.w);
 }
 
@@ -989,7 +1027,7 @@ __device__ __forceinline__ bool batch_primary(const TraceParams& P, uint32_t id,
     float org[4];
     mul4(J.ubo.viewInverse, 0.0f, 0.0f, 0.0f, 1.0f, org);
     const int aaRow = J.S < 8 ? (int)J.S : 8;
-    start_sample(J.ubo, v3(org[0], org[1], org[2]), px, py, J.W, J.H, (int)s, aaRow, p, ray);
+    start_sample(J.ubo, v3(org[0], org[1], org[2]), px, py, J.W, J.H, (int)s, aaRow, p, ray, P.glossySeed);
     sampleIdx = J.sampleBase + (py * J.W + px) * J.S + s;
     return true;
 }
@@ -1020,7 +1058,7 @@ __global__ void __launch_bounds__(256) k_wf_raygen(const TraceParams P) {
         if (valid) {
             Payload p;
             RayReq ray;
-            start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray);
+            start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray, P.glossySeed);
             const uint32_t path = (py * P.W + px) * S + sample;
             store_payload(wf.payload + 4 * (size_t)path, p);
             wf.meta[path] = make_int2(0, 0);

@@ -25,7 +25,7 @@ RG_FLAG_MEGAKERNEL = 4
 RG_FLAG_KERNEL_TIMING = 8
 RG_FLAG_HOST_LOOP = 16
 IMAGES = {"final": 0, "base": 1, "normal": 2, "rough": 3, "rough_transition": 4, "rough_colors_a": 5,
-          "rough_colors_b": 6, "pre_fxaa": 7}
+          "rough_colors_b": 6, "pre_fxaa": 7, "filter_out": 8}
 
 EXPORTS = [
     "rg_create", "rg_destroy", "rg_last_error", "rg_upload_geometry", "rg_update_vertices", "rg_update_materials",
@@ -35,8 +35,13 @@ EXPORTS = [
     "rg_update_vertices_device", "rg_get_total_stats", "rg_reset_total_stats", "rg_set_flags", "rg_launch_count",
     "rg_lbvh_build_device_noalloc", "rg_scene_create", "rg_scene_select", "rg_scene_destroy", "rg_scene_bytes",
     "rg_render_batch", "rg_batch_framebuffer", "rg_batch_download", "rg_set_batch_tune", "rg_get_batch_tune",
-    "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory",
+    "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory", "rg_filter_create", "rg_filter_destroy",
+    "rg_filter_last_error", "rg_filter_get_params", "rg_filter_set_params", "rg_filter_get_grads", "rg_filter_forward",
+    "rg_filter_train_step", "rg_filter_input", "rg_filter_target", "rg_set_filter", "rg_set_glossy",
 ]
+FILTER_PARAMS = 78243
+# layer shapes of the learned filter: (out, in) real channel counts
+FILTER_LAYERS = ((32, 12), (64, 32), (64, 64), (32, 64), (3, 32))
 
 # rg_job (include/rgcuda.h): one render of a batch
 JOB = np.dtype([("scene", "<u4"), ("width", "<u4"), ("height", "<u4"), ("fxaa", "<i4"), ("ubo", scenes.UBO)])
@@ -131,6 +136,18 @@ def load(path: str = LIB_PATH):
         "rg_set_batch_slots": ([P, U32], I32),
         "rg_autotune_batch": ([P, P, U32, U32, ctypes.POINTER(BatchTune), P], I32),
         "rg_get_memory": ([P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)], I32),
+        "rg_filter_create": ([P, ctypes.c_uint64, ctypes.POINTER(P)], I32),
+        "rg_filter_destroy": ([P], I32),
+        "rg_filter_last_error": ([P], ctypes.c_char_p),
+        "rg_filter_get_params": ([P, P, U32], I32),
+        "rg_filter_set_params": ([P, P, U32], I32),
+        "rg_filter_get_grads": ([P, P, U32], I32),
+        "rg_filter_forward": ([P, P, U32, U32, U32, P], I32),
+        "rg_filter_train_step": ([P, P, P, U32, U32, U32, ctypes.c_float, ctypes.POINTER(ctypes.c_float)], I32),
+        "rg_filter_input": ([P, P], I32),
+        "rg_filter_target": ([P, P], I32),
+        "rg_set_filter": ([P, P], I32),
+        "rg_set_glossy": ([P, U32], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -335,6 +352,21 @@ class Context:
         self._ck(self.L.rg_get_memory(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def set_filter(self, flt):
+        self._filter = flt
+        self._ck(self.L.rg_set_filter(self.h, flt.h if flt is not None else None))
+
+    def set_glossy(self, seed: int):
+        self._ck(self.L.rg_set_glossy(self.h, seed))
+
+    def filter_input(self, dev_ptr: int):
+        """The last frame's 16-channel BF16 filter input into device memory [H][W][16]."""
+        self._ck(self.L.rg_filter_input(self.h, ctypes.c_void_p(dev_ptr)))
+
+    def filter_target(self, dev_ptr: int):
+        """The last frame's rough RGB as FP32 [H][W][4] into device memory."""
+        self._ck(self.L.rg_filter_target(self.h, ctypes.c_void_p(dev_ptr)))
+
     def set_batch_slots(self, slots: int):
         self._ck(self.L.rg_set_batch_slots(self.h, slots))
 
@@ -457,3 +489,65 @@ class BatchRenderer:
         jobs = self.jobs(fxaa) if jobs is None else jobs
         self.ctx.render_batch(jobs)
         return [self.ctx.batch_download(k) for k in range(len(jobs))]
+
+
+class Filter:
+    """The learned roughness filter (rg_filter_*): parameters, forward, Adam training step."""
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.L = ctx.L
+        self.ctx = ctx
+        self.h = ctypes.c_void_p()
+        rc = self.L.rg_filter_create(ctx.h, seed, ctypes.byref(self.h))
+        if rc != RG_OK:
+            raise RgError(rc, "rg_filter_create failed")
+
+    def _ck(self, rc):
+        if rc != RG_OK:
+            raise RgError(rc, self.L.rg_filter_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.L.rg_filter_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(FILTER_PARAMS, np.float32)
+        self._ck(self.L.rg_filter_get_params(self.h, _p(out), FILTER_PARAMS))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self._ck(self.L.rg_filter_set_params(self.h, _p(p), len(p)))
+
+    def grads(self) -> np.ndarray:
+        out = np.zeros(FILTER_PARAMS, np.float32)
+        self._ck(self.L.rg_filter_get_grads(self.h, _p(out), FILTER_PARAMS))
+        return out
+
+    def forward(self, d_in: int, batch: int, height: int, width: int, d_out: int):
+        self._ck(self.L.rg_filter_forward(self.h, ctypes.c_void_p(d_in), batch, height, width, ctypes.c_void_p(d_out)))
+
+    def train_step(self, d_in: int, d_target: int, batch: int, height: int, width: int, lr: float) -> float:
+        loss = ctypes.c_float()
+        self._ck(self.L.rg_filter_train_step(self.h, ctypes.c_void_p(d_in), ctypes.c_void_p(d_target), batch, height, width,
+                                             ctypes.c_float(lr), ctypes.byref(loss)))
+        return loss.value
+
+
+def filter_layers(params: np.ndarray):
+    """Split a parameter vector into [(W[out][in][3][3], b[out])] per layer."""
+    out, off = [], 0
+    for co, ci in FILTER_LAYERS:
+        w = params[off:off + co * ci * 9].reshape(co, ci, 3, 3)
+        off += co * ci * 9
+        b = params[off:off + co]
+        off += co
+        out.append((w, b))
+    return out
