@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="rows per render of the CPU-baseline sample (0: full frames)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", default="1920x1080", help="WxH; smaller sizes are for profiling captures only")
-    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch", "serve"],
+    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch", "serve", "filter"],
                     help="game-frame: the 1080p 4x SSAA frame loop; batch: 64 independent scenes per step; "
                          "serve: Poisson render requests through the render server")
     ap.add_argument("--serve-requests", type=int, default=2000)
@@ -64,6 +64,12 @@ def parse():
     ap.add_argument("--serve-large", type=int, default=12, help="large terrain scenes in the catalog")
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
     ap.add_argument("--serve-graph", action="store_true", help="serve: CUDA-graph batches instead of the host loop")
+    ap.add_argument("--filter-scenes", type=int, default=200, help="filter: training scenes")
+    ap.add_argument("--filter-crops", type=int, default=20000, help="filter: 128x128 training crops")
+    ap.add_argument("--filter-epochs", type=int, default=30)
+    ap.add_argument("--filter-eval", type=int, default=4, help="filter: held-out 1080p scenes")
+    ap.add_argument("--filter-weights", default=None, help="filter: load these weights instead of training")
+    ap.add_argument("--filter-save", default=None, help="filter: write the trained weights here")
     ap.add_argument("--no-tune", action="store_true", help="batch: skip the autotuner (default launch shape)")
     ap.add_argument("--batch-scenes", type=int, default=64, help="batch: scenes per batch (profiling captures only)")
     return ap.parse_args()
@@ -558,6 +564,65 @@ def run_serve(args):
         print(json.dumps(out), flush=True)
 
 
+FILTER_FLOPS_PER_PX = 2 * 9 * (12 * 32 + 32 * 64 + 64 * 64 + 64 * 32 + 32 * 3)  # 156,096 (all layers at full resolution)
+
+
+def measured_peak_bf16():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+def run_filter(args):
+    import torch
+    from raygun_gb300 import build as rgbuild, rgcuda, filter_train as FT
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    rgbuild.build()
+    ctx = rgcuda.Context(device=local)
+    flt = rgcuda.Filter(ctx, seed=1)
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+    t0 = time.perf_counter()
+    if args.filter_weights:
+        FT.load_weights(flt, args.filter_weights)
+        data, stats = None, {"loaded": args.filter_weights}
+    else:
+        X, T = FT.build_dataset(ctx, args.filter_scenes, 640, 360, log=log)
+        data = {"scenes": args.filter_scenes, "frame": "640x360", "seconds": time.perf_counter() - t0}
+        stats = FT.train(flt, X, T, args.filter_crops, args.filter_epochs, log=log)
+        del X, T
+        if args.filter_save:
+            FT.save_weights(flt, args.filter_save)
+    mean, rows = FT.evaluate(flt, args.filter_eval, log=log)
+    times = FT.post_times(flt)
+    px = 1920 * 1080
+    filt_ms = times["learned"]["rough_ms"]
+    achieved = FILTER_FLOPS_PER_PX * px / (filt_ms * 1e-3) / 1e12
+    peak, src = measured_peak_bf16()
+    out = {
+        "metric": "rough-reflection PSNR (dB) of the learned filter against 256-spp glossy references",
+        "value": mean["rough_psnr_learned"], "unit": "dB", "n_gpus": world, "steps": stats.get("steps", 0), "warmup": 0,
+        "ms_per_step": filt_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)",
+        "data": "synthetic: training frames and 256-spp glossy targets rendered by the tracer from seeded scenes (no dataset)",
+        "config": {"workload": "learned roughness filter: 5-layer 3x3 conv 12-32-64-64-32-3, ReLU, skip 1->5, BF16 / FP32 "
+                               "accumulate on tcgen05; trained on 128x128 crops of 1-spp G-buffers vs 256-spp glossy renders; "
+                               "evaluated on held-out 1080p frames", "training_scenes": args.filter_scenes,
+                   "crops": args.filter_crops, "epochs": args.filter_epochs, "eval_scenes": args.filter_eval,
+                   "parallelism": "single GPU"},
+        "quality": mean, "quality_per_scene": rows, "training": stats, "dataset": data,
+        "post_times_ms": times,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "kernel": "filter stage of a 1080p frame (G-buffer pack, 5 convolutions, composite); FLOPs counted "
+                               f"{FILTER_FLOPS_PER_PX} per pixel", "peak_source": f"{src} bf16_tflops"},
+        "frame_time_ratio": times["learned"]["frame_ms"] / times["plain"]["frame_ms"],
+    }
+    print(json.dumps(out), flush=True)
+
+
 def cpu_baseline_batch(scenes, min_seconds=10.0, max_passes=10):
     """The oracle on all host cores over the whole batch (every scene, every row), repeated until at
     least `min_seconds` of CPU work."""
@@ -645,6 +710,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "filter":
+        run_filter(args)
     else:
         run_ours(args)
 

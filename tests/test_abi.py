@@ -81,3 +81,11 @@ def test_batch_scene_generators():
 
 def test_job_layout(rg):
     assert rg.JOB.itemsize == 208 and rg.JOB.fields["ubo"][1] == 16
+
+
+def test_filter_weights_file():
+    from raygun_gb300 import filter_train as FT, rgcuda
+    w = np.fromfile(FT.WEIGHTS, dtype="<f4")
+    assert len(w) == rgcuda.FILTER_PARAMS and np.isfinite(w).all()
+    layers = rgcuda.filter_layers(w)
+    assert [l[0].shape for l in layers] == [(32, 12, 3, 3), (64, 32, 3, 3), (64, 64, 3, 3), (32, 64, 3, 3), (3, 32, 3, 3)]

@@ -169,3 +169,29 @@ def test_glossy_shading(rg):
         assert np.isfinite(glossy).all()
         assert np.array_equal(glossy, mirror) != rough
         rt.ctx.close()
+
+
+def test_trained_weights_beat_the_plain_passes(rg):
+    """The committed weights (trained by bench.py --workload filter) on a scene they never saw: the
+    prediction is closer to the 256-spp glossy reference than the plain roughness approximation."""
+    import torch
+    from raygun_gb300 import filter_train as FT
+    W, H = 320, 180
+    sc = FT.training_scene(123456, W, H)
+    ctx = rg.Context(flags=rg.RG_FLAG_DEBUG_IMAGES)
+    flt = rg.Filter(ctx)
+    FT.load_weights(flt)
+    d_in = torch.zeros(H, W, 16, dtype=torch.bfloat16, device="cuda")
+    d_t = torch.zeros(H, W, 4, device="cuda")
+    FT.render_pair(ctx, sc, d_in, d_t, seed=7)
+    target = d_t.cpu().numpy()
+    slot = ctx.scene_create()
+    ctx.scene_select(slot)
+    rg.load_scene(ctx, sc)
+    ctx.render(sc.ubo, False)
+    plain = ctx.download_image("rough_colors_a")
+    ctx.set_filter(flt)
+    ctx.render(sc.ubo, False)
+    learned = ctx.download_image("filter_out")
+    p_plain, p_learned = FT.psnr(plain[..., :3], target[..., :3]), FT.psnr(learned[..., :3], target[..., :3])
+    assert p_learned > p_plain + 2.0, (p_plain, p_learned)
