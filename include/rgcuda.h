@@ -255,7 +255,9 @@ rg_status rg_get_batch_tune(rg_ctx* ctx, rg_batch_tune* out);
  * Parameters: per layer W[out][in][3][3] then b[out], FP32, real channel counts. */
 typedef struct rg_filter rg_filter;
 #define RG_FILTER_PARAMS 78243u
-rg_status rg_filter_create(rg_ctx* ctx, uint64_t seed, rg_filter** out);  /* He-normal weights; ctx's device and stream */
+/* He-normal weights, on ctx's device with a stream of its own (frames of a context run it on the
+ * context's stream); independent of ctx's lifetime */
+rg_status rg_filter_create(rg_ctx* ctx, uint64_t seed, rg_filter** out);
 rg_status rg_filter_destroy(rg_filter* f);
 const char* rg_filter_last_error(const rg_filter* f);
 rg_status rg_filter_get_params(rg_filter* f, float* host, uint32_t n);

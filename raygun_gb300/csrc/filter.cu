@@ -16,6 +16,9 @@
 //
 // Descriptor conventions (no swizzle): core matrix = 8 rows x 16 bytes; the leading-byte offset is
 // the stride between core matrices along K, the stride-byte offset the stride along M / N.
+#include <algorithm>
+
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "rg_internal.cuh"
@@ -76,6 +79,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, int* s
     if (!done && status) atomicExch(status, 1);
     return done != 0;
 }
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+// TMA: box of a 4-D tensor map at coordinates (c0 innermost) into shared memory, completing on mbar
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // 16 consecutive FP32 columns of this thread's TMEM lane
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
@@ -129,27 +145,38 @@ template <int CIN, int COUT>
 struct ConvShape {
     static constexpr int kWeightBytes = 9 * CIN * COUT * 2;
     static constexpr int kPatchBytes = (CIN / 8) * kPatchPlane;
-    static constexpr int kSmem = kWeightBytes + kPatchBytes + 1024;
+    static constexpr int kSmem = kWeightBytes + 2 * kPatchBytes + 1024;  // weights + two patch buffers + alignment
     static constexpr uint32_t kCols = kTileRows * COUT < 32 ? 32 : kTileRows * COUT;
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "shape");
     static_assert((kCols & (kCols - 1)) == 0, "TMEM columns must be a power of two");
+    static_assert(kWeightBytes % 1024 == 0 || kWeightBytes % 128 == 0, "patch buffers 128-byte aligned");
 };
 
+// Persistent CTA over tiles blockIdx.x, + gridDim.x, ...  One thread issues the TMA loads (one box of
+// 8 channels x 130 pixels x 4 rows per channel chunk, zero-filled outside the image) for tile i + 1
+// into the other patch buffer while tile i's MMAs and epilogue run.
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128, 1) k_filter_conv(const FilterConvArgs a) {
-    using bf16 = __nv_bfloat16;
+__global__ void __launch_bounds__(128) k_filter_conv(const __grid_constant__ CUtensorMap tmapX, const FilterConvArgs a) {
     using S = ConvShape<CIN, COUT>;
+    using bf16 = __nv_bfloat16;
+    constexpr int CC = CIN / 8;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* wsm = smem;
-    uint8_t* patch = smem + S::kWeightBytes;
+    uint8_t* patch[2] = {smem + S::kWeightBytes, smem + S::kWeightBytes + S::kPatchBytes};
     __shared__ uint32_t tmem_base;
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbarMma;
+    __shared__ __align__(8) uint64_t mbarLoad[2];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // weights once per CTA
     for (int i = tid; i < S::kWeightBytes / 16; i += blockDim.x)
         reinterpret_cast<uint4*>(wsm)[i] = reinterpret_cast<const uint4*>(a.w)[i];
-    if (tid == 0) mbar_init(&mbar, 1);
+    if (tid == 0) {
+        mbar_init(&mbarMma, 1);
+        mbar_init(&mbarLoad[0], 1);
+        mbar_init(&mbarLoad[1], 1);
+        mbar_init_fence();
+    }
+    async_proxy_fence();  // the weight tile is read by the tensor core
     if (warp == 0) tmem_alloc(&tmem_base, S::kCols);
     tc_fence_before();
     __syncthreads();
@@ -157,35 +184,54 @@ __global__ void __launch_bounds__(128, 1) k_filter_conv(const FilterConvArgs a) 
     const uint32_t tmem = tmem_base;
     const int tilesX = (a.W + kTilePx - 1) / kTilePx, tilesY = (a.H + kTileRows - 1) / kTileRows;
     const int tiles = a.B * tilesY * tilesX;
-    constexpr uint32_t idesc = umma_idesc(128, COUT, false, false);
-    uint32_t phase = 0;
-    bool ok = true;
-    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+    const int mine = blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto issue_load = [&](int i) {  // tile i of this CTA into patch[i & 1]
+        const int t = blockIdx.x + i * gridDim.x;
         const int b = t / (tilesY * tilesX), rem = t % (tilesY * tilesX);
         const int y0 = (rem / tilesX) * kTileRows, x0 = (rem % tilesX) * kTilePx;
-        load_patch<CIN>(patch, a.x, a.x2, b, y0, x0, a.H, a.W);
-        async_proxy_fence();
-        __syncthreads();
-        if (tid == 0) {
+        uint64_t* mb = &mbarLoad[i & 1];
+        mbar_expect_tx(mb, (uint32_t)S::kPatchBytes);
+#pragma unroll 1
+        for (int cc = 0; cc < CC; ++cc) tma_load_4d(patch[i & 1] + cc * kPatchPlane, &tmapX, cc * 8, x0 - 1, y0 - 1, b, mb);
+    };
+    int issued = 0, consumed = 0, mmas = 0;  // loads issued (thread 0), loads waited for, MMA batches waited for
+    if (tid == 0 && mine > 0) {
+        issue_load(0);
+        issued = 1;
+    }
+    constexpr uint32_t idesc = umma_idesc(128, COUT, false, false);
+    bool ok = true;
+    for (int i = 0; i < mine && ok; ++i) {
+        const int t = blockIdx.x + i * gridDim.x;
+        const int b = t / (tilesY * tilesX), rem = t % (tilesY * tilesX);
+        const int y0 = (rem / tilesX) * kTileRows, x0 = (rem % tilesX) * kTilePx;
+        if (tid == 0 && i + 1 < mine) {  // the other buffer's MMAs completed in iteration i - 1
+            issue_load(i + 1);
+            issued = i + 2;
+        }
+        const bool loaded = mbar_wait(&mbarLoad[i & 1], (uint32_t)((i >> 1) & 1), a.status);
+        if (loaded) consumed = i + 1;
+        if (tid == 0 && loaded) {
             tc_fence_after();
-            const uint32_t pbase = smem_u32(patch), wbase = smem_u32(wsm);
+            const uint32_t pbase = smem_u32(patch[i & 1]), wbase = smem_u32(wsm);
 #pragma unroll 1
             for (int r = 0; r < kTileRows; ++r)
 #pragma unroll 1
                 for (int tap = 0; tap < 9; ++tap) {
                     const int dy = tap / 3, dx = tap % 3;
-#pragma unroll 1
+#pragma unroll
                     for (int kk = 0; kk < CIN / 16; ++kk) {
                         const uint64_t ad = umma_desc(pbase + (uint32_t)(2 * kk * kPatchPlane + ((r + dy) * kPatchW + dx) * 16),
                                                       kPatchPlane, 128);
-                        const uint64_t bd = umma_desc(wbase + (uint32_t)((tap * (CIN / 8) + 2 * kk) * COUT * 16), COUT * 16, 128);
+                        const uint64_t bd = umma_desc(wbase + (uint32_t)((tap * CC + 2 * kk) * COUT * 16), COUT * 16, 128);
                         umma(tmem + (uint32_t)(r * COUT), ad, bd, idesc, (tap | kk) ? 1u : 0u);
                     }
                 }
-            umma_commit(&mbar);
+            umma_commit(&mbarMma);
         }
-        ok = __syncthreads_and(mbar_wait(&mbar, phase, a.status)) != 0;
-        phase ^= 1u;
+        const bool computed = loaded && mbar_wait(&mbarMma, (uint32_t)(i & 1), a.status);
+        if (computed) mmas = i + 1;
+        ok = __syncthreads_and(computed) != 0;
         tc_fence_after();
         if (ok) {
 #pragma unroll 1
@@ -203,12 +249,6 @@ __global__ void __launch_bounds__(128, 1) k_filter_conv(const FilterConvArgs a) 
                         if (a.bias) v[j] += a.bias[c0 + j];
                         if (a.relu) v[j] = fmaxf(v[j], 0.0f);
                     }
-                    if (a.add) {
-                        const bf16* ad = a.add + px * COUT + c0;
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) v[j] += __bfloat162float(ad[j]);
-                    }
-                    if (a.yf && c0 == 0) reinterpret_cast<float4*>(a.yf)[px] = make_float4(v[0], v[1], v[2], v[3]);
                     __align__(16) bf16 o[16];
                     if (a.y) {
 #pragma unroll
@@ -217,10 +257,35 @@ __global__ void __launch_bounds__(128, 1) k_filter_conv(const FilterConvArgs a) 
                         dst[0] = reinterpret_cast<uint4*>(o)[0];
                         dst[1] = reinterpret_cast<uint4*>(o)[1];
                     }
-                    if (a.ym) {
-                        const bf16* m = a.mask + px * COUT + c0;
+                    if (a.add) {
+                        const uint4* ad = reinterpret_cast<const uint4*>(a.add + px * COUT + c0);
+                        const uint4 u0 = ad[0], u1 = ad[1];
+                        const bf16* h0 = reinterpret_cast<const bf16*>(&u0);
+                        const bf16* h1 = reinterpret_cast<const bf16*>(&u1);
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) o[j] = __float2bfloat16(__bfloat162float(m[j]) > 0.0f ? v[j] : 0.0f);
+                        for (int j = 0; j < 8; ++j) {
+                            v[j] += __bfloat162float(h0[j]);
+                            v[8 + j] += __bfloat162float(h1[j]);
+                        }
+                    }
+                    if (a.ya) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) o[j] = __float2bfloat16(v[j]);
+                        uint4* dst = reinterpret_cast<uint4*>(a.ya + px * COUT + c0);
+                        dst[0] = reinterpret_cast<uint4*>(o)[0];
+                        dst[1] = reinterpret_cast<uint4*>(o)[1];
+                    }
+                    if (a.yf && c0 == 0) reinterpret_cast<float4*>(a.yf)[px] = make_float4(v[0], v[1], v[2], v[3]);
+                    if (a.ym) {
+                        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + px * COUT + c0);
+                        const uint4 u0 = mp[0], u1 = mp[1];
+                        const bf16* m0 = reinterpret_cast<const bf16*>(&u0);
+                        const bf16* m1 = reinterpret_cast<const bf16*>(&u1);
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            o[j] = __float2bfloat16(__bfloat162float(m0[j]) > 0.0f ? v[j] : 0.0f);
+                            o[8 + j] = __float2bfloat16(__bfloat162float(m1[j]) > 0.0f ? v[8 + j] : 0.0f);
+                        }
                         uint4* dst = reinterpret_cast<uint4*>(a.ym + px * COUT + c0);
                         dst[0] = reinterpret_cast<uint4*>(o)[0];
                         dst[1] = reinterpret_cast<uint4*>(o)[1];
@@ -231,6 +296,13 @@ __global__ void __launch_bounds__(128, 1) k_filter_conv(const FilterConvArgs a) 
         tc_fence_before();
         __syncthreads();
     }
+    // an abandoned pipeline may still have copies or MMAs in flight: wait for them (bounded) before
+    // the shared memory and the tensor memory go away
+    if (!ok && tid == 0) {
+        for (int k = consumed; k < issued; ++k) mbar_wait(&mbarLoad[k & 1], (uint32_t)((k >> 1) & 1), nullptr);
+        if (mmas < consumed) mbar_wait(&mbarMma, (uint32_t)(mmas & 1), nullptr);
+    }
+    __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, S::kCols);
 }
@@ -493,6 +565,52 @@ int persistent_blocks(K kernel, int smem) {
     return sms * (per > 0 ? per : 1);
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                   const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// tensor map of an NHWC BF16 activation [B][H][W][C]: boxes of 8 channels x 130 pixels x 4 rows
+cudaError_t patch_map(CUtensorMap* map, const void* x, int B, int H, int W, int C) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return cudaErrorNotSupported;
+    if ((reinterpret_cast<uintptr_t>(x) & 15u) != 0) return cudaErrorMisalignedAddress;
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)kPatchW, (cuuint32_t)kPatchRows, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// CTAs per SM of a persistent kernel: shared memory, registers and TMEM columns (512 per SM)
+template <class K>
+int ctas_per_sm(K kernel, int smem, uint32_t tmemCols) {
+    int dev = 0, smemSm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smemSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 1;
+    int per = smemSm / (smem + 1024);
+    per = std::min(per, 65536 / std::max(1, fa.numRegs * 128));
+    per = std::min(per, (int)(512 / tmemCols));
+    per = std::min(per, 16);
+    return std::max(per, 1);
+}
+
 template <int CIN, int COUT>
 cudaError_t conv_launch(const FilterConvArgs& a, cudaStream_t s) {
     using S = ConvShape<CIN, COUT>;
@@ -500,11 +618,16 @@ cudaError_t conv_launch(const FilterConvArgs& a, cudaStream_t s) {
     if (!grid) {
         cudaError_t e = cudaFuncSetAttribute(k_filter_conv<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
         if (e != cudaSuccess) return e;
-        grid = persistent_blocks(k_filter_conv<CIN, COUT>, S::kSmem);
-        if (!grid) return cudaErrorUnknown;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = sms * ctas_per_sm(k_filter_conv<CIN, COUT>, S::kSmem, S::kCols);
     }
+    CUtensorMap map;
+    cudaError_t e = patch_map(&map, a.x, a.B, a.H, a.W, CIN);
+    if (e != cudaSuccess) return e;
     const int tiles = a.B * ((a.H + kTileRows - 1) / kTileRows) * ((a.W + kTilePx - 1) / kTilePx);
-    k_filter_conv<CIN, COUT><<<tiles < grid ? tiles : grid, 128, S::kSmem, s>>>(a);
+    k_filter_conv<CIN, COUT><<<tiles < grid ? tiles : grid, 128, S::kSmem, s>>>(map, a);
     count_launch();
     return cudaGetLastError();
 }

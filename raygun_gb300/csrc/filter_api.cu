@@ -59,7 +59,7 @@ struct rg_filter {
     std::string err;
     int offW[kL], offB[kL];
     Dev params, grads, m, v, wf[kL], wt[kL], bias[kL], status;
-    Dev x0, y1, y2, y3, y4, out, g5, gx5, gp4, gp3, gp2, gp1, target, dwPartial, bPartial, lossPartial;
+    Dev x0, y1, y2, y3, y4, x5, out, g5, gx5, gp4, gp3, gp2, gp1, target, dwPartial, bPartial, lossPartial;
     size_t actPixels = 0;
     uint64_t steps = 0;
     bool packed = false;
@@ -98,6 +98,7 @@ rg_status ensure_activations(rg_filter* f, size_t P, bool training) {
     FCK(f->y2.ensure(2 * 64 * P));
     FCK(f->y3.ensure(2 * 64 * P));
     FCK(f->y4.ensure(2 * 32 * P));
+    FCK(f->x5.ensure(2 * 32 * P));
     if (training) {
         FCK(f->g5.ensure(2 * 16 * P));
         FCK(f->gx5.ensure(2 * 32 * P));
@@ -120,7 +121,7 @@ rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W) {
     using bf = __nv_bfloat16;
     const bf* w[kL];
     for (int l = 0; l < kL; ++l) w[l] = f->wf[l].as<bf>();
-    // layers 1-4: conv + bias + ReLU
+    // layers 1-4: conv + bias + ReLU; layer 4 also writes x5 = y4 + y1 (the skip)
     bf* outs[4] = {f->y1.as<bf>(), f->y2.as<bf>(), f->y3.as<bf>(), f->y4.as<bf>()};
     const bf* in = x0;
     for (int l = 0; l < 4; ++l) {
@@ -130,13 +131,16 @@ rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W) {
         c.bias = f->bias[l].as<float>();
         c.relu = 1;
         c.y = outs[l];
+        if (l == 3) {
+            c.add = f->y1.as<bf>();
+            c.ya = f->x5.as<bf>();
+        }
         FCK(filter_conv(kCin[l], kCout[l], c, f->stream));
         in = outs[l];
     }
-    // layer 5 on y4 + y1 (skip), linear, FP32 prediction
+    // layer 5 on x5, linear, FP32 prediction
     FilterConvArgs c = a;
-    c.x = f->y4.as<bf>();
-    c.x2 = f->y1.as<bf>();
+    c.x = f->x5.as<bf>();
     c.w = w[4];
     c.bias = f->bias[4].as<float>();
     c.yf = f->out.as<float>();
@@ -151,6 +155,8 @@ namespace rg {
 cudaError_t filter_frame(rg_filter* f, const uint2* base, const uint2* normal, const uint2* rough, uint32_t W, uint32_t H, float samples,
                          const float fade[4], int showAlpha, uint2* finalImg, cudaStream_t s) {
     const size_t P = (size_t)W * H;
+    cudaError_t e0 = cudaStreamSynchronize(f->stream);  // parameter updates issued on the filter's stream
+    if (e0 != cudaSuccess) return e0;
     cudaStream_t saved = f->stream;
     f->stream = s;
     cudaError_t e = f->x0.ensure(2 * 16 * P);
@@ -172,10 +178,15 @@ rg_status rg_filter_create(rg_ctx* ctx, uint64_t seed, rg_filter** out) {
     if (!ctx || !out) return RG_ERR_INVALID_ARG;
     *out = nullptr;
     void* s = nullptr;
-    if (rg_get_stream(ctx, &s) != RG_OK) return RG_ERR_INVALID_ARG;
+    if (rg_get_stream(ctx, &s) != RG_OK) return RG_ERR_INVALID_ARG;  // the context's device is current
     rg_filter* f = new rg_filter();
     cudaGetDevice(&f->device);
-    f->stream = static_cast<cudaStream_t>(s);
+    // its own stream: the filter may outlive the context it was created with; frames of a context
+    // run it on the context's stream (filter_frame)
+    if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete f;
+        return RG_ERR_CUDA;
+    }
     int off = 0;
     for (int l = 0; l < kL; ++l) {
         f->offW[l] = off;
@@ -219,7 +230,7 @@ rg_status rg_filter_destroy(rg_filter* f) {
     if (!f) return RG_ERR_INVALID_ARG;
     cudaSetDevice(f->device);
     if (f->stream) cudaStreamSynchronize(f->stream);
-    Dev* all[] = {&f->params, &f->grads, &f->m, &f->v, &f->status, &f->x0, &f->y1, &f->y2, &f->y3, &f->y4, &f->out, &f->g5, &f->gx5,
+    Dev* all[] = {&f->params, &f->grads, &f->m, &f->v, &f->status, &f->x0, &f->y1, &f->y2, &f->y3, &f->y4, &f->x5, &f->out, &f->g5, &f->gx5,
                   &f->gp4, &f->gp3, &f->gp2, &f->gp1, &f->target, &f->dwPartial, &f->bPartial, &f->lossPartial};
     for (Dev* d : all) d->release();
     for (int l = 0; l < kL; ++l) {
@@ -227,6 +238,7 @@ rg_status rg_filter_destroy(rg_filter* f) {
         f->wt[l].release();
         f->bias[l].release();
     }
+    if (f->stream) cudaStreamDestroy(f->stream);
     delete f;
     return RG_OK;
 }
@@ -302,8 +314,8 @@ rg_status rg_filter_train_step(rg_filter* f, const void* d_input, const float* d
     a.H = (int)H;
     a.W = (int)W;
     a.status = st;
-    // layer 5 (input y4 + y1)
-    TRY_F(dW(4, f->y4.p, f->y1.p, f->g5.p));
+    // layer 5 (input x5 = y4 + y1)
+    TRY_F(dW(4, f->x5.p, nullptr, f->g5.p));
     {
         FilterConvArgs c = a;  // gx5 (kept for the skip), gp4 = gx5 where y4 > 0
         c.x = f->g5.as<bf>();

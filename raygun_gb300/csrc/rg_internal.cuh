@@ -247,19 +247,20 @@ cudaError_t launch_resolve_job(const float4* samples, const JobDesc& hostJob, ui
 cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
 
 // ---- learned roughness filter (filter.cu) ----
-// one 3x3 convolution: y = epilogue(conv(x [+ x2], w) + bias); NHWC BF16 activations
+// one 3x3 convolution of NHWC BF16 activations (x 16-byte aligned): v = conv(x, w) + bias, then
+// ReLU (relu), y = v, v += add, ya = v, ym = v where mask > 0 else 0, yf = v[0..3] in FP32
 struct FilterConvArgs {
     const __nv_bfloat16* x;     // [B][H][W][CIN]
-    const __nv_bfloat16* x2;    // nullable, added to x
     const __nv_bfloat16* w;     // packed [9][CIN/8][COUT][8] (K = tap * CIN + ci, rows = output channels)
     const float* bias;          // nullable [COUT]
-    const __nv_bfloat16* add;   // nullable [B][H][W][COUT], added after the activation
-    const __nv_bfloat16* mask;  // nullable [B][H][W][COUT]: ym = value where mask > 0, else 0
+    const __nv_bfloat16* add;   // nullable [B][H][W][COUT]
+    const __nv_bfloat16* mask;  // nullable [B][H][W][COUT] (required with ym)
     __nv_bfloat16* y;           // nullable [B][H][W][COUT]
+    __nv_bfloat16* ya;          // nullable [B][H][W][COUT]
     __nv_bfloat16* ym;          // nullable [B][H][W][COUT]
-    float* yf;                  // nullable [B][H][W][4]: channels 0..3 in FP32
+    float* yf;                  // nullable [B][H][W][4]
     int B, H, W, relu;
-    int* status;                // set when a tensor-core completion wait gave up
+    int* status;                // set when a tensor-core or copy completion wait gave up
 };
 cudaError_t filter_conv(int cin, int cout, const FilterConvArgs& a, cudaStream_t s);
 int filter_dw_ctas();

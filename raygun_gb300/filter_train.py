@@ -209,3 +209,31 @@ def save_weights(flt, path: str = WEIGHTS):
 
 def load_weights(flt, path: str = WEIGHTS):
     flt.set_params(np.fromfile(path, dtype="<f4"))
+
+
+def main():
+    """python -m raygun_gb300.filter_train --infer W H [--repeat N]: the committed weights on a
+    seeded random 16-channel input of W x H (inference only; used for kernel profiles)."""
+    import argparse
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--infer", nargs=2, type=int, required=True, metavar=("W", "H"))
+    ap.add_argument("--repeat", type=int, default=3)
+    args = ap.parse_args()
+    W, H = args.infer
+    ctx = rg.Context()
+    flt = rg.Filter(ctx)
+    load_weights(flt)
+    g = torch.Generator().manual_seed(1)
+    x = torch.zeros(H, W, 16)
+    x[..., :12] = torch.rand(H, W, 12, generator=g)
+    d_in = x.to(torch.bfloat16).cuda()
+    d_out = torch.empty(H, W, 4, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(args.repeat):
+        flt.forward(d_in.data_ptr(), 1, H, W, d_out.data_ptr())
+    print(f"filter forward {W}x{H} x{args.repeat}: mean prediction {float(d_out[..., :3].mean()):.5f}")
+
+
+if __name__ == "__main__":
+    main()

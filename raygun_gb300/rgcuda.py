@@ -496,7 +496,6 @@ class Filter:
 
     def __init__(self, ctx: Context, seed: int = 0):
         self.L = ctx.L
-        self.ctx = ctx
         self.h = ctypes.c_void_p()
         rc = self.L.rg_filter_create(ctx.h, seed, ctypes.byref(self.h))
         if rc != RG_OK:
