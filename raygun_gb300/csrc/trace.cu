@@ -484,6 +484,7 @@ __device__ __forceinline__ V3 ggx_normal(V3 n, float roughness, uint32_t seed, u
 // One step of the closest-hit / miss state machine: consume the result `h` of the pending trace and
 // run the paused invocations on the frame stack until the next trace is needed (returns true, `ray`
 // set) or the sample's primary trace has returned (returns false).
+template <bool GLOSSY = true>
 __device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const int maxRec, const Hit& h, Payload& p, RayReq& ray,
                                            Frame* frames, int& fsp, Frame& cur, RayCounts& cnt) {
     int ph;
@@ -613,7 +614,7 @@ __device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const
         } else if (ph == PH_G_REFLECT) {  // :206-221
             if (p.recDepth < maxRec && cur.reflectivity > 0.0f) {
                 V3 dir = reflect(cur.D, cur.n);
-                if (p.seed && p.recDepth == 0 && cur.roughness > 0.0f) {  // glossy reference shading
+                if (GLOSSY && p.seed && p.recDepth == 0 && cur.roughness > 0.0f) {  // glossy reference shading
                     const V3 g = reflect(cur.D, ggx_normal(cur.n, cur.roughness, p.seed, 1u));
                     if (dot(g, cur.n) > 0.0f) dir = g;
                 }
@@ -630,7 +631,7 @@ __device__ __forceinline__ bool shade_step(const DevScene& sc, const V3 L, const
         } else if (ph == PH_G_REFRACT) {  // :223-251
             if (p.recDepth < maxRec && cur.transparency > 0.0f) {
                 V3 dir;
-                const bool glossy = p.seed && p.recDepth == 0 && cur.roughness > 0.0f;
+                const bool glossy = GLOSSY && p.seed && p.recDepth == 0 && cur.roughness > 0.0f;
                 const V3 mn = glossy ? ggx_normal(cur.n, cur.roughness, p.seed, 2u) : cur.n;
                 if (cur.front) {
                     float eta = p.curIOR / cur.ior;
@@ -1105,6 +1106,12 @@ __global__ void __launch_bounds__(256) k_wfb_raygen(const TraceParams P) {
 #ifndef RG_WF_STEPS
 #define RG_WF_STEPS 8
 #endif
+#ifndef RG_WHILE_WHILE
+#define RG_WHILE_WHILE 1
+#endif
+#ifndef RG_INNER_ROUNDS
+#define RG_INNER_ROUNDS 2
+#endif
 template <bool COUNT, bool BATCH, int THREADS, int DEPTH>
 __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k_wf_trace(const TraceParams P, int q) {
     RG_DECLARE_SMEM_STACK(stk, THREADS, DEPTH);
@@ -1148,6 +1155,32 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
             }
             if (!__any_sync(0xFFFFFFFFu, T.active || !exhausted)) break;
         }
+#if RG_WHILE_WHILE
+        // while-while: lanes on inner nodes descend together (the others wait), then every lane at a
+        // leaf processes it, so each pass runs one kind of step across most of the warp
+#pragma unroll 1
+        for (int k = 0; k < RG_WF_STEPS; ++k) {
+#pragma unroll 1
+            for (int j = 0; j < RG_INNER_ROUNDS; ++j) {
+                const bool inner = T.active && !(T.ref & kLeaf);
+                if (!__any_sync(0xFFFFFFFFu, inner)) break;
+                if (inner) {
+                    trav_step<COUNT>(T, RG_SC, stk, vc);
+                    if (!T.active) {
+                        wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
+                        wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;
+                    }
+                }
+            }
+            if (T.active && (T.ref & kLeaf)) {
+                trav_step<COUNT>(T, RG_SC, stk, vc);
+                if (!T.active) {
+                    wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
+                    wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;
+                }
+            }
+        }
+#else
         if (T.active) {
 #pragma unroll 1
             for (int k = 0; k < RG_WF_STEPS; ++k) {
@@ -1159,6 +1192,7 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
                 }
             }
         }
+#endif
     }
 #undef RG_SC
     unsigned long long c[3] = {vc.nodes, vc.tris, vc.overflow};
@@ -1174,11 +1208,12 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
 
 // shading of one path from a trace result up to its next traversed ray (false) or to the end of
 // its sample (true); mask-0 traces and zero directions run their miss shader right away
+template <bool GLOSSY>
 __device__ __forceinline__ bool shade_until_trace(const DevScene& sc, const V3 L, const int maxRec, Hit h, Payload& p, RayReq& ray,
                                                   Frame* frames, int& fsp, RayCounts& cnt) {
     Frame cur;
     for (;;) {
-        if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) return true;
+        if (!shade_step<GLOSSY>(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) return true;
         if (ray.masked || (ray.d.x == 0.0f && ray.d.y == 0.0f && ray.d.z == 0.0f)) {
             h.hit = false;
             continue;
@@ -1189,7 +1224,7 @@ __device__ __forceinline__ bool shade_until_trace(const DevScene& sc, const V3 L
 
 // shading of every result of queue q; next rays go to queue q^1, finished samples to P.samples.
 // BATCH: a slot whose path finished starts the batch's next work item in place.
-template <bool BATCH>
+template <bool BATCH, bool GLOSSY = false>
 __global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
     const WavefrontBuffers& wf = P.wf;
     const V3 L = v3(P.ubo.lightDir[0], P.ubo.lightDir[1], P.ubo.lightDir[2]);
@@ -1231,10 +1266,10 @@ __global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
             bool done;
             if constexpr (BATCH) {
                 const JobDesc& J = P.jobs[P.slotJob[path]];
-                done = shade_until_trace(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, h,
+                done = shade_until_trace<GLOSSY>(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, h,
                                          p, ray, frames, fsp, cnt);
             } else {
-                done = shade_until_trace(P.scene, L, maxRec, h, p, ray, frames, fsp, cnt);
+                done = shade_until_trace<GLOSSY>(P.scene, L, maxRec, h, p, ray, frames, fsp, cnt);
             }
             if (done) {
                 store_sample(P.samples + 3 * (size_t)(BATCH ? P.slotSample[path] : path), p);
@@ -1281,7 +1316,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
 }
 
 // the rest of one path, traced and shaded back to back
-template <class STACK>
+template <bool GLOSSY, class STACK>
 __device__ __forceinline__ void finish_path(const DevScene& sc, const V3 L, const int maxRec, RayReq& ray, Payload& p, Frame* frames,
                                             int& fsp, const STACK& stk, VisitCounts& vc, RayCounts& cnt) {
     Frame cur;
@@ -1289,14 +1324,14 @@ __device__ __forceinline__ void finish_path(const DevScene& sc, const V3 L, cons
         Hit h;
         h.hit = false;
         if (!ray.masked) h = closest_hit<false>(sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, stk, vc);
-        if (!shade_step(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) break;
+        if (!shade_step<GLOSSY>(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) break;
     }
 }
 
 // Tail of the wavefront loop: once few paths remain, one launch finishes every remaining path --
 // each thread traces and shades its path's remaining sequence back to back -- instead of one
 // (trace, shade) launch pair per remaining round.  BATCH: only after the last work item was taken.
-template <bool BATCH>
+template <bool BATCH, bool GLOSSY = false>
 __global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, int q) {
     RG_DECLARE_STACK(stk);
     const WavefrontBuffers& wf = P.wf;
@@ -1323,10 +1358,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, 
         Frame* frames = framesBase + (size_t)path * kMaxFrames;
         if constexpr (BATCH) {
             const JobDesc& J = P.jobs[P.slotJob[path]];
-            finish_path(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, ray, p, frames, fsp,
+            finish_path<GLOSSY>(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, ray, p, frames, fsp,
                         stk, vc, cnt);
         } else {
-            finish_path(P.scene, L0, maxRec0, ray, p, frames, fsp, stk, vc, cnt);
+            finish_path<GLOSSY>(P.scene, L0, maxRec0, ray, p, frames, fsp, stk, vc, cnt);
         }
         store_sample(P.samples + 3 * (size_t)(BATCH ? P.slotSample[path] : path), p);
     }
@@ -1532,9 +1567,13 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
     const int c = p.countVisits ? 1 : 0;
     const TraceKernel trace = trace_kernel(false, c, kTraceThreads, kTraversalStack);
     const int gTrace = grid_of((const void*)trace, kTraceThreads);
-    const int gShade = grid_of((const void*)k_wf_shade<false>, 128);
+    // glossy reference shading has kernels of its own; the reference's shading keeps the lean ones
+    typedef void (*WfKernel)(const TraceParams, int);
+    const WfKernel shade = p.glossySeed ? k_wf_shade<false, true> : k_wf_shade<false, false>;
+    const WfKernel tail = p.glossySeed ? k_wf_tail<false, true> : k_wf_tail<false, false>;
+    const int gShade = grid_of((const void*)shade, 128);
     const int gRaygen = grid_of((const void*)k_wf_raygen, 256);
-    const int gTail = grid_of((const void*)k_wf_tail<false>, kTraceThreads);
+    const int gTail = grid_of((const void*)tail, kTraceThreads);
     if (!gTrace || !gShade || !gRaygen || !gTail) return cudaErrorUnknown;
     cudaError_t e = cudaMemsetAsync(p.wf.counts, 0, 4 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
@@ -1552,7 +1591,7 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
             if (e0) cudaEventRecord(e0, s);
             trace<<<gTrace, kTraceThreads, 0, s>>>(p, q);
             if (e1) cudaEventRecord(e1, s);
-            k_wf_shade<false><<<gShade, 128, 0, s>>>(p, q);
+            shade<<<gShade, 128, 0, s>>>(p, q);
             count_launch(2);
             q ^= 1;
         }
@@ -1564,7 +1603,7 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
             if (e0) cudaEventRecord(e0, s);
-            k_wf_tail<false><<<gTail, kTraceThreads, 0, s>>>(p, q);
+            tail<<<gTail, kTraceThreads, 0, s>>>(p, q);
             if (e1) cudaEventRecord(e1, s);
             count_launch();
             break;
