@@ -175,7 +175,7 @@ using TravStack = LocalStackT<kTraversalStack>;
 #define RG_WF_MIN_BLOCKS 7
 #endif
 #ifndef RG_TAIL_RAYS
-#define RG_TAIL_RAYS 65536
+#define RG_TAIL_RAYS 32768
 #endif
 #ifndef RG_POLL_ROUNDS
 #define RG_POLL_ROUNDS 4
@@ -1224,8 +1224,11 @@ __device__ __forceinline__ bool shade_until_trace(const DevScene& sc, const V3 L
 
 // shading of every result of queue q; next rays go to queue q^1, finished samples to P.samples.
 // BATCH: a slot whose path finished starts the batch's next work item in place.
+#ifndef RG_SHADE_MIN_BLOCKS
+#define RG_SHADE_MIN_BLOCKS 6  // 85 registers, a few spilled: 6 blocks of 128 per SM beat 4 unspilled
+#endif
 template <bool BATCH, bool GLOSSY = false>
-__global__ void __launch_bounds__(128) k_wf_shade(const TraceParams P, int q) {
+__global__ void __launch_bounds__(128, BATCH ? 1 : RG_SHADE_MIN_BLOCKS) k_wf_shade(const TraceParams P, int q) {
     const WavefrontBuffers& wf = P.wf;
     const V3 L = v3(P.ubo.lightDir[0], P.ubo.lightDir[1], P.ubo.lightDir[2]);
     const int maxRec = P.ubo.maxRecursions;
