@@ -306,6 +306,12 @@ rg_status rg_autotune_batch(rg_ctx* ctx, const rg_job* jobs, uint32_t n, uint32_
  * internal node boxes (6 floats: lo xyz, hi xyz).  Pointers may be NULL.  *n_out = primitive count. */
 rg_status rg_bvh_info(rg_ctx* ctx, uint32_t blas, uint32_t* n_out, uint32_t* morton, uint32_t* order, uint32_t* left,
                       uint32_t* right, float* nodeboxes);
+/* The traversal's 4-wide records of a BLAS (blas) or of the TLAS (blas = 0xFFFFFFFF), one per
+ * internal LBVH node, 112 bytes each: float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4] (the
+ * boxes of the node's grandchildren, a leaf child standing in for its own slot); uint32 ref[4] (bit 31 =
+ * leaf; 0xFFFFFFFE = empty slot, box lo = +inf, hi = -inf).  Copies min(capacity, n - 1) records to
+ * out (may be NULL); *n_out = n - 1. */
+rg_status rg_bvh_records(rg_ctx* ctx, uint32_t blas, void* out, uint32_t capacity, uint32_t* n_out);
 /* World-to-object transforms the TLAS build computed (12 floats per instance). */
 rg_status rg_instance_inverse(rg_ctx* ctx, float* out);
 /* Closest hit of n rays (8 floats: origin.xyz, tmin, dir.xyz, tmax) through the current TLAS:

@@ -460,13 +460,29 @@ static void ray_pre(RayPre& r, const float* o, const float* d) {
 
 static const float kInflate = 1.0000004f;  // 1 + 2*gamma_3 (Ize 2013) rounded up
 
+// One axis of the slab test: the interval [min(t0, t1), max(t0, t1)].  A zero direction component
+// whose plane passes through the origin gives 0 * inf = NaN: the ray then runs inside that closed
+// slab, so the axis does not constrain t (-inf, +inf).  Without that rule min/max would drop the NaN
+// and reject boxes the ray lies on.
+static inline void slab_axis(float lo, float hi, float o, float id, float& n, float& f) {
+    const float t0 = (lo - o) * id, t1 = (hi - o) * id;
+    if (t0 != t0 || t1 != t1) {
+        n = -INFINITY;
+        f = INFINITY;
+        return;
+    }
+    n = std::fmin(t0, t1);
+    f = std::fmax(t0, t1);
+}
+
 // slab test against [tmin, tbest]; returns entry distance or +inf when missed
 static inline float slab(const RayPre& r, const Box& b, float tmin, float tbest) {
-    float t0x = (b.lo[0] - r.o[0]) * r.idir[0], t1x = (b.hi[0] - r.o[0]) * r.idir[0];
-    float t0y = (b.lo[1] - r.o[1]) * r.idir[1], t1y = (b.hi[1] - r.o[1]) * r.idir[1];
-    float t0z = (b.lo[2] - r.o[2]) * r.idir[2], t1z = (b.hi[2] - r.o[2]) * r.idir[2];
-    float tn = std::fmax(std::fmax(std::fmin(t0x, t1x), std::fmin(t0y, t1y)), std::fmax(std::fmin(t0z, t1z), tmin));
-    float tf = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)), std::fmin(std::fmax(t0z, t1z), tbest));
+    float nx, fx, ny, fy, nz, fz;
+    slab_axis(b.lo[0], b.hi[0], r.o[0], r.idir[0], nx, fx);
+    slab_axis(b.lo[1], b.hi[1], r.o[1], r.idir[1], ny, fy);
+    slab_axis(b.lo[2], b.hi[2], r.o[2], r.idir[2], nz, fz);
+    float tn = std::fmax(std::fmax(nx, ny), std::fmax(nz, tmin));
+    float tf = std::fmin(std::fmin(fx, fy), std::fmin(fz, tbest));
     return tn <= tf * kInflate ? tn : INFINITY;
 }
 

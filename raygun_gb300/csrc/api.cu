@@ -887,6 +887,26 @@ rg_status rg_bvh_info(rg_ctx* c, uint32_t b, uint32_t* n_out, uint32_t* morton, 
     return download_bvh(c, *s, morton, order, left, right, nodeboxes);
 }
 
+rg_status rg_bvh_records(rg_ctx* c, uint32_t b, void* out, uint32_t capacity, uint32_t* n_out) {
+    if (!c) return RG_ERR_INVALID_ARG;
+    const BvhSet* s = nullptr;
+    if (b == 0xFFFFFFFFu) {
+        if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+        s = &c->sc->tlas;
+    } else if (b < c->sc->blas.size()) {
+        s = &c->sc->blas[b].bvh;
+    } else {
+        return fail(c, RG_ERR_INVALID_ARG, "unknown BLAS");
+    }
+    const uint32_t m = s->n > 1 ? s->n - 1 : 0;
+    if (n_out) *n_out = m;
+    if (!out || !m || !capacity) return RG_OK;
+    TRY(set_device(c));
+    CK(cudaMemcpyAsync(out, s->wide.p, sizeof(WideNode) * (size_t)std::min(m, capacity), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
+}
+
 rg_status rg_instance_inverse(rg_ctx* c, float* out) {
     if (!c || !out) return RG_ERR_INVALID_ARG;
     if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");

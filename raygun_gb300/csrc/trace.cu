@@ -4,11 +4,12 @@
 // (render/raytracer.cpp:99-100; resources/shaders/raygen.h:69-115, raygen.rgen:30-39,
 // closesthit.rchit:74-268, miss.rmiss:38-83, shadowMiss.rmiss:30-34).
 //
-// GB300 has no RT cores, so traversal is software: a BVH2 whose nodes carry both children's
-// boxes (one 64-byte node = four 16-byte loads tests two children), near-child-first stack
-// traversal, TLAS leaves switch to the instance's BLAS with the ray moved into object space, and a
-// watertight ray/triangle test (Woop, Benthin, Wald 2013).  Closest-hit ties (equal t) resolve to
-// the smaller (instance, primitive).
+// GB300 has no RT cores, so traversal is software: 4-wide records derived from the BVH2 (one
+// 112-byte record = six 16-byte plane loads plus the refs tests four children), nearest-child-first
+// stack traversal, TLAS leaves switch to the instance's BLAS with the ray moved into object space, and
+// a watertight ray/triangle test (Woop, Benthin, Wald 2013).  Closest-hit ties (equal t) resolve to
+// the smaller (instance, primitive).  Box tests only ever accept more than the exact test would (see
+// the ray set-up below), so the hit found does not depend on the tree: it is the brute-force answer.
 //
 // The reference's recursion (nested traceRayEXT calls sharing ONE payload, payload.h:29-43) runs
 // here as an explicit state machine per thread: a paused closest-hit invocation is a Frame on a
@@ -28,18 +29,56 @@ namespace {
 
 // ---------------------------------------------------------------------------------------------
 // ray set-up and primitive tests
+//
+// Box tests use one fused multiply-add per plane: t = l * j + C with j = 1/d and C = -o/d.  C is a
+// rounded product, so it is kept as a bracket [cl, ch] around -o*j, and the products-sums are rounded
+// down for entry planes and up for exit planes: every computed entry is at or below the exact one and
+// every exit at or above, and the remaining rounding of 1/d itself is covered by the kInflate margin
+// (Ize 2013).  |j| is clamped to [2^-60, 2^64] so that nothing overflows: past 2^64 (a zero or tiny
+// direction component) the entry plane's t stays a lower bound where it is positive and the exit plane
+// is dropped (ch = +inf); below 2^-60 the exit plane's t stays an upper bound where it is positive and
+// the entry plane is dropped (cl = -inf).  Boxes are therefore never rejected when the exact test
+// accepts them, including rays that start on a plane with a zero direction component.  Which of a
+// box's two planes is the entry one follows from the sign of j (the ray's octant).
 struct Ray {
-    float ox, oy, oz, dx, dy, dz, ix, iy, iz;  // origin, direction, 1/direction
-    float Sx, Sy, Sz;
-    int kx, ky, kz;
+    float ox, oy, oz;              // origin of the current level (world, or the instance's object space)
+    float dx, dy, dz;              // WORLD direction (kept while inside a BLAS: only instance entry reads it)
+    float jx, jy, jz;              // 1/d of the current level, magnitude clamped to [2^-60, 2^64]
+    float clx, cly, clz;           // -o*j rounded down (-inf: entry planes dropped)
+    float chx, chy, chz;           // -o*j rounded up (+inf: exit planes dropped)
+    float Sx, Sy, Sz;              // shear of the watertight triangle test (BLAS level)
+    uint32_t bits;                 // kx | ky << 2 | kz << 4 (triangle test axes) | octant << 6
 };
 
 __device__ __forceinline__ float comp(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
 
+// j, cl, ch and the octant from the origin and 1/d
+__device__ __forceinline__ void box_terms(float o, float inv, float& j, float& cl, float& ch) {
+    const float ai = fabsf(inv);
+    j = copysignf(fminf(fmaxf(ai, 0x1p-60f), 0x1p64f), inv);
+    const float c = -(o * j);
+    const float err = fabsf(c) * 0x1p-22f;  // |c - (-o j)| <= 2^-24 |c| (one rounding)
+    // the drop rules read j alone (so that a saved j restores the same terms); at exactly 2^64 or
+    // 2^-60 dropping a plane only accepts more
+    cl = fabsf(j) > 0x1p-60f ? __fsub_rd(c, err) : -INFINITY;
+    ch = fabsf(j) < 0x1p64f ? __fadd_ru(c, err) : INFINITY;
+}
+
+__device__ __forceinline__ uint32_t octant(float jx, float jy, float jz) {
+    return (jx < 0.0f ? 1u : 0u) | (jy < 0.0f ? 2u : 0u) | (jz < 0.0f ? 4u : 0u);
+}
+
+__device__ __forceinline__ void set_box_terms(Ray& r, float ix, float iy, float iz) {
+    box_terms(r.ox, ix, r.jx, r.clx, r.chx);
+    box_terms(r.oy, iy, r.jy, r.cly, r.chy);
+    box_terms(r.oz, iz, r.jz, r.clz, r.chz);
+    r.bits = (r.bits & 63u) | octant(r.jx, r.jy, r.jz) << 6;
+}
+
+// object-space ray at instance entry: origin, box terms and the triangle test's shear; the world
+// direction in r stays untouched
 __device__ __forceinline__ void ray_pre(Ray& r, float ox, float oy, float oz, float dx, float dy, float dz) {
     r.ox = ox; r.oy = oy; r.oz = oz;
-    r.dx = dx; r.dy = dy; r.dz = dz;
-    r.ix = 1.0f / dx; r.iy = 1.0f / dy; r.iz = 1.0f / dz;
     float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
     int kz = 0;
     if (ay > ax) kz = 1;
@@ -48,30 +87,38 @@ __device__ __forceinline__ void ray_pre(Ray& r, float ox, float oy, float oz, fl
     int ky = kx + 1 == 3 ? 0 : kx + 1;
     float dkz = comp(dx, dy, dz, kz);
     if (dkz < 0.0f) { int t = kx; kx = ky; ky = t; }
-    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.bits = (uint32_t)kx | (uint32_t)ky << 2 | (uint32_t)kz << 4;
     r.Sx = comp(dx, dy, dz, kx) / dkz;
     r.Sy = comp(dx, dy, dz, ky) / dkz;
     r.Sz = 1.0f / dkz;
+    set_box_terms(r, 1.0f / dx, 1.0f / dy, 1.0f / dz);
 }
 
-// the world-space ray at the TLAS level needs origin, direction and inverse direction only (no
-// triangle is tested there)
+// the world-space ray at the TLAS level (no triangle is tested there)
 __device__ __forceinline__ void ray_pre_world(Ray& r, float ox, float oy, float oz, float dx, float dy, float dz) {
     r.ox = ox; r.oy = oy; r.oz = oz;
     r.dx = dx; r.dy = dy; r.dz = dz;
-    r.ix = 1.0f / dx; r.iy = 1.0f / dy; r.iz = 1.0f / dz;
+    r.bits = 0u;
+    set_box_terms(r, 1.0f / dx, 1.0f / dy, 1.0f / dz);
 }
 
 constexpr float kInflate = 1.0000004f;  // 1 + 2*gamma_3 (Ize 2013) rounded up
 
-// slab test of one box against [tmin, tbest]; returns entry distance or +inf
-__device__ __forceinline__ float slab(const Ray& r, float lx, float hx, float ly, float hy, float lz, float hz, float tmin, float tbest) {
-    float t0x = (lx - r.ox) * r.ix, t1x = (hx - r.ox) * r.ix;
-    float t0y = (ly - r.oy) * r.iy, t1y = (hy - r.oy) * r.iy;
-    float t0z = (lz - r.oz) * r.iz, t1z = (hz - r.oz) * r.iz;
-    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tbest));
+
+
+// entry and exit t of one box given its entry planes (n) and exit planes (f)
+__device__ __forceinline__ float box_test(const Ray& r, float nx, float ny, float nz, float fx, float fy, float fz, float tmin,
+                                          float tbest) {
+    const float tn = fmaxf(fmaxf(__fmaf_rd(nx, r.jx, r.clx), __fmaf_rd(ny, r.jy, r.cly)), fmaxf(__fmaf_rd(nz, r.jz, r.clz), tmin));
+    const float tf = fminf(fminf(__fmaf_ru(fx, r.jx, r.chx), __fmaf_ru(fy, r.jy, r.chy)), fminf(__fmaf_ru(fz, r.jz, r.chz), tbest));
     return tn <= tf * kInflate ? tn : INFINITY;
+}
+
+// a box given as lo xyz, hi xyz
+__device__ __forceinline__ float box_test6(const Ray& r, const float* lo, const float* hi, float tmin, float tbest) {
+    const uint32_t o = r.bits >> 6;
+    return box_test(r, (o & 1) ? hi[0] : lo[0], (o & 2) ? hi[1] : lo[1], (o & 4) ? hi[2] : lo[2],
+                    (o & 1) ? lo[0] : hi[0], (o & 2) ? lo[1] : hi[1], (o & 4) ? lo[2] : hi[2], tmin, tbest);
 }
 
 struct Hit {
@@ -89,13 +136,14 @@ __device__ __forceinline__ bool accept(float t, float tmin, uint32_t inst, uint3
 }
 
 __device__ __forceinline__ void tri_test(const Ray& r, float4 a, float4 b, float4 c, float tmin, uint32_t inst, Hit& h) {
+    const int kx = (int)(r.bits & 3u), ky = (int)((r.bits >> 2) & 3u), kz = (int)((r.bits >> 4) & 3u);
     float A0 = a.x - r.ox, A1 = a.y - r.oy, A2 = a.z - r.oz;
     float B0 = b.x - r.ox, B1 = b.y - r.oy, B2 = b.z - r.oz;
     float C0 = c.x - r.ox, C1 = c.y - r.oy, C2 = c.z - r.oz;
-    float Akz = comp(A0, A1, A2, r.kz), Bkz = comp(B0, B1, B2, r.kz), Ckz = comp(C0, C1, C2, r.kz);
-    float Ax = comp(A0, A1, A2, r.kx) - r.Sx * Akz, Ay = comp(A0, A1, A2, r.ky) - r.Sy * Akz;
-    float Bx = comp(B0, B1, B2, r.kx) - r.Sx * Bkz, By = comp(B0, B1, B2, r.ky) - r.Sy * Bkz;
-    float Cx = comp(C0, C1, C2, r.kx) - r.Sx * Ckz, Cy = comp(C0, C1, C2, r.ky) - r.Sy * Ckz;
+    float Akz = comp(A0, A1, A2, kz), Bkz = comp(B0, B1, B2, kz), Ckz = comp(C0, C1, C2, kz);
+    float Ax = comp(A0, A1, A2, kx) - r.Sx * Akz, Ay = comp(A0, A1, A2, ky) - r.Sy * Akz;
+    float Bx = comp(B0, B1, B2, kx) - r.Sx * Bkz, By = comp(B0, B1, B2, ky) - r.Sy * Bkz;
+    float Cx = comp(C0, C1, C2, kx) - r.Sx * Ckz, Cy = comp(C0, C1, C2, ky) - r.Sy * Ckz;
     float U = Cx * By - Cy * Bx;
     float V = Ax * Cy - Ay * Cx;
     float W = Bx * Ay - By * Ax;
@@ -134,9 +182,9 @@ constexpr int kTraceThreads = 128;
 
 // per-thread traversal stack in shared memory, laid out [depth][thread] so that the 32 lanes of a
 // warp touching the same depth hit 32 different banks.  THREADS = block size, DEPTH = entries.
-// Beside it, nine floats per thread keep the world-space ray's origin, direction and inverse
-// direction while the ray is inside a BLAS, so leaving the BLAS restores them instead of
-// recomputing them.
+// Beside it, six floats per thread keep the world-space ray's origin and clamped inverse direction
+// while the ray is inside a BLAS (the world direction itself stays in registers), so leaving the BLAS
+// restores them instead of dividing again.
 template <int THREADS, int DEPTH>
 struct SmemStackT {
     static constexpr int kDepth = DEPTH;
@@ -159,7 +207,7 @@ struct LocalStackT {
 };
 #define RG_DECLARE_SMEM_STACK(name, THREADS, DEPTH)      \
     __shared__ uint32_t name##_mem[DEPTH][THREADS];      \
-    __shared__ float name##_world[9][THREADS];           \
+    __shared__ float name##_world[6][THREADS];           \
     const SmemStackT<THREADS, DEPTH> name{&name##_mem[0][threadIdx.x], &name##_world[0][threadIdx.x]}
 #if RG_STACK_SMEM
 #define RG_DECLARE_STACK(name) RG_DECLARE_SMEM_STACK(name, kTraceThreads, kTraversalStack)
@@ -167,7 +215,7 @@ using TravStack = SmemStackT<kTraceThreads, kTraversalStack>;
 #else
 #define RG_DECLARE_STACK(name)                 \
     uint32_t name##_mem[kTraversalStack];      \
-    float name##_world[9];                     \
+    float name##_world[6];                     \
     const LocalStackT<kTraversalStack> name{name##_mem, name##_world}
 using TravStack = LocalStackT<kTraversalStack>;
 #endif
@@ -181,11 +229,11 @@ using TravStack = LocalStackT<kTraversalStack>;
 #define RG_POLL_ROUNDS 4
 #endif
 
-// Resumable traversal of one ray: trav_begin sets it up, each trav_step processes one node or one
-// leaf (a 4-wide record tests up to four grandchildren of a BVH2 node and descends into the nearest
-// hit; a TLAS leaf moves the ray into the instance's object space and descends into its BLAS
-// behind a marker entry; a BLAS leaf runs the triangle test).  The
-// kernel interleaves trav_step with shading so that a lane whose ray finished does not idle.
+// Resumable traversal of one ray: trav_begin sets it up, each trav_step processes one record or one
+// leaf (a record tests up to eight children and descends into the nearest hit; a TLAS leaf moves
+// the ray into the instance's object space and descends into its BLAS behind a marker entry; a BLAS
+// leaf runs the triangle test).  The kernel interleaves trav_step with shading so that a lane whose
+// ray finished does not idle.
 struct Trav {
     float tmin;
     Ray r;  // the ray of the current level (world or object space); its shear terms are used in BLASes only
@@ -207,8 +255,7 @@ __device__ __forceinline__ void trav_begin(Trav& T, const DevScene& sc, float ox
     if ((dx == 0.0f && dy == 0.0f && dz == 0.0f) || sc.tlasN == 0) return;
     T.tmin = tmin;
     ray_pre_world(T.r, ox, oy, oz, dx, dy, dz);
-    if (sc.tlasN > 1 && slab(T.r, sc.tlasRoot[0], sc.tlasRoot[3], sc.tlasRoot[1], sc.tlasRoot[4], sc.tlasRoot[2], sc.tlasRoot[5], tmin, T.h.t) == INFINITY)
-        return;
+    if (sc.tlasN > 1 && box_test6(T.r, sc.tlasRoot, sc.tlasRoot + 3, tmin, T.h.t) == INFINITY) return;
     T.sp = 0;
     T.nodes = sc.tlasWide;
     T.tris = nullptr;
@@ -225,15 +272,20 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
     if (!(ref & kLeaf)) {
         if (COUNT) vc.nodes++;
         const WideNode* nd = T.nodes + ref;
-        const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix), ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
-        const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+        // entry and exit plane vectors of the ray's octant (lox, hix, loy, hiy, loz, hiz in order)
+        const float4* pl = &nd->lox;
+        const uint32_t o = T.r.bits >> 6;
+        const uint32_t ox = o & 1u, oy = (o >> 1) & 1u, oz = (o >> 2) & 1u;
+        const float4 nx = __ldg(pl + ox), fx = __ldg(pl + (ox ^ 1u));
+        const float4 ny = __ldg(pl + 2 + oy), fy = __ldg(pl + 2 + (oy ^ 1u));
+        const float4 nz = __ldg(pl + 4 + oz), fz = __ldg(pl + 4 + (oz ^ 1u));
         const uint4 rf = __ldg(&nd->ref);
         float t[4];
         uint32_t r[4] = {rf.x, rf.y, rf.z, rf.w};
-        t[0] = slab(T.r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, tmin, T.h.t);
-        t[1] = slab(T.r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, tmin, T.h.t);
-        t[2] = r[2] != kEmptySlot ? slab(T.r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, tmin, T.h.t) : INFINITY;
-        t[3] = r[3] != kEmptySlot ? slab(T.r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, tmin, T.h.t) : INFINITY;
+        t[0] = box_test(T.r, nx.x, ny.x, nz.x, fx.x, fy.x, fz.x, tmin, T.h.t);
+        t[1] = box_test(T.r, nx.y, ny.y, nz.y, fx.y, fy.y, fz.y, tmin, T.h.t);
+        t[2] = r[2] != kEmptySlot ? box_test(T.r, nx.z, ny.z, nz.z, fx.z, fy.z, fz.z, tmin, T.h.t) : INFINITY;
+        t[3] = r[3] != kEmptySlot ? box_test(T.r, nx.w, ny.w, nz.w, fx.w, fy.w, fz.w, tmin, T.h.t) : INFINITY;
         // nearest first: 5 compare-exchanges sort the four (t, ref) pairs
 #define RG_CSWAP(a, b)                                           \
         if (t[b] < t[a]) {                                       \
@@ -271,13 +323,14 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
             float ez = (i2.x * dx + i2.y * dy) + i2.z * dz;
             if (!(ex == 0.0f && ey == 0.0f && ez == 0.0f)) {
                 Ray orr;
+                orr.dx = dx; orr.dy = dy; orr.dz = dz;  // the world direction stays in the ray
                 ray_pre(orr, qx, qy, qz, ex, ey, ez);
-                if (slab(orr, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, tmin, T.h.t) != INFINITY) {
+                const float blo[3] = {lo.x, lo.y, lo.z}, bhi[3] = {hi.x, hi.y, hi.z};
+                if (box_test6(orr, blo, bhi, tmin, T.h.t) != INFINITY) {
                     if (T.sp < STACK::kDepth) {
                         const ulonglong2 pp = __ldg(reinterpret_cast<const ulonglong2*>(&ir->wide));
                         stack.w(0) = ox; stack.w(1) = oy; stack.w(2) = oz;
-                        stack.w(3) = dx; stack.w(4) = dy; stack.w(5) = dz;
-                        stack.w(6) = T.r.ix; stack.w(7) = T.r.iy; stack.w(8) = T.r.iz;
+                        stack.w(3) = T.r.jx; stack.w(4) = T.r.jy; stack.w(5) = T.r.jz;
                         stack[T.sp++] = kMarker;
                         T.r = orr;
                         T.nodes = reinterpret_cast<const WideNode*>(pp.x);
@@ -306,9 +359,11 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
         T.inBlas = false;
         T.nodes = sc.tlasWide;
         T.r.ox = stack.w(0); T.r.oy = stack.w(1); T.r.oz = stack.w(2);
-        T.r.dx = stack.w(3); T.r.dy = stack.w(4); T.r.dz = stack.w(5);
-        T.r.ix = stack.w(6); T.r.iy = stack.w(7); T.r.iz = stack.w(8);
-    }
+        box_terms(T.r.ox, stack.w(3), T.r.jx, T.r.clx, T.r.chx);
+        box_terms(T.r.oy, stack.w(4), T.r.jy, T.r.cly, T.r.chy);
+        box_terms(T.r.oz, stack.w(5), T.r.jz, T.r.clz, T.r.chz);
+        T.r.bits = octant(T.r.jx, T.r.jy, T.r.jz) << 6;
+        }
 }
 
 template <bool COUNT, class STACK>

@@ -38,10 +38,15 @@ EXPORTS = [
     "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory", "rg_filter_create", "rg_filter_destroy",
     "rg_filter_last_error", "rg_filter_get_params", "rg_filter_set_params", "rg_filter_get_grads", "rg_filter_forward",
     "rg_filter_train_step", "rg_filter_input", "rg_filter_target", "rg_set_filter", "rg_set_glossy",
+    "rg_bvh_records",
 ]
 FILTER_PARAMS = 78243
 # layer shapes of the learned filter: (out, in) real channel counts
 FILTER_LAYERS = ((32, 12), (64, 32), (64, 64), (32, 64), (3, 32))
+
+# one 4-wide traversal record (rg_bvh_records): planes lo_x, hi_x, lo_y, hi_y, lo_z, hi_z of 4 slots
+WIDE_RECORD = np.dtype([("planes", "<f4", (6, 4)), ("ref", "<u4", 4)])
+assert WIDE_RECORD.itemsize == 112
 
 # rg_job (include/rgcuda.h): one render of a batch
 JOB = np.dtype([("scene", "<u4"), ("width", "<u4"), ("height", "<u4"), ("fxaa", "<i4"), ("ubo", scenes.UBO)])
@@ -115,6 +120,7 @@ def load(path: str = LIB_PATH):
         "rg_get_stream": ([P, ctypes.POINTER(P)], I32),
         "rg_bvh_info": ([P, U32, ctypes.POINTER(U32), P, P, P, P, P], I32),
         "rg_instance_inverse": ([P, P], I32),
+        "rg_bvh_records": ([P, U32, P, U32, ctypes.POINTER(U32)], I32),
         "rg_trace_rays": ([P, P, U32, P, P], I32),
         "rg_post_only": ([P, P, P, P, P, I32], I32),
         "rg_lbvh_build_host": ([P, P, U32, P, P, P, P, P], I32),
@@ -381,6 +387,16 @@ class Context:
                    nodeboxes=np.zeros((max(n - 1, 0), 6), np.float32))
         self._ck(self.L.rg_bvh_info(self.h, b, None, _p(out["morton"]), _p(out["order"]), _p(out["left"]),
                                     _p(out["right"]), _p(out["nodeboxes"])))
+        return out
+
+    def bvh_records(self, blas: int):
+        """The traversal's 4-wide records (WIDE_RECORD) of a BLAS, or of the TLAS for blas < 0."""
+        b = 0xFFFFFFFF if blas < 0 else blas
+        n = ctypes.c_uint32()
+        self._ck(self.L.rg_bvh_records(self.h, b, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, WIDE_RECORD)
+        if n.value:
+            self._ck(self.L.rg_bvh_records(self.h, b, _p(out), n.value, ctypes.byref(n)))
         return out
 
     def instance_inverse(self, n):

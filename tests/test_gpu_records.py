@@ -1,0 +1,130 @@
+"""The traversal's 4-wide records (raygun_gb300/csrc/lbvh.cu k_wide_records) and its box tests.
+
+Records are not compared with the oracle (its traversal walks the BVH2 itself); they are checked for
+what the traversal relies on:
+* structure: the record of BVH2 node i holds i's grandchildren (a leaf child stands in for its own
+  slot), empty slots carry ref 0xFFFFFFFE and an inverted box;
+* boxes: every slot's box is exactly its child's box (BLAS leaves: the triangle's box; internal
+  children: the LBVH node box), for BLASes and the TLAS, also after BLAS refits.
+The box tests accept at least what the exact test accepts, so hits equal the brute-force answer: rays
+with zero, tiny and huge direction components (the clamped terms of the test), rays along the ground
+plane and rays from vertices along an axis (origins on box planes) hit exactly what the oracle hits.
+"""
+import numpy as np
+import pytest
+
+from raygun_gb300 import scenes as S
+
+from test_oracle import camera_rays, degenerate_rays, random_rays
+
+pytestmark = pytest.mark.gpu
+
+LEAF = 0x80000000
+EMPTY = 0xFFFFFFFE
+
+
+def small_two_level():
+    return S.instanced_scene(width=96, height=54, counts=(6, 5, 3, 1, 4, 4, 1, 1), hf_n=32, ico_levels=(1, 2, 3, 3),
+                             num_samples=2, max_recursions=5, name="mini-c1")
+
+
+@pytest.fixture(scope="module", params=["c0", "c1"])
+def scene_pair(request, rg, orc):
+    sc = S.c0_scene() if request.param == "c0" else small_two_level()
+    rt = rg.Raytracer(sc).prepare()
+    yield sc, rt, orc.OracleScene(sc)
+    rt.ctx.close()
+
+
+def tri_boxes(sc, b):
+    m = sc.meshes[b]
+    vo, io, nt = int(m["vertexOffset"]), int(m["indexOffset"]), int(m["triCount"])
+    idx = sc.indices[io:io + 3 * nt].astype(np.int64).reshape(-1, 3) + vo
+    p = sc.vertices["position"][idx]  # (nt, 3, 3) float32
+    return np.concatenate([p.min(1), p.max(1)], 1)
+
+
+def check_records(rec, bvh, leaf_boxes):
+    """leaf_boxes: sorted position -> box (n x 6), or None (TLAS: instance boxes are not checked)."""
+    left, right = bvh["left"].astype(np.int64), bvh["right"].astype(np.int64)
+    m = len(left)
+    assert len(rec) == m
+    if m == 0:
+        return 0
+    # expected refs: grandchildren, leaves standing in for themselves
+    exp = np.full((m, 4), EMPTY, np.int64)
+    for i in range(m):
+        k = 0
+        for c in (left[i], right[i]):
+            if c & LEAF:
+                exp[i, k] = c
+                k += 1
+            else:
+                exp[i, k], exp[i, k + 1] = left[c], right[c]
+                k += 2
+    got = rec["ref"].astype(np.int64)
+    assert np.array_equal(got, exp)
+    planes = rec["planes"]  # (m, 6, 4): lo_x, hi_x, lo_y, hi_y, lo_z, hi_z
+    lo = planes[:, 0::2, :].transpose(0, 2, 1)  # (m, 4, 3)
+    hi = planes[:, 1::2, :].transpose(0, 2, 1)
+    empty = got == EMPTY
+    assert (lo[empty] == np.inf).all() and (hi[empty] == -np.inf).all()
+    internal = ~empty & ((got & LEAF) == 0)
+    nb = bvh["nodeboxes"]
+    assert np.array_equal(lo[internal], nb[got[internal], :3]) and np.array_equal(hi[internal], nb[got[internal], 3:])
+    checked = int(internal.sum())
+    if leaf_boxes is not None:
+        leaf = ~empty & ((got & LEAF) != 0)
+        lb = leaf_boxes[got[leaf] & ~LEAF]
+        assert np.array_equal(lo[leaf], lb[:, :3]) and np.array_equal(hi[leaf], lb[:, 3:])
+        checked += int(leaf.sum())
+    return checked
+
+
+def test_blas_records(rg, scene_pair):
+    sc, rt, o = scene_pair
+    checked = 0
+    for b in range(len(sc.meshes)):
+        bvh = rt.ctx.bvh(b)
+        checked += check_records(rt.ctx.bvh_records(b), bvh, tri_boxes(sc, b)[bvh["order"]])
+    assert checked > 1000
+
+
+def test_tlas_records(rg, scene_pair):
+    sc, rt, o = scene_pair
+    check_records(rt.ctx.bvh_records(-1), rt.ctx.bvh(-1), None)
+
+
+def test_closest_hit_degenerate_directions(rg, scene_pair):
+    sc, rt, o = scene_pair
+    rays = np.concatenate([degenerate_rays(sc, 12000, 7), camera_rays(sc, stride=4)])
+    tg, ig = rt.ctx.trace_rays(rays)
+    to, io = o.trace(rays)
+    assert np.array_equal(ig, io)
+    assert np.array_equal(tg, to)
+    assert (ig[:12000, 0] != 0xFFFFFFFF).sum() > 100
+
+
+def test_records_follow_refit(rg, orc):
+    """After BLAS refits and a TLAS rebuild the records carry the moved boxes, and hits still match
+    the oracle."""
+    sc = small_two_level()
+    rt = rg.Raytracer(sc).prepare()
+    o = orc.OracleScene(sc)
+    anim = S.FrameAnimator(sc, seed=11, refit_prob=1.0)
+    refits = anim.step()
+    assert refits
+    for b, vo, nv in refits:
+        rt.ctx.update_vertices(vo, sc.vertices[vo:vo + nv])
+        rt.ctx.refit_blas(rt.blas_ids[b])
+        o.refit(b, sc.vertices[vo:vo + nv], vo)
+    rt.setup_top_level_as()
+    o.set_instances(sc.instances)
+    for b, _, _ in refits:
+        bvh = rt.ctx.bvh(b)
+        check_records(rt.ctx.bvh_records(b), bvh, tri_boxes(sc, b)[bvh["order"]])
+    rays = np.concatenate([camera_rays(sc), random_rays(5000, 8, lo=(-60, 0, -60), hi=(60, 14, 60))])
+    tg, ig = rt.ctx.trace_rays(rays)
+    to, io = o.trace(rays)
+    assert np.array_equal(ig, io) and np.array_equal(tg, to)
+    rt.ctx.close()

@@ -101,6 +101,38 @@ def random_rays(n, seed, lo=(-12, 0.2, -12), hi=(12, 8, 12)):
     return rays
 
 
+def degenerate_rays(sc, n, seed):
+    """Rays with zero, tiny (1e-30) and huge components, rays in the ground plane, rays from box planes."""
+    rng = np.random.RandomState(seed)
+    V = sc.vertices["position"]
+    lo, hi = V.min(0), V.max(0)
+    o = rng.uniform(lo - 2, hi + 2, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    kind = rng.randint(0, 6, n)
+    for i in range(n):
+        axes = rng.permutation(3)
+        if kind[i] == 0:  # axis-parallel
+            d[i, axes[1:]] = 0.0
+        elif kind[i] == 1:  # in a coordinate plane
+            d[i, axes[0]] = 0.0
+        elif kind[i] == 2:  # tiny components
+            d[i, axes[0]] = np.float32(1e-30) * np.sign(d[i, axes[0]] + 0.5)
+            d[i, axes[1]] = np.float32(-3e-25)
+        elif kind[i] == 3:  # huge direction (tiny 1/d)
+            d[i] *= np.float32(1e25)
+        elif kind[i] == 4:  # horizontal, starting on y = 0 (the ground plane of the scenes)
+            o[i, 1] = 0.0
+            d[i, 1] = 0.0
+        else:  # from a vertex, along an axis
+            o[i] = V[rng.randint(len(V))]
+            d[i] = 0.0
+            d[i, axes[0]] = 1.0 if rng.rand() < 0.5 else -1.0
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3], rays[:, 3], rays[:, 4:7], rays[:, 7] = o, 0.0, d, 1e4
+    rays[kind == 3, 7] = 1e-20  # t is scaled by |d|
+    return rays
+
+
 def test_traversal_matches_brute_force(orc):
     sc = S.spheres_scene(n_spheres=12, width=64, height=36, slices=16, stacks=8)
     o = orc.OracleScene(sc)
@@ -120,6 +152,22 @@ def test_traversal_two_level_matches_brute_force(orc):
     f2, i2 = o.trace(rays, brute=True)
     assert np.array_equal(i1, i2) and np.array_equal(f1, f2)
     assert (i1[:, 0] != 0xFFFFFFFF).sum() > 50
+
+
+@pytest.mark.parametrize("which", ["spheres", "two-level"])
+def test_traversal_degenerate_directions_match_brute_force(orc, which):
+    """Zero, tiny and huge direction components, rays in the ground plane and rays from vertices along
+    an axis (origins on box planes): the BVH walk finds what the brute force finds."""
+    if which == "spheres":
+        sc = S.spheres_scene(n_spheres=12, width=64, height=36, slices=16, stacks=8)
+    else:
+        sc = S.instanced_scene(width=64, height=36, counts=(6, 5, 3, 0, 4, 4, 1, 1), hf_n=24, ico_levels=(1, 2, 2, 3))
+    o = orc.OracleScene(sc)
+    rays = degenerate_rays(sc, 3000, 5)
+    f1, i1 = o.trace(rays)
+    f2, i2 = o.trace(rays, brute=True)
+    assert np.array_equal(i1, i2) and np.array_equal(f1, f2)
+    assert (i1[:, 0] != 0xFFFFFFFF).sum() > 100
 
 
 def test_half_rounding(orc):
