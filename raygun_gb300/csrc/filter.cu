@@ -105,6 +105,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+// 16 consecutive FP32 columns of this thread's TMEM lane, without waiting (tmem_wait_ld before use)
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+          "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ uint4 add_bf16x8(uint4 a, uint4 b) {
     const bf16* x = reinterpret_cast<const bf16*>(&a);
     const bf16* y = reinterpret_cast<const bf16*>(&b);
@@ -141,170 +151,342 @@ __device__ __forceinline__ void load_patch(uint8_t* patch, const bf16* __restric
 
 namespace {
 
+// Row-streaming convolution.  A work item is a strip of 128 output pixels x a segment of rows of
+// one image; a CTA walks its items down the rows, three output rows (a group) at a time.  Input rows
+// (130 pixels: the strip and a 1-pixel halo, zero outside the image) stream through a ring of
+// shared-memory slots, each row loaded once per item as channel-chunk planes [chunk][pixel][8].  Input
+// row i feeds output rows i+1, i, i-1 through the kernel rows dy = 0, 1, 2, so a group's accumulator is
+// a window of three adjacent TMEM blocks and each of its five input rows r-1 .. r+3 feeds it with ONE
+// tcgen05.mma per column tap dx and 16-channel step (M = 128 pixels, N = COUT, 2 COUT, 3 COUT, 2 COUT,
+// COUT), the B operand stacking the kernel rows' weights.  62 MMAs instead of 108 per 3 rows of a
+// 64-channel layer, each issued from fully unrolled code with constant offsets: one issuing thread
+// must keep the tensor core fed, so the issue path carries no arithmetic beyond descriptor adds.
+// Warp roles (320 threads):
+//   warp 0     TMA producer: refills a slot once the MMAs of the last group reading its row completed;
+//   warp 1     MMA issuer: group by group into alternating accumulator windows;
+//   warps 2-9  epilogue, two warps per TMEM lane quarter (half the channels each): drain a completed
+//              window (bias, ReLU, skip add, mask) and hand it back; BF16 rows leave through a small
+//              swizzled shared-memory stage so that each store instruction writes whole sectors.
+constexpr int kStripPx = 128, kRowW = kStripPx + 2;
+constexpr int kRowPlane = 2176;  // 130 pixels x 16 B rounded up to 128 B (TMA destination alignment)
+constexpr int kEpiWarps = 8;
+constexpr int kConvThreads = 32 * (2 + kEpiWarps);
+constexpr int kGroupRows = 3;
+
 template <int CIN, int COUT>
 struct ConvShape {
-    static constexpr int kWeightBytes = 9 * CIN * COUT * 2;
-    static constexpr int kPatchBytes = (CIN / 8) * kPatchPlane;
-    static constexpr int kSmem = kWeightBytes + 2 * kPatchBytes + 1024;  // weights + two patch buffers + alignment
-    static constexpr uint32_t kCols = kTileRows * COUT < 32 ? 32 : kTileRows * COUT;
-    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "shape");
-    static_assert((kCols & (kCols - 1)) == 0, "TMEM columns must be a power of two");
-    static_assert(kWeightBytes % 1024 == 0 || kWeightBytes % 128 == 0, "patch buffers 128-byte aligned");
+    static constexpr int CC = CIN / 8;
+    static constexpr int kRing = 8;                               // input row slots
+    static constexpr int kWin = 3 * COUT;                         // TMEM columns of one group's window
+    static constexpr int kWindows = 3 * COUT * 4 <= 512 ? 4 : 2;  // accumulator windows (groups in flight)
+    static constexpr int kRowBytes = CC * kRowPlane;              // one slot
+    static constexpr uint32_t kRowTx = CC * kRowW * 16;           // bytes the TMA writes per row
+    static constexpr int kWeightBytes = 9 * CIN * COUT * 2;       // [dx][ci/8][kernel row 2, 1, 0][co][8]
+    static constexpr int kStageBytes = 32 * COUT;                 // per epilogue warp: 32 pixels x COUT/2 channels (BF16)
+    static constexpr int kSmem = kWeightBytes + kRing * kRowBytes + kEpiWarps * kStageBytes + 1024;
+    static constexpr uint32_t kCols = kWindows * kWin <= 32 ? 32 : (kWindows * kWin <= 64 ? 64 : (kWindows * kWin <= 128 ? 128 : (kWindows * kWin <= 256 ? 256 : 512)));
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && kWin <= 256 && kWindows * kWin <= 512, "shape");
+    static_assert(kWeightBytes % 128 == 0, "ring slots 128-byte aligned");
 };
 
-// Persistent CTA over tiles blockIdx.x, + gridDim.x, ...  One thread issues the TMA loads (one box of
-// 8 channels x 130 pixels x 4 rows per channel chunk, zero-filled outside the image) for tile i + 1
-// into the other patch buffer while tile i's MMAs and epilogue run.
+// bounded wait that also gives up when another role has given up (abort flag in shared memory)
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* mbar, uint32_t phase, volatile int* abort, int* status) {
+    for (int spin = 0; spin < (1 << 22); ++spin) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(smem_u32(mbar)), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if ((spin & 255) == 255 && *abort) return false;
+    }
+    *abort = 1;
+    if (status) atomicExch(status, 1);
+    return false;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+// 8 consecutive FP32 columns of this thread's TMEM lane, without waiting (tmem_wait_ld before use)
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
+// A warp's 32 pixels x NC 16-byte chunks in shared memory, chunk c of pixel p at slot c ^ f(p) so that
+// both the per-pixel writes and the row-order reads below touch 8 distinct bank groups per phase.
+template <int NC>
+__device__ __forceinline__ uint32_t stage_off(int p, int c) {
+    const int f = NC == 1 ? 0 : (p / (8 / NC)) % NC;
+    return (uint32_t)(p * NC * 16 + ((c ^ f) * 16));
+}
+// copies the staged 32 x NC chunks to dst (pixel p at dst + p * pixStride bytes), pixels < valid only
+template <int NC>
+__device__ __forceinline__ void stage_out(const uint8_t* stage, uint8_t* dst, size_t pixStride, int valid, int lane) {
+#pragma unroll
+    for (int it = 0; it < NC; ++it) {
+        const int k = it * 32 + lane, p = k / NC, c = k % NC;
+        const uint4 v = *reinterpret_cast<const uint4*>(stage + stage_off<NC>(p, c));
+        if (p < valid) *reinterpret_cast<uint4*>(dst + (size_t)p * pixStride + c * 16) = v;
+    }
+}
+
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) k_filter_conv(const __grid_constant__ CUtensorMap tmapX, const FilterConvArgs a) {
+__global__ void __launch_bounds__(kConvThreads, 1) k_filter_conv(const __grid_constant__ CUtensorMap tmapX, const FilterConvArgs a,
+                                                                 int segRows) {
     using S = ConvShape<CIN, COUT>;
     using bf16 = __nv_bfloat16;
-    constexpr int CC = CIN / 8;
+    constexpr int CC = S::CC, NW = S::kWindows, KK = CIN / 16;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* wsm = smem;
-    uint8_t* patch[2] = {smem + S::kWeightBytes, smem + S::kWeightBytes + S::kPatchBytes};
+    uint8_t* ring = smem + S::kWeightBytes;
     __shared__ uint32_t tmem_base;
-    __shared__ __align__(8) uint64_t mbarMma;
-    __shared__ __align__(8) uint64_t mbarLoad[2];
+    __shared__ __align__(8) uint64_t full[S::kRing], empty[S::kRing], accFull[NW], accEmpty[NW], drain;
+    __shared__ int abortFlag, issuedRows, consumedRows;
+    __shared__ float biasSm[COUT];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int i = tid; i < S::kWeightBytes / 16; i += blockDim.x)
-        reinterpret_cast<uint4*>(wsm)[i] = reinterpret_cast<const uint4*>(a.w)[i];
+    // weights: packed [tap = dy * 3 + dx][ci/8][co][8] -> [dx][ci/8][kernel row 2, 1, 0][co][8]
+    for (int i = tid; i < S::kWeightBytes / 16; i += blockDim.x) {
+        const int co = i % COUT, dyr = (i / COUT) % 3, cc = (i / (3 * COUT)) % CC, dx = i / (3 * COUT * CC);
+        const int tap = (2 - dyr) * 3 + dx;
+        reinterpret_cast<uint4*>(wsm)[i] = reinterpret_cast<const uint4*>(a.w)[((size_t)tap * CC + cc) * COUT + co];
+    }
+    for (int i = tid; i < COUT; i += blockDim.x) biasSm[i] = a.bias ? a.bias[i] : 0.0f;
     if (tid == 0) {
-        mbar_init(&mbarMma, 1);
-        mbar_init(&mbarLoad[0], 1);
-        mbar_init(&mbarLoad[1], 1);
+        for (int k = 0; k < S::kRing; ++k) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], 1);
+        }
+        for (int k = 0; k < NW; ++k) {
+            mbar_init(&accFull[k], 1);
+            mbar_init(&accEmpty[k], kEpiWarps);
+        }
+        mbar_init(&drain, 1);
+        abortFlag = 0;
+        issuedRows = consumedRows = 0;
         mbar_init_fence();
     }
-    async_proxy_fence();  // the weight tile is read by the tensor core
-    if (warp == 0) tmem_alloc(&tmem_base, S::kCols);
+    async_proxy_fence();  // the weights are read by the tensor core
+    if (warp == 1) tmem_alloc(&tmem_base, S::kCols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
-    const int tilesX = (a.W + kTilePx - 1) / kTilePx, tilesY = (a.H + kTileRows - 1) / kTileRows;
-    const int tiles = a.B * tilesY * tilesX;
-    const int mine = blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    auto issue_load = [&](int i) {  // tile i of this CTA into patch[i & 1]
-        const int t = blockIdx.x + i * gridDim.x;
-        const int b = t / (tilesY * tilesX), rem = t % (tilesY * tilesX);
-        const int y0 = (rem / tilesX) * kTileRows, x0 = (rem % tilesX) * kTilePx;
-        uint64_t* mb = &mbarLoad[i & 1];
-        mbar_expect_tx(mb, (uint32_t)S::kPatchBytes);
-#pragma unroll 1
-        for (int cc = 0; cc < CC; ++cc) tma_load_4d(patch[i & 1] + cc * kPatchPlane, &tmapX, cc * 8, x0 - 1, y0 - 1, b, mb);
+    volatile int* abort = &abortFlag;
+    // segRows is a multiple of 3; a segment's last group may run past the image (zero input rows,
+    // results not stored)
+    const int strips = (a.W + kStripPx - 1) / kStripPx, segs = (a.H + segRows - 1) / segRows;
+    const int items = a.B * strips * segs;
+    auto item_of = [&](int item, int& b, int& x0, int& ys, int& ng) {
+        b = item / (strips * segs);
+        const int rem = item % (strips * segs);
+        x0 = (rem / segs) * kStripPx;
+        ys = (rem % segs) * segRows;
+        ng = (min(ys + segRows, a.H) - ys + kGroupRows - 1) / kGroupRows;
     };
-    int issued = 0, consumed = 0, mmas = 0;  // loads issued (thread 0), loads waited for, MMA batches waited for
-    if (tid == 0 && mine > 0) {
-        issue_load(0);
-        issued = 1;
-    }
-    constexpr uint32_t idesc = umma_idesc(128, COUT, false, false);
-    bool ok = true;
-    for (int i = 0; i < mine && ok; ++i) {
-        const int t = blockIdx.x + i * gridDim.x;
-        const int b = t / (tilesY * tilesX), rem = t % (tilesY * tilesX);
-        const int y0 = (rem / tilesX) * kTileRows, x0 = (rem % tilesX) * kTilePx;
-        if (tid == 0 && i + 1 < mine) {  // the other buffer's MMAs completed in iteration i - 1
-            issue_load(i + 1);
-            issued = i + 2;
+    if (warp == 0) {
+        if (lane == 0) {  // producer: input rows ys - 1 .. ys + 3 ng of each item
+            int seq = 0;
+            bool ok = true;
+            for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+                int b, x0, ys, ng;
+                item_of(item, b, x0, ys, ng);
+                for (int k = 0; k < kGroupRows * ng + 2 && ok; ++k, ++seq) {
+                    const int slot = seq % S::kRing, fill = seq / S::kRing;
+                    if (fill > 0 && !mbar_wait_or_abort(&empty[slot], (uint32_t)((fill - 1) & 1), abort, a.status)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(&full[slot], S::kRowTx);
+#pragma unroll 1
+                    for (int cc = 0; cc < CC; ++cc)
+                        tma_load_4d(ring + slot * S::kRowBytes + cc * kRowPlane, &tmapX, cc * 8, x0 - 1, ys - 1 + k, b, &full[slot]);
+                    issuedRows = seq + 1;
+                }
+            }
         }
-        const bool loaded = mbar_wait(&mbarLoad[i & 1], (uint32_t)((i >> 1) & 1), a.status);
-        if (loaded) consumed = i + 1;
-        if (tid == 0 && loaded) {
-            tc_fence_after();
-            const uint32_t pbase = smem_u32(patch[i & 1]), wbase = smem_u32(wsm);
-#pragma unroll 1
-            for (int r = 0; r < kTileRows; ++r)
-#pragma unroll 1
-                for (int tap = 0; tap < 9; ++tap) {
-                    const int dy = tap / 3, dx = tap % 3;
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            // descriptors: the start address sits in the low 14 bits (address / 16) and every operand
+            // lies below 256 KB, so offsets add to it without a carry
+            const uint64_t adesc0 = umma_desc(smem_u32(ring), kRowPlane, 128), bdesc0 = umma_desc(smem_u32(wsm), 3 * COUT * 16, 128);
+            constexpr uint32_t id1 = umma_idesc(128, COUT, false, false), id2 = umma_idesc(128, 2 * COUT, false, false),
+                               id3 = umma_idesc(128, 3 * COUT, false, false);
+            int base = 0, waited = 0, g = 0;  // first input row of the item, input rows waited for, groups issued
+            bool ok = true;
+            for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+                int b, x0, ys, ng;
+                item_of(item, b, x0, ys, ng);
+                for (int j = 0; j < ng && ok; ++j, ++g) {
+                    const int w = g % NW;
+                    if (g >= NW && !mbar_wait_or_abort(&accEmpty[w], (uint32_t)((g / NW - 1) & 1), abort, a.status)) {
+                        ok = false;
+                        break;
+                    }
+                    const int first = base + kGroupRows * j;  // input row r - 1 of this group
+                    for (; waited < first + 5; ++waited)
+                        if (!mbar_wait_or_abort(&full[waited % S::kRing], (uint32_t)((waited / S::kRing) & 1), abort, a.status)) {
+                            ok = false;
+                            break;
+                        }
+                    if (!ok) break;
+                    consumedRows = waited;
+                    tc_fence_after();
+                    uint64_t arow[5];
 #pragma unroll
-                    for (int kk = 0; kk < CIN / 16; ++kk) {
-                        const uint64_t ad = umma_desc(pbase + (uint32_t)(2 * kk * kPatchPlane + ((r + dy) * kPatchW + dx) * 16),
-                                                      kPatchPlane, 128);
-                        const uint64_t bd = umma_desc(wbase + (uint32_t)((tap * CC + 2 * kk) * COUT * 16), COUT * 16, 128);
-                        umma(tmem + (uint32_t)(r * COUT), ad, bd, idesc, (tap | kk) ? 1u : 0u);
+                    for (int p = 0; p < 5; ++p) arow[p] = adesc0 + (uint64_t)((((first + p) % S::kRing) * S::kRowBytes) >> 4);
+                    const uint32_t d0 = tmem + (uint32_t)(w * S::kWin);
+#pragma unroll
+                    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+                        for (int kk = 0; kk < KK; ++kk) {
+                            const uint64_t aoff = (uint64_t)((2 * kk * kRowPlane + dx * 16) >> 4);
+                            const uint64_t bk = bdesc0 + (uint64_t)((dx * CC + 2 * kk) * 3 * COUT);
+                            const bool f = dx == 0 && kk == 0;  // the step where rows r+1 and r+2 start
+                            // input r - 1: row r (kernel row 0)
+                            umma(d0, arow[0] + aoff, bk + 2 * COUT, id1, f ? 0u : 1u);
+                            // input r: rows r, r + 1 (kernel rows 1, 0)
+                            if (f) {
+                                umma(d0, arow[1] + aoff, bk + COUT, id1, 1u);
+                                umma(d0 + COUT, arow[1] + aoff, bk + 2 * COUT, id1, 0u);
+                            } else {
+                                umma(d0, arow[1] + aoff, bk + COUT, id2, 1u);
+                            }
+                            // input r + 1: rows r .. r + 2 (kernel rows 2, 1, 0)
+                            if (f) {
+                                umma(d0, arow[2] + aoff, bk, id2, 1u);
+                                umma(d0 + 2 * COUT, arow[2] + aoff, bk + 2 * COUT, id1, 0u);
+                            } else {
+                                umma(d0, arow[2] + aoff, bk, id3, 1u);
+                            }
+                            // input r + 2: rows r + 1, r + 2 (kernel rows 2, 1); input r + 3: row r + 2
+                            umma(d0 + COUT, arow[3] + aoff, bk, id2, 1u);
+                            umma(d0 + 2 * COUT, arow[4] + aoff, bk, id1, 1u);
+                        }
+                    umma_commit(&accFull[w]);
+                    // input rows no later group of the item reads
+                    umma_commit(&empty[first % S::kRing]);
+                    umma_commit(&empty[(first + 1) % S::kRing]);
+                    umma_commit(&empty[(first + 2) % S::kRing]);
+                    if (j == ng - 1) {
+                        umma_commit(&empty[(first + 3) % S::kRing]);
+                        umma_commit(&empty[(first + 4) % S::kRing]);
                     }
                 }
-            umma_commit(&mbarMma);
+                base += kGroupRows * ng + 2;
+            }
+            umma_commit(&drain);  // completes when every MMA issued above has
+            mbar_wait(&drain, 0u, nullptr);
         }
-        const bool computed = loaded && mbar_wait(&mbarMma, (uint32_t)(i & 1), a.status);
-        if (computed) mmas = i + 1;
-        ok = __syncthreads_and(computed) != 0;
-        tc_fence_after();
-        if (ok) {
-#pragma unroll 1
-            for (int r = 0; r < kTileRows; ++r) {
-                const int y = y0 + r, xx = x0 + warp * 32 + lane;
-                const bool in = y < a.H && xx < a.W;
-                const size_t px = in ? ((size_t)b * a.H + y) * a.W + xx : 0;
-#pragma unroll 1
-                for (int c0 = 0; c0 < COUT; c0 += 16) {
-                    float v[16];
-                    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(r * COUT + c0), v);
-                    if (!in) continue;
+    } else {  // epilogue: TMEM lane quarter warp % 4 = pixels 32 (warp % 4) .. + 31; channel half h
+        constexpr int CH = COUT / 2, NC = CH / 8;
+        const int q = warp & 3, h = (warp - 2) >> 2, cbase = h * CH;
+        uint8_t* stage = ring + S::kRing * S::kRowBytes + (warp - 2) * S::kStageBytes;
+        int g = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+            int b, x0, ys, ng;
+            item_of(item, b, x0, ys, ng);
+            const int ye = min(ys + segRows, a.H);
+            const int xx = x0 + q * 32 + lane;
+            for (int j = 0; j < ng; ++j, ++g) {
+                const int w = g % NW;
+                // narrow layers fetch the skip input of the group's rows before waiting for the
+                // accumulators (registers allow it); 64-channel layers and masks load in place
+                constexpr bool kPre = NC <= 2;
+                constexpr int PR = kPre ? kGroupRows : 1;
+                uint4 addPre[PR][NC];
+                auto aux_load = [&](const bf16* src, int y, int c) {
+                    return src && y < ye && xx < a.W ? reinterpret_cast<const uint4*>(src + (((size_t)b * a.H + y) * a.W + xx) * COUT + cbase)[c]
+                                                     : make_uint4(0u, 0u, 0u, 0u);
+                };
+                if (kPre) {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        if (a.bias) v[j] += a.bias[c0 + j];
-                        if (a.relu) v[j] = fmaxf(v[j], 0.0f);
-                    }
-                    __align__(16) bf16 o[16];
-                    if (a.y) {
+                    for (int r = 0; r < PR; ++r)
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) o[j] = __float2bfloat16(v[j]);
-                        uint4* dst = reinterpret_cast<uint4*>(a.y + px * COUT + c0);
-                        dst[0] = reinterpret_cast<uint4*>(o)[0];
-                        dst[1] = reinterpret_cast<uint4*>(o)[1];
+                        for (int c = 0; c < NC; ++c) addPre[r][c] = aux_load(a.add, ys + kGroupRows * j + r, c);
+                }
+                if (!mbar_wait_or_abort(&accFull[w], (uint32_t)((g / NW) & 1), abort, a.status)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                uint32_t raw[kGroupRows][CH];
+#pragma unroll
+                for (int r = 0; r < kGroupRows; ++r)
+#pragma unroll
+                    for (int c = 0; c < CH; c += 8)
+                        tmem_ld8_nowait(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(w * S::kWin + r * COUT + cbase + c), raw[r] + c);
+                tmem_wait_ld();
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&accEmpty[w]);  // the window goes back before the math and stores
+#pragma unroll
+                for (int r = 0; r < kGroupRows; ++r) {
+                    const int y = ys + kGroupRows * j + r;
+                    if (y >= ye) continue;  // uniform across the warp
+                    const size_t px0 = ((size_t)b * a.H + y) * a.W + x0 + q * 32;  // pixel of lane 0
+                    const size_t px = px0 + lane;
+                    const bool in = xx < a.W;
+                    const int valid = min(32, a.W - (x0 + q * 32));
+                    float v[CH];
+#pragma unroll
+                    for (int e = 0; e < CH; ++e) {
+                        v[e] = __uint_as_float(raw[r][e]) + biasSm[cbase + e];
+                        if (a.relu) v[e] = fmaxf(v[e], 0.0f);
                     }
+                    auto put = [&](bf16* out, const float* vals, const uint4* mask) {  // BF16 row out through the stage
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) {
+                            __align__(16) bf16 o[8];
+                            if (mask) {
+                                const bf16* mv = reinterpret_cast<const bf16*>(&mask[c]);
+#pragma unroll
+                                for (int e = 0; e < 8; ++e) o[e] = __float2bfloat16(__bfloat162float(mv[e]) > 0.0f ? vals[8 * c + e] : 0.0f);
+                            } else {
+#pragma unroll
+                                for (int e = 0; e < 8; ++e) o[e] = __float2bfloat16(vals[8 * c + e]);
+                            }
+                            *reinterpret_cast<uint4*>(stage + stage_off<NC>(lane, c)) = *reinterpret_cast<uint4*>(o);
+                        }
+                        __syncwarp();
+                        stage_out<NC>(stage, reinterpret_cast<uint8_t*>(out + px0 * COUT + cbase), (size_t)COUT * 2, valid, lane);
+                        __syncwarp();
+                    };
+                    if (a.y) put(a.y, v, nullptr);
                     if (a.add) {
-                        const uint4* ad = reinterpret_cast<const uint4*>(a.add + px * COUT + c0);
-                        const uint4 u0 = ad[0], u1 = ad[1];
-                        const bf16* h0 = reinterpret_cast<const bf16*>(&u0);
-                        const bf16* h1 = reinterpret_cast<const bf16*>(&u1);
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            v[j] += __bfloat162float(h0[j]);
-                            v[8 + j] += __bfloat162float(h1[j]);
+                        for (int c = 0; c < NC; ++c) {
+                            const uint4 av = kPre ? addPre[kPre ? r : 0][c] : aux_load(a.add, y, c);
+                            const bf16* hv = reinterpret_cast<const bf16*>(&av);
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) v[8 * c + e] += __bfloat162float(hv[e]);
                         }
                     }
-                    if (a.ya) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) o[j] = __float2bfloat16(v[j]);
-                        uint4* dst = reinterpret_cast<uint4*>(a.ya + px * COUT + c0);
-                        dst[0] = reinterpret_cast<uint4*>(o)[0];
-                        dst[1] = reinterpret_cast<uint4*>(o)[1];
-                    }
-                    if (a.yf && c0 == 0) reinterpret_cast<float4*>(a.yf)[px] = make_float4(v[0], v[1], v[2], v[3]);
+                    if (a.ya) put(a.ya, v, nullptr);
+                    if (a.yf && cbase == 0 && in) reinterpret_cast<float4*>(a.yf)[px] = make_float4(v[0], v[1], v[2], v[3]);
                     if (a.ym) {
-                        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + px * COUT + c0);
-                        const uint4 u0 = mp[0], u1 = mp[1];
-                        const bf16* m0 = reinterpret_cast<const bf16*>(&u0);
-                        const bf16* m1 = reinterpret_cast<const bf16*>(&u1);
+                        uint4 mk[NC];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            o[j] = __float2bfloat16(__bfloat162float(m0[j]) > 0.0f ? v[j] : 0.0f);
-                            o[8 + j] = __float2bfloat16(__bfloat162float(m1[j]) > 0.0f ? v[8 + j] : 0.0f);
-                        }
-                        uint4* dst = reinterpret_cast<uint4*>(a.ym + px * COUT + c0);
-                        dst[0] = reinterpret_cast<uint4*>(o)[0];
-                        dst[1] = reinterpret_cast<uint4*>(o)[1];
+                        for (int c = 0; c < NC; ++c) mk[c] = aux_load(a.mask, y, c);
+                        put(a.ym, v, mk);
                     }
                 }
             }
         }
-        tc_fence_before();
-        __syncthreads();
-    }
-    // an abandoned pipeline may still have copies or MMAs in flight: wait for them (bounded) before
-    // the shared memory and the tensor memory go away
-    if (!ok && tid == 0) {
-        for (int k = consumed; k < issued; ++k) mbar_wait(&mbarLoad[k & 1], (uint32_t)((k >> 1) & 1), nullptr);
-        if (mmas < consumed) mbar_wait(&mbarMma, (uint32_t)(mmas & 1), nullptr);
     }
     __syncthreads();
+    // an abandoned pipeline may still have row copies in flight: wait for them (bounded) before the
+    // shared memory goes away; the MMA issuer already waited for its MMAs
+    if (tid == 0 && abortFlag)
+        for (int k = consumedRows; k < issuedRows; ++k) mbar_wait(&full[k % S::kRing], (uint32_t)((k / S::kRing) & 1), nullptr);
+    __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, S::kCols);
+    if (warp == 1) tmem_dealloc(tmem, S::kCols);
 }
 
 // ---- weight gradient: dW[co][tap][ci] = sum_p g[p][co] * x[p + tap][ci] ----------------------------
@@ -581,14 +763,14 @@ EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// tensor map of an NHWC BF16 activation [B][H][W][C]: boxes of 8 channels x 130 pixels x 4 rows
+// tensor map of an NHWC BF16 activation [B][H][W][C]: boxes of 8 channels x 130 pixels x 1 row
 cudaError_t patch_map(CUtensorMap* map, const void* x, int B, int H, int W, int C) {
     EncodeTiledFn enc = encode_tiled();
     if (!enc) return cudaErrorNotSupported;
     if ((reinterpret_cast<uintptr_t>(x) & 15u) != 0) return cudaErrorMisalignedAddress;
     const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
     const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-    const cuuint32_t box[4] = {8, (cuuint32_t)kPatchW, (cuuint32_t)kPatchRows, 1};
+    const cuuint32_t box[4] = {8, (cuuint32_t)kRowW, 1, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -598,14 +780,14 @@ cudaError_t patch_map(CUtensorMap* map, const void* x, int B, int H, int W, int 
 
 // CTAs per SM of a persistent kernel: shared memory, registers and TMEM columns (512 per SM)
 template <class K>
-int ctas_per_sm(K kernel, int smem, uint32_t tmemCols) {
+int ctas_per_sm(K kernel, int smem, uint32_t tmemCols, int threads) {
     int dev = 0, smemSm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smemSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 1;
     int per = smemSm / (smem + 1024);
-    per = std::min(per, 65536 / std::max(1, fa.numRegs * 128));
+    per = std::min(per, 65536 / std::max(1, fa.numRegs * threads));
     per = std::min(per, (int)(512 / tmemCols));
     per = std::min(per, 16);
     return std::max(per, 1);
@@ -621,13 +803,19 @@ cudaError_t conv_launch(const FilterConvArgs& a, cudaStream_t s) {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = sms * ctas_per_sm(k_filter_conv<CIN, COUT>, S::kSmem, S::kCols);
+        grid = sms * ctas_per_sm(k_filter_conv<CIN, COUT>, S::kSmem, S::kCols, kConvThreads);
     }
+    if (a.B <= 0 || a.H <= 0 || a.W <= 0) return cudaSuccess;
     CUtensorMap map;
     cudaError_t e = patch_map(&map, a.x, a.B, a.H, a.W, CIN);
     if (e != cudaSuccess) return e;
-    const int tiles = a.B * ((a.H + kTileRows - 1) / kTileRows) * ((a.W + kTilePx - 1) / kTilePx);
-    k_filter_conv<CIN, COUT><<<tiles < grid ? tiles : grid, 128, S::kSmem, s>>>(map, a);
+    // segments of rows (a multiple of 3): about two items per CTA, at least 9 rows (each item re-reads
+    // 2 halo rows)
+    const long long strips = (a.W + kStripPx - 1) / kStripPx, rowsTotal = (long long)a.B * strips * a.H;
+    int segRows = (int)std::min<long long>(a.H, std::max<long long>(9, (rowsTotal + 2LL * grid - 1) / (2LL * grid)));
+    segRows = (segRows + kGroupRows - 1) / kGroupRows * kGroupRows;
+    const long long items = (long long)a.B * strips * ((a.H + segRows - 1) / segRows);
+    k_filter_conv<CIN, COUT><<<(int)std::min<long long>(items, grid), kConvThreads, S::kSmem, s>>>(map, a, segRows);
     count_launch();
     return cudaGetLastError();
 }
