@@ -43,6 +43,8 @@ typedef struct {
 #define RG_FLAG_MEGAKERNEL 4u   /* trace + shade in one persistent kernel instead of the wavefront loop */
 #define RG_FLAG_KERNEL_TIMING 8u /* CUDA events around every traversal launch (rg_timings.traceKernel) */
 #define RG_FLAG_HOST_LOOP 16u    /* rg_render_batch: host-polled round loop instead of the CUDA graph */
+#define RG_FLAG_TLAS_LBVH 32u    /* build the TLAS as an LBVH (Morton order) instead of by binned SAH; TLASes of more
+                                    than 8192 instances are always LBVHs */
 
 /* resources/shaders/vertex.def:3-7 (render/vertex.hpp:27-29): 32 B */
 typedef struct {

@@ -317,7 +317,8 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
     CK(cudaEventRecord(fe->ev[EV_AS0], c->stream));
     CK(setup_instances(c->sc->instIn.as<rg_instance>(), n, c->sc->blasTable.as<DevBlas>(), (uint32_t)c->sc->blas.size(),
                        c->sc->instDev.as<DevInstance>(), c->sc->tlas.primBoxes.as<float>(), c->stream));
-    CK(lbvh_build(buffers(c, c->sc->tlas), c->stream));
+    if (!(c->flags & RG_FLAG_TLAS_LBVH) && n > 1 && n <= kSahMaxPrims) CK(tlas_sah_build(buffers(c, c->sc->tlas), c->stream));
+    else CK(lbvh_build(buffers(c, c->sc->tlas), c->stream));
     CK(wide_records(buffers(c, c->sc->tlas), c->sc->tlas.wide.as<WideNode>(), c->stream));
     CK(inst_records(c->sc->tlas.order.as<uint32_t>(), n, c->sc->instDev.as<DevInstance>(), c->sc->blasTable.as<DevBlas>(),
                     c->sc->tlasLeaves.as<InstRec>(), c->stream));

@@ -348,6 +348,206 @@ __global__ void k_wide_records(const float* __restrict__ primBoxes, const uint32
     out[i] = w;
 }
 
+// ---- binned-SAH TLAS ------------------------------------------------------------------------------
+// One CTA builds a BVH2 over at most kSahMaxPrims instance boxes, top-down, level by level: each warp
+// takes a node task (a range of the order array), reduces the range's box and centroid box, bins the
+// centroids into 16 bins per axis (shared-memory atomics on order-preserving integer images of the
+// bounds), evaluates the 45 surface-area-heuristic splits, partitions the range stably with ballots,
+// and emits its children (single primitives become leaf refs, the rest next-level tasks).  The
+// result has the LBVH's layout (order, left, right, nodeBoxes), so records and traversal are shared.
+constexpr int kSahBins = 16;
+constexpr int kSahWarps = 32;
+
+__device__ __forceinline__ int ord_float(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float unord_float(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+__device__ __forceinline__ float half_area3(const float* lo, const float* hi) {
+    const float dx = fmaxf(hi[0] - lo[0], 0.0f), dy = fmaxf(hi[1] - lo[1], 0.0f), dz = fmaxf(hi[2] - lo[2], 0.0f);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void __launch_bounds__(kSahWarps * 32, 1) k_tlas_sah(const float* __restrict__ boxes, uint32_t n, uint32_t* __restrict__ order,
+                                                                uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
+                                                                uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
+                                                                uint2* __restrict__ tasksA, uint2* __restrict__ tasksB) {
+    __shared__ int bLo[kSahWarps][3][kSahBins][3], bHi[kSahWarps][3][kSahBins][3];
+    __shared__ int bCnt[kSahWarps][3][kSahBins];
+    __shared__ uint32_t nCur, nNext, nodeCounter;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) order[i] = i;
+    if (threadIdx.x == 0) {
+        tasksA[0] = make_uint2(n << 16, 0u);  // range [0, n), node 0
+        nCur = 1;
+        nNext = 0;
+        nodeCounter = 1;
+    }
+    __syncthreads();
+    uint2* cur = tasksA;
+    uint2* nxt = tasksB;
+    for (;;) {
+        const uint32_t count = nCur;
+        if (count == 0) break;
+        for (uint32_t t = warp; t < count; t += kSahWarps) {
+            const uint2 tk = cur[t];
+            const uint32_t b = tk.x & 0xFFFFu, e = tk.x >> 16, node = tk.y;
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (uint32_t i = b + lane; i < e; i += 32) {
+                const float* bx = boxes + 6 * (size_t)order[i];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = fminf(lo[a], bx[a]);
+                    hi[a] = fmaxf(hi[a], bx[3 + a]);
+                    const float c = 0.5f * (bx[a] + bx[3 + a]);
+                    clo[a] = fminf(clo[a], c);
+                    chi[a] = fmaxf(chi[a], c);
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = fminf(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], off));
+                    hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], off));
+                    clo[a] = fminf(clo[a], __shfl_xor_sync(0xFFFFFFFFu, clo[a], off));
+                    chi[a] = fmaxf(chi[a], __shfl_xor_sync(0xFFFFFFFFu, chi[a], off));
+                }
+            if (lane == 0)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    nodeBoxes[6 * (size_t)node + a] = lo[a];
+                    nodeBoxes[6 * (size_t)node + 3 + a] = hi[a];
+                }
+            float scale[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float ext = chi[a] - clo[a];
+                scale[a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
+            }
+            for (int k = lane; k < 3 * kSahBins; k += 32) {
+                const int a = k / kSahBins, bn = k % kSahBins;
+                bCnt[warp][a][bn] = 0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    bLo[warp][a][bn][c] = ord_float(INFINITY);
+                    bHi[warp][a][bn][c] = ord_float(-INFINITY);
+                }
+            }
+            __syncwarp();
+            auto bin_of = [&](const float* bx, int a) {
+                const float c = 0.5f * (bx[a] + bx[3 + a]);
+                return max(0, min((int)((c - clo[a]) * scale[a]), kSahBins - 1));
+            };
+            for (uint32_t i = b + lane; i < e; i += 32) {
+                const float* bx = boxes + 6 * (size_t)order[i];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    if (scale[a] <= 0.0f) continue;
+                    const int k = bin_of(bx, a);
+                    atomicAdd(&bCnt[warp][a][k], 1);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        atomicMin(&bLo[warp][a][k][c], ord_float(bx[c]));
+                        atomicMax(&bHi[warp][a][k][c], ord_float(bx[3 + c]));
+                    }
+                }
+            }
+            __syncwarp();
+            float bestCost = INFINITY;
+            int bestCand = -1;
+            for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
+                const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
+                if (scale[a] <= 0.0f) continue;
+                float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                int nl = 0, nr = 0;
+                for (int k = 0; k < kSahBins; ++k) {
+                    const int cnt = bCnt[warp][a][k];
+                    if (!cnt) continue;
+                    float* X0 = k < sp ? L0 : R0;
+                    float* X1 = k < sp ? L1 : R1;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        X0[c] = fminf(X0[c], unord_float(bLo[warp][a][k][c]));
+                        X1[c] = fmaxf(X1[c], unord_float(bHi[warp][a][k][c]));
+                    }
+                    if (k < sp) nl += cnt;
+                    else nr += cnt;
+                }
+                if (!nl || !nr) continue;
+                const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
+                if (cost < bestCost) {
+                    bestCost = cost;
+                    bestCand = cand;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
+                const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
+                if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
+                    bestCost = oc;
+                    bestCand = oi;
+                }
+            }
+            uint32_t mid = b + (e - b) / 2;  // no usable split (coincident centroids): halve the range
+            if (bestCand >= 0) {
+                const int a = bestCand / (kSahBins - 1), sp = bestCand % (kSahBins - 1) + 1;
+                uint32_t nl = 0;
+                for (uint32_t i0 = b; i0 < e; i0 += 32) {
+                    const uint32_t i = i0 + lane;
+                    const bool isL = i < e && bin_of(boxes + 6 * (size_t)order[i], a) < sp;
+                    nl += __popc(__ballot_sync(0xFFFFFFFFu, isL));
+                }
+                uint32_t lb = 0, rb = 0;
+                for (uint32_t i0 = b; i0 < e; i0 += 32) {
+                    const uint32_t i = i0 + lane;
+                    const bool valid = i < e;
+                    const uint32_t prim = valid ? order[i] : 0u;
+                    const bool isL = valid && bin_of(boxes + 6 * (size_t)prim, a) < sp;
+                    const unsigned lm = __ballot_sync(0xFFFFFFFFu, isL), rm = __ballot_sync(0xFFFFFFFFu, valid && !isL);
+                    const unsigned below = (1u << lane) - 1u;
+                    if (isL) tmp[b + lb + __popc(lm & below)] = prim;
+                    else if (valid) tmp[b + nl + rb + __popc(rm & below)] = prim;
+                    lb += __popc(lm);
+                    rb += __popc(rm);
+                }
+                __syncwarp();
+                for (uint32_t i = b + lane; i < e; i += 32) order[i] = tmp[i];
+                __syncwarp();
+                mid = b + nl;
+            }
+            if (lane == 0) {
+                const uint32_t rb0[2] = {b, mid}, re0[2] = {mid, e};
+                uint32_t ref[2];
+                for (int c = 0; c < 2; ++c) {
+                    if (re0[c] - rb0[c] == 1) {
+                        ref[c] = kLeaf | rb0[c];
+                    } else {
+                        const uint32_t id = atomicAdd(&nodeCounter, 1u);
+                        nxt[atomicAdd(&nNext, 1u)] = make_uint2(rb0[c] | (re0[c] << 16), id);
+                        ref[c] = id;
+                    }
+                }
+                left[node] = ref[0];
+                right[node] = ref[1];
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            nCur = nNext;
+            nNext = 0;
+        }
+        uint2* sw = cur;
+        cur = nxt;
+        nxt = sw;
+        __syncthreads();
+    }
+}
+
 // ---- instances ----------------------------------------------------------------------------------
 __global__ void k_instances(const rg_instance* __restrict__ in, uint32_t n, const DevBlas* __restrict__ blas, uint32_t nblas,
                             DevInstance* __restrict__ out, float* __restrict__ boxes) {
@@ -440,6 +640,16 @@ cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b.flags, 0, sizeof(uint32_t) * (b.n - 1), s);
     if (e != cudaSuccess) return e;
     k_bottom_up<<<blocks(b.n, 256), 256, 0, s>>>(b.primBoxes, b.order, b.n, b.left, b.right, b.parents, b.flags, b.nodeBoxes, b.nodes);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t tlas_sah_build(const LbvhBuffers& b, cudaStream_t s) {
+    if (b.n <= 1) return cudaSuccess;
+    if (b.n > kSahMaxPrims) return cudaErrorInvalidValue;
+    // scratch: the sort buffers (n words each); at most n / 2 tasks per level, 2 words each
+    k_tlas_sah<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes,
+                                             reinterpret_cast<uint2*>(b.valsA), reinterpret_cast<uint2*>(b.valsB));
     count_launch();
     return cudaGetLastError();
 }

@@ -151,6 +151,10 @@ size_t sort_block_count(uint32_t n);
 cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s);  // topology kept, primBoxes changed
 cudaError_t wide_records(const LbvhBuffers& b, WideNode* out, cudaStream_t s);  // after build / refit
+// binned-SAH BVH2 over b.primBoxes in the LBVH's layout (order, left, right, nodeBoxes), one CTA;
+// n <= kSahMaxPrims
+constexpr uint32_t kSahMaxPrims = 8192;
+cudaError_t tlas_sah_build(const LbvhBuffers& b, cudaStream_t s);
 cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes,
                       cudaStream_t s);
 cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, const uint32_t* order, uint32_t n,

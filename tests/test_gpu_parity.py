@@ -71,8 +71,10 @@ def c0_pair(rg, orc):
 
 @pytest.fixture(scope="module")
 def c1_pair(rg, orc):
+    # the LBVH TLAS, whose topology the oracle pins (the default binned-SAH TLAS is checked in
+    # test_gpu_records.py)
     sc = small_two_level()
-    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES).prepare()
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES | rg.RG_FLAG_TLAS_LBVH).prepare()
     return sc, rt, orc.OracleScene(sc)
 
 
@@ -148,7 +150,7 @@ def test_post_passes_bit_exact(c0_pair, orc, show_alpha, fade):
 
 def test_animation_refit_and_tlas_rebuild(rg, orc):
     sc = small_two_level()
-    rt = rg.Raytracer(sc).prepare()
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_TLAS_LBVH).prepare()
     o = orc.OracleScene(sc)
     anim = S.FrameAnimator(sc, seed=7, refit_prob=0.5)
     for frame in range(3):

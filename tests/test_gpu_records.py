@@ -90,6 +90,54 @@ def test_blas_records(rg, scene_pair):
     assert checked > 1000
 
 
+def half_area(b):
+    d = np.maximum(b[..., 3:] - b[..., :3], 0).astype(np.float64)
+    return d[..., 0] * d[..., 1] + d[..., 1] * d[..., 2] + d[..., 2] * d[..., 0]
+
+
+def check_bvh2(bvh):
+    """A BVH2 in the LBVH layout: every primitive in one leaf, every internal node reached once from
+    the root, each internal node's box enclosing its internal children's boxes."""
+    n = len(bvh["order"])
+    assert sorted(bvh["order"].tolist()) == list(range(n))
+    left, right, nb = bvh["left"].astype(np.int64), bvh["right"].astype(np.int64), bvh["nodeboxes"]
+    seen_nodes, seen_leaves, st = set(), set(), [0]
+    while st:
+        i = st.pop()
+        assert i not in seen_nodes
+        seen_nodes.add(i)
+        for c in (left[i], right[i]):
+            if c & LEAF:
+                assert (c & ~LEAF) not in seen_leaves
+                seen_leaves.add(c & ~LEAF)
+            else:
+                assert (nb[i, :3] <= nb[c, :3]).all() and (nb[i, 3:] >= nb[c, 3:]).all()
+                st.append(int(c))
+    assert len(seen_nodes) == n - 1 and len(seen_leaves) == n
+
+
+def test_sah_tlas(rg, orc):
+    """The default TLAS (binned SAH) is a valid BVH2 over all instances with a lower surface-area cost
+    than the LBVH over the same instances, and both trace the same hits."""
+    sc = S.instanced_scene(width=96, height=54, num_samples=1, max_recursions=2, name="c1-instances")
+    rt = rg.Raytracer(sc).prepare()
+    rl = rg.Raytracer(sc, flags=rg.RG_FLAG_TLAS_LBVH).prepare()
+    sah, lb = rt.ctx.bvh(-1), rl.ctx.bvh(-1)
+    assert len(sah["order"]) == len(sc.instances) > 1000
+    check_bvh2(sah)
+    check_records(rt.ctx.bvh_records(-1), sah, None)
+    cost = lambda b: half_area(b["nodeboxes"]).sum() / half_area(b["nodeboxes"][0])
+    assert cost(sah) < 0.9 * cost(lb), (cost(sah), cost(lb))
+    rays = np.concatenate([camera_rays(sc), random_rays(20000, 9, lo=(-60, 0, -60), hi=(60, 14, 60))])
+    tg, ig = rt.ctx.trace_rays(rays)
+    tl, il = rl.ctx.trace_rays(rays)
+    to, io = orc.OracleScene(sc).trace(rays)
+    assert np.array_equal(ig, io) and np.array_equal(tg, to)
+    assert np.array_equal(il, io) and np.array_equal(tl, to)
+    rt.ctx.close()
+    rl.ctx.close()
+
+
 def test_tlas_records(rg, scene_pair):
     sc, rt, o = scene_pair
     check_records(rt.ctx.bvh_records(-1), rt.ctx.bvh(-1), None)
