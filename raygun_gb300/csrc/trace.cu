@@ -511,8 +511,8 @@ struct RayReq {
     bool masked;
 };
 
-struct RayCounts {
-    unsigned long long primary, shadow, secondary, masked;
+struct RayCounts {  // per thread (flushed as 64-bit sums)
+    uint32_t primary, shadow, secondary, masked;
 };
 
 __device__ __forceinline__ uint32_t pcg_hash(uint32_t v) {  // PCG-RXS-M-XS (O'Neill 2014) output permutation
@@ -1159,13 +1159,13 @@ __global__ void __launch_bounds__(256) k_wfb_raygen(const TraceParams P) {
 #define RG_FETCH_THRESHOLD 8
 #endif
 #ifndef RG_WF_STEPS
-#define RG_WF_STEPS 8
+#define RG_WF_STEPS 6
 #endif
 #ifndef RG_WHILE_WHILE
 #define RG_WHILE_WHILE 1
 #endif
 #ifndef RG_INNER_ROUNDS
-#define RG_INNER_ROUNDS 2
+#define RG_INNER_ROUNDS 3
 #endif
 template <bool COUNT, bool BATCH, int THREADS, int DEPTH>
 __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k_wf_trace(const TraceParams P, int q) {
@@ -1265,8 +1265,7 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
 // its sample (true); mask-0 traces and zero directions run their miss shader right away
 template <bool GLOSSY>
 __device__ __forceinline__ bool shade_until_trace(const DevScene& sc, const V3 L, const int maxRec, Hit h, Payload& p, RayReq& ray,
-                                                  Frame* frames, int& fsp, RayCounts& cnt) {
-    Frame cur;
+                                                  Frame* frames, int& fsp, Frame& cur, RayCounts& cnt) {
     for (;;) {
         if (!shade_step<GLOSSY>(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) return true;
         if (ray.masked || (ray.d.x == 0.0f && ray.d.y == 0.0f && ray.d.z == 0.0f)) {
@@ -1298,6 +1297,7 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : RG_SHADE_MIN_BLOCKS) k_wf_sha
         bool emit = false, regen = false;
         uint32_t path = 0;
         Payload p;
+        Frame cur;
         RayReq ray;
         int fsp = 0;
         if (i < count) {
@@ -1325,9 +1325,9 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : RG_SHADE_MIN_BLOCKS) k_wf_sha
             if constexpr (BATCH) {
                 const JobDesc& J = P.jobs[P.slotJob[path]];
                 done = shade_until_trace<GLOSSY>(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, h,
-                                         p, ray, frames, fsp, cnt);
+                                                 p, ray, frames, fsp, cur, cnt);
             } else {
-                done = shade_until_trace<GLOSSY>(P.scene, L, maxRec, h, p, ray, frames, fsp, cnt);
+                done = shade_until_trace<GLOSSY>(P.scene, L, maxRec, h, p, ray, frames, fsp, cur, cnt);
             }
             if (done) {
                 store_sample(P.samples + 3 * (size_t)(BATCH ? P.slotSample[path] : path), p);
