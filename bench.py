@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="rows per render of the CPU-baseline sample (0: full frames)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", default="1920x1080", help="WxH; smaller sizes are for profiling captures only")
-    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch", "serve", "filter"],
+    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch", "serve", "filter", "spheres"],
                     help="game-frame: the 1080p 4x SSAA frame loop; batch: 64 independent scenes per step; "
                          "serve: Poisson render requests through the render server")
     ap.add_argument("--serve-requests", type=int, default=2000)
@@ -661,6 +661,65 @@ def cpu_baseline(orc_scene, sc, rows, min_seconds=10.0, max_renders=20):
                       f"{rays} rays in {dt:.2f} s (trace + shade)"}
 
 
+def run_spheres(args):
+    """The single-level sphere scene (640x360, 1 spp, depth 4, 61,442 triangles; the reference's
+    CPU-runnable case): GPU frame time and Mrays/s with the scene resident, the same frames read back
+    to pinned host memory (e2e), and the oracle on every host core rendering the same frame."""
+    import torch
+    from raygun_gb300 import build as rgbuild, rgcuda
+    import oracle
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    rgbuild.build()
+    sc = S.c0_scene()
+    rt = rgcuda.Raytracer(sc, device=local).prepare()
+    ctx = rt.ctx
+    K, W = max(args.steps, 10), max(args.warmup, 3)
+    for _ in range(W):
+        rt.do_raytracing()
+    ctx.synchronize()
+    ctx.timings()
+    ctx.reset_total_stats()
+    for _ in range(K):
+        rt.do_raytracing()
+    ctx.synchronize()
+    t = ctx.timings()
+    st = ctx.total_stats()
+    rays = st["primary"] + st["shadow"] + st["secondary"]
+    frame_ms = t["rtTotalSum"] / t["frames"]
+    value = rays / (t["rtTotalSum"] * 1e-3) / 1e6
+    host = torch.empty(sc.height * sc.width * 4, dtype=torch.float32).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        rt.do_raytracing()
+        ctx.download_to(host.data_ptr())
+    ctx.synchronize()
+    e2e_ms = (time.perf_counter() - t0) / K * 1e3
+    o = oracle.OracleScene(sc)
+    cores = os.cpu_count() or 1
+    o.render(nthreads=cores)
+    t0 = time.perf_counter()
+    n_cpu = 0
+    cpu_rays = 0
+    while time.perf_counter() - t0 < 5.0 and n_cpu < 20:
+        _, _, _, cs = o.render(nthreads=cores)
+        cpu_rays += cs["primary"] + cs["shadow"] + cs["secondary"]
+        n_cpu += 1
+    cpu_dt = time.perf_counter() - t0
+    out = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": frame_ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic: seeded procedural scene (no dataset)",
+           "config": {"workload": "spheres: 640x360, 1 spp, depth 4, ground quad + 64 UV spheres (61,442 tris), single-level BVH",
+                      "width": sc.width, "height": sc.height, "parallelism": "single GPU"},
+           "rays_per_frame": rays / K, "frame_ms": frame_ms,
+           "e2e": {"value": rays / K / (e2e_ms * 1e-3) / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": sc.height * sc.width * 16, "ms_per_step": e2e_ms},
+           "cpu_baseline": {"value": cpu_rays / cpu_dt / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                            "sample": f"{n_cpu} renders of the whole frame (trace + shade), {cpu_dt:.2f} s"}}
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     """Reference arm: the CPU restatement of the reference shaders on all host cores."""
     rank, world, _ = dist_env()
@@ -712,6 +771,8 @@ def main():
         run_serve(args)
     elif args.workload == "filter":
         run_filter(args)
+    elif args.workload == "spheres":
+        run_spheres(args)
     else:
         run_ours(args)
 
