@@ -356,19 +356,20 @@ uint64_t scene_bytes(const SceneState& st) {
 }
 
 // path state of the wavefront loop for `paths` path slots
-rg_status ensure_wavefront(rg_ctx* c, size_t paths, WavefrontBuffers& w) {
-    const size_t P = paths ? paths : 1;
+// path state for `paths` paths; queues and hit records for max(paths, hitSlots) entries
+rg_status ensure_wavefront(rg_ctx* c, size_t paths, WavefrontBuffers& w, size_t hitSlots = 0) {
+    const size_t P = paths ? paths : 1, Q = std::max(P, hitSlots);
     TRY(ensure(c, c->wfPayload, 64 * P));
     TRY(ensure(c, c->wfMeta, 8 * P));
     TRY(ensure(c, c->wfFrames, 144ull * kMaxFrames * P));
-    TRY(ensure(c, c->wfQO0, 16 * P));
-    TRY(ensure(c, c->wfQO1, 16 * P));
-    TRY(ensure(c, c->wfQD0, 16 * P));
-    TRY(ensure(c, c->wfQD1, 16 * P));
-    TRY(ensure(c, c->wfQP0, 4 * P));
-    TRY(ensure(c, c->wfQP1, 4 * P));
-    TRY(ensure(c, c->wfHitTUV, 16 * P));
-    TRY(ensure(c, c->wfHitInst, 4 * P));
+    TRY(ensure(c, c->wfQO0, 16 * Q));
+    TRY(ensure(c, c->wfQO1, 16 * Q));
+    TRY(ensure(c, c->wfQD0, 16 * Q));
+    TRY(ensure(c, c->wfQD1, 16 * Q));
+    TRY(ensure(c, c->wfQP0, 4 * Q));
+    TRY(ensure(c, c->wfQP1, 4 * Q));
+    TRY(ensure(c, c->wfHitTUV, 16 * Q));
+    TRY(ensure(c, c->wfHitInst, 4 * Q));
     TRY(ensure(c, c->wfCounts, 16));
     w.payload = c->wfPayload.as<float4>();
     w.meta = c->wfMeta.as<int2>();
@@ -671,7 +672,9 @@ rg_status rg_render(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     tp.glossySeed = c->glossySeed;
     c->lastSamples = (uint32_t)ubo->numSamples;
     const bool mega = (c->flags & RG_FLAG_MEGAKERNEL) != 0;
-    if (!mega) TRY(ensure_wavefront(c, (size_t)c->W * c->H * (uint32_t)ubo->numSamples, tp.wf));
+    if (!mega)
+        TRY(ensure_wavefront(c, (size_t)c->W * c->H * (uint32_t)ubo->numSamples, tp.wf,
+                             frame_work_items(c->W, c->H, (uint32_t)ubo->numSamples)));
     CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
     FrameEvents* fe;
     TRY(cur_events(c, &fe));

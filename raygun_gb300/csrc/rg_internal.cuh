@@ -215,8 +215,18 @@ struct TraceParams {
     uint32_t* slotSample;
     const uint32_t* perm;  // nullable: order in which the trace kernel takes the queue's rays
     uint32_t glossySeed;   // 0: the reference's mirror shading; else glossy reference shading (seed)
+    // frame loop: the first (trace, shade) round computes the camera rays and initial payloads of
+    // work items 0 .. W*H*S-1 (8x4-tile order) itself instead of reading a raygen queue
+    int firstRound;
 };
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
+// Work items of the frame loop: W x H pixels padded to whole 8 x 4 tiles, times S samples.  The first
+// round indexes its hit records by work item, so the hit buffers hold this many entries (more than
+// W * H * S when W or H is not a multiple of the tile).
+constexpr int kTileW = 8, kTileH = 4;
+inline size_t frame_work_items(uint32_t W, uint32_t H, uint32_t S) {
+    return (size_t)((W + kTileW - 1) / kTileW) * ((H + kTileH - 1) / kTileH) * (kTileW * kTileH) * S;
+}
 // hostCount: pinned host word used to poll the queue length; iterations: trace/shade rounds run
 // kernelEvents (nullable): callback that returns a (start, end) event pair to record around each
 // traversal launch

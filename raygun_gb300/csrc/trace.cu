@@ -840,7 +840,7 @@ __device__ __forceinline__ int begin_ray(Trav& T, const DevScene& sc, const RayR
     return T.active ? kTraverse : kResult;
 }
 
-constexpr int kTileW = 8, kTileH = 4;  // 32 pixels of one work tile
+// (kTileW x kTileH, the 32 pixels of one work tile, are declared in rg_internal.cuh)
 
 // Persistent kernel: each lane takes (pixel, sample) work items from a global counter -- in
 // warp-aggregated batches -- and runs the sample's whole depth-first trace sequence.  Traversal is
@@ -1094,35 +1094,24 @@ __device__ __forceinline__ void store_sample(float4* so, const Payload& p) {
     so[2] = make_float4(p.roughRGB.x, p.roughRGB.y, p.roughRGB.z, p.roughA);
 }
 
-// raygen: one path per (pixel, sample) in 8x4-tile order; primary rays go to queue 0
-__global__ void __launch_bounds__(256) k_wf_raygen(const TraceParams P) {
-    const WavefrontBuffers& wf = P.wf;
+// work items of the frame loop: one path per (pixel, sample) in 8x4-tile order, all of them in the
+// first round; path = (py * W + px) * S + sample
+__device__ __forceinline__ uint32_t frame_work_total(const TraceParams& P) {
+    const uint32_t S = (uint32_t)P.ubo.numSamples;
+    return ((P.W + kTileW - 1) / kTileW) * ((P.H + kTileH - 1) / kTileH) * (kTileW * kTileH) * S;
+}
+// camera ray and initial payload of work item id (raygen.h:84-102); false outside the image
+__device__ __forceinline__ bool frame_work_item(const TraceParams& P, uint32_t id, uint32_t& path, Payload& p, RayReq& ray) {
     const rg_ubo& U = P.ubo;
     const uint32_t S = (uint32_t)U.numSamples;
-    const int aaRow = S < 8 ? (int)S : 8;
-    const uint32_t tilesX = (P.W + kTileW - 1) / kTileW, tilesY = (P.H + kTileH - 1) / kTileH;
-    const uint32_t total = tilesX * tilesY * (kTileW * kTileH) * S;
+    const uint32_t tilesX = (P.W + kTileW - 1) / kTileW;
+    uint32_t px = 0, py = 0, sample = 0;
+    if (!decode_work(id, P.W, P.H, S, tilesX, px, py, sample)) return false;
     float org[4];
     mul4(U.viewInverse, 0.0f, 0.0f, 0.0f, 1.0f, org);
-    const V3 camO = v3(org[0], org[1], org[2]);
-    unsigned long long c[4] = {0, 0, 0, 0};
-    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
-        const uint32_t id = base + threadIdx.x;
-        uint32_t px = 0, py = 0, sample = 0;
-        const bool valid = id < total && decode_work(id, P.W, P.H, S, tilesX, px, py, sample);
-        const uint32_t pos = warp_append(wf.counts + 0, valid);
-        if (valid) {
-            Payload p;
-            RayReq ray;
-            start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray, P.glossySeed);
-            const uint32_t path = (py * P.W + px) * S + sample;
-            store_payload(wf.payload + 4 * (size_t)path, p);
-            wf.meta[path] = make_int2(0, 0);
-            emit_ray(wf, 0, pos, path, ray);
-            c[0]++;
-        }
-    }
-    flush_counts(P, c, 1);
+    start_sample(U, v3(org[0], org[1], org[2]), px, py, P.W, P.H, (int)sample, S < 8 ? (int)S : 8, p, ray, P.glossySeed);
+    path = (py * P.W + px) * S + sample;
+    return true;
 }
 
 // raygen of a batch: path slot k starts work item k (k < min(totalWork, slots)); the shade kernel
@@ -1171,7 +1160,8 @@ template <bool COUNT, bool BATCH, int THREADS, int DEPTH>
 __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k_wf_trace(const TraceParams P, int q) {
     RG_DECLARE_SMEM_STACK(stk, THREADS, DEPTH);
     const WavefrontBuffers& wf = P.wf;
-    const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
+    const bool first = !BATCH && P.firstRound;
+    const uint32_t count = first ? frame_work_total(P) : *(volatile uint32_t*)(wf.counts + q);
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.counts[q ^ 1] = 0;  // the shade kernel appends there next
     const unsigned lane = threadIdx.x & 31;
     const unsigned ltmask = (1u << lane) - 1u;
@@ -1196,6 +1186,18 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
                     const uint32_t k = base + (uint32_t)__popc(needMask & ltmask);
                     if (k >= count) {
                         exhausted = true;
+                    } else if (first) {  // camera ray of work item k, computed here
+                        slot = k;
+                        uint32_t path;
+                        Payload p0;
+                        RayReq r0;
+                        if (frame_work_item(P, k, path, p0, r0)) {
+                            trav_begin(T, P.scene, r0.o.x, r0.o.y, r0.o.z, r0.d.x, r0.d.y, r0.d.z, r0.tmin, r0.tmax);
+                            if (!T.active) {
+                                wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
+                                wf.hitInst[slot] = 0xFFFFFFFFu;
+                            }
+                        }
                     } else {
                         slot = P.perm ? P.perm[k] : k;
                         if (BATCH) scp = &P.jobs[P.slotJob[wf.qPath[q][slot]]].scene;
@@ -1286,7 +1288,8 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : RG_SHADE_MIN_BLOCKS) k_wf_sha
     const WavefrontBuffers& wf = P.wf;
     const V3 L = v3(P.ubo.lightDir[0], P.ubo.lightDir[1], P.ubo.lightDir[2]);
     const int maxRec = P.ubo.maxRecursions;
-    const uint32_t count = *(volatile uint32_t*)(wf.counts + q);
+    const bool first = !BATCH && P.firstRound;
+    const uint32_t count = first ? frame_work_total(P) : *(volatile uint32_t*)(wf.counts + q);
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.counts[2] = 0;  // the next trace kernel's work counter
     const unsigned lane = threadIdx.x & 31;
     RayCounts cnt = {0, 0, 0, 0};
@@ -1300,7 +1303,12 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : RG_SHADE_MIN_BLOCKS) k_wf_sha
         Frame cur;
         RayReq ray;
         int fsp = 0;
-        if (i < count) {
+        bool live = i < count;
+        if (live && first) {  // the work item's camera ray and initial payload, as the trace kernel made them
+            live = frame_work_item(P, i, path, p, ray);
+            fsp = 0;
+            if (live) cnt.primary++;
+        } else if (live) {
             path = wf.qPath[q][i];
             const float4 o = wf.qO[q][i], d = wf.qD[q][i];
             const int2 meta = wf.meta[path];
@@ -1312,6 +1320,8 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : RG_SHADE_MIN_BLOCKS) k_wf_sha
             ray.missIndex = meta.y;
             ray.masked = false;
             load_payload(wf.payload + 4 * (size_t)path, p);
+        }
+        if (live) {
             const float4 ht = wf.hitTUV[i];
             Hit h;
             h.inst = wf.hitInst[i];
@@ -1630,13 +1640,13 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
     const WfKernel shade = p.glossySeed ? k_wf_shade<false, true> : k_wf_shade<false, false>;
     const WfKernel tail = p.glossySeed ? k_wf_tail<false, true> : k_wf_tail<false, false>;
     const int gShade = grid_of((const void*)shade, 128);
-    const int gRaygen = grid_of((const void*)k_wf_raygen, 256);
     const int gTail = grid_of((const void*)tail, kTraceThreads);
-    if (!gTrace || !gShade || !gRaygen || !gTail) return cudaErrorUnknown;
+    if (!gTrace || !gShade || !gTail) return cudaErrorUnknown;
     cudaError_t e = cudaMemsetAsync(p.wf.counts, 0, 4 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    k_wf_raygen<<<gRaygen, 256, 0, s>>>(p);
-    count_launch();
+    // the first round generates the camera rays itself (no raygen queue)
+    TraceParams p1 = p;
+    p1.firstRound = 1;
     // the pending-ray count below which the remaining paths finish in one k_wf_tail launch; the
     // visit-counting build stays in the round loop (the tail kernel does not count visits)
     const uint32_t tailBelow = c ? 0u : (uint32_t)RG_TAIL_RAYS;
@@ -1647,9 +1657,9 @@ cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (kernelEvents && !kernelEvents(user, &e0, &e1)) e0 = e1 = nullptr;
             if (e0) cudaEventRecord(e0, s);
-            trace<<<gTrace, kTraceThreads, 0, s>>>(p, q);
+            trace<<<gTrace, kTraceThreads, 0, s>>>(it == 0 ? p1 : p, q);
             if (e1) cudaEventRecord(e1, s);
-            shade<<<gShade, 128, 0, s>>>(p, q);
+            shade<<<gShade, 128, 0, s>>>(it == 0 ? p1 : p, q);
             count_launch(2);
             q ^= 1;
         }
