@@ -25,7 +25,7 @@ struct DevBuf {
 
 struct BvhSet {  // buffers of one LBVH (BLAS or TLAS)
     uint32_t n = 0;
-    DevBuf primBoxes, morton, order, left, right, nodeBoxes, nodes, parents, flags, wide;
+    DevBuf primBoxes, morton, order, left, right, nodeBoxes, parents, flags, wide;
 };
 
 struct BlasRec {
@@ -216,7 +216,6 @@ rg_status ensure_bvh(rg_ctx* c, BvhSet& s, uint32_t n) {
     TRY(ensure(c, s.left, 4ull * m));
     TRY(ensure(c, s.right, 4ull * m));
     TRY(ensure(c, s.nodeBoxes, 24ull * m));
-    TRY(ensure(c, s.nodes, sizeof(BvhNode) * m));
     TRY(ensure(c, s.parents, 8ull * n));
     TRY(ensure(c, s.flags, 4ull * m));
     TRY(ensure(c, s.wide, sizeof(WideNode) * m));
@@ -232,7 +231,6 @@ LbvhBuffers buffers(rg_ctx* c, const BvhSet& s) {
     b.left = s.left.as<uint32_t>();
     b.right = s.right.as<uint32_t>();
     b.nodeBoxes = s.nodeBoxes.as<float>();
-    b.nodes = s.nodes.as<BvhNode>();
     b.keysA = c->keysA.as<uint32_t>();
     b.keysB = c->keysB.as<uint32_t>();
     b.valsA = c->valsA.as<uint32_t>();
@@ -251,7 +249,6 @@ rg_status upload_blas_entry(rg_ctx* c, uint32_t b) {
     BlasRec& r = c->sc->blas[b];
     DevBlas e;
     std::memset(&e, 0, sizeof(e));
-    e.nodes = r.bvh.nodes.as<BvhNode>();
     e.wide = r.bvh.wide.as<WideNode>();
     e.tris = r.tris.as<float4>();
     e.n = r.bvh.n;
@@ -294,7 +291,6 @@ DevScene scene_of(const SceneState& st) {
     DevScene s;
     s.blas = st.blasTable.as<DevBlas>();
     s.inst = st.instDev.as<DevInstance>();
-    s.tlasNodes = st.tlas.nodes.as<BvhNode>();
     s.tlasWide = st.tlas.wide.as<WideNode>();
     s.tlasLeaves = st.tlasLeaves.as<InstRec>();
     s.tlasN = st.nInst;
@@ -329,7 +325,7 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
 }
 
 void release_bvh(rg_ctx* c, BvhSet& s) {
-    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags, &s.wide};
+    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.parents, &s.flags, &s.wide};
     for (DevBuf* b : bb) release(c, *b);
 }
 
@@ -346,7 +342,7 @@ void release_scene(rg_ctx* c, SceneState& st) {
 
 uint64_t scene_bytes(const SceneState& st) {
     auto bvh = [](const BvhSet& s) {
-        return s.primBoxes.cap + s.morton.cap + s.order.cap + s.left.cap + s.right.cap + s.nodeBoxes.cap + s.nodes.cap +
+        return s.primBoxes.cap + s.morton.cap + s.order.cap + s.left.cap + s.right.cap + s.nodeBoxes.cap +
                s.parents.cap + s.flags.cap + s.wide.cap;
     };
     uint64_t b = st.vertices.cap + st.indices.cap + st.materials.cap + st.blasTable.cap + st.instIn.cap + st.instDev.cap +
@@ -956,7 +952,7 @@ rg_status rg_lbvh_build_host(rg_ctx* c, const float* boxes, uint32_t n, uint32_t
         if (e != cudaSuccess) st = fail(c, RG_ERR_CUDA, cudaGetErrorString(e));
         if (st == RG_OK) st = download_bvh(c, s, morton, order, left, right, nodeboxes);
     }
-    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.nodes, &s.parents, &s.flags, &s.wide};
+    DevBuf* bb[] = {&s.primBoxes, &s.morton, &s.order, &s.left, &s.right, &s.nodeBoxes, &s.parents, &s.flags, &s.wide};
     cudaStreamSynchronize(c->stream);
     for (DevBuf* b : bb) release(c, *b);
     return st;

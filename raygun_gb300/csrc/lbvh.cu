@@ -266,7 +266,7 @@ __device__ inline void load_box_cg(const float* p, float* b) {
 
 __global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t* __restrict__ order, uint32_t n,
                             const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
-                            const uint32_t* __restrict__ parents, uint32_t* flags, float* nodeBoxes, BvhNode* nodes) {
+                            const uint32_t* __restrict__ parents, uint32_t* flags, float* nodeBoxes) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     uint32_t node = parents[(n - 1) + k];
@@ -286,12 +286,6 @@ __global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t*
             __stcg(o + a, fminf(bl[a], br[a]));
             __stcg(o + 3 + a, fmaxf(bl[3 + a], br[3 + a]));
         }
-        BvhNode nd;
-        nd.a = make_float4(bl[0], bl[3], bl[1], bl[4]);
-        nd.b = make_float4(bl[2], bl[5], br[0], br[3]);
-        nd.c = make_float4(br[1], br[4], br[2], br[5]);
-        nd.d = make_uint4(L, R, 0u, 0u);
-        nodes[node] = nd;
         node = parents[node];
     }
 }
@@ -639,7 +633,7 @@ cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
     if (b.n <= 1) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(b.flags, 0, sizeof(uint32_t) * (b.n - 1), s);
     if (e != cudaSuccess) return e;
-    k_bottom_up<<<blocks(b.n, 256), 256, 0, s>>>(b.primBoxes, b.order, b.n, b.left, b.right, b.parents, b.flags, b.nodeBoxes, b.nodes);
+    k_bottom_up<<<blocks(b.n, 256), 256, 0, s>>>(b.primBoxes, b.order, b.n, b.left, b.right, b.parents, b.flags, b.nodeBoxes);
     count_launch();
     return cudaGetLastError();
 }

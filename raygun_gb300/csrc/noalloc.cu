@@ -32,9 +32,8 @@ constexpr size_t kKeysBytes = align_up(4ull * kMaxPrims);
 constexpr size_t kHistBytes = align_up(4ull * 256 * ((kMaxPrims + 2047) / 2048));
 constexpr size_t kParentsBytes = align_up(8ull * kMaxPrims);
 constexpr size_t kFlagsBytes = align_up(4ull * kMaxPrims);
-constexpr size_t kNodesBytes = align_up(sizeof(BvhNode) * kMaxPrims);
 constexpr size_t kBoundsBytes = align_up(64);
-constexpr size_t kScratchBytes = 4 * kKeysBytes + kHistBytes + kParentsBytes + kFlagsBytes + kNodesBytes + kBoundsBytes;
+constexpr size_t kScratchBytes = 4 * kKeysBytes + kHistBytes + kParentsBytes + kFlagsBytes + kBoundsBytes;
 
 static __device__ __align__(256) unsigned char g_lbvh_scratch[kScratchBytes];
 
@@ -87,7 +86,6 @@ extern "C" rg_status rg_lbvh_build_device_noalloc(const float* d_boxes, uint32_t
     b.blockHist = reinterpret_cast<uint32_t*>(p); p += kHistBytes;
     b.parents = reinterpret_cast<uint32_t*>(p); p += kParentsBytes;
     b.flags = reinterpret_cast<uint32_t*>(p); p += kFlagsBytes;  // zeroed inside lbvh_build (refit step)
-    b.nodes = reinterpret_cast<BvhNode*>(p); p += kNodesBytes;
     b.bounds = reinterpret_cast<uint32_t*>(p);                    // reset by the build's first kernel
     cudaError_t e = lbvh_build(b, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? RG_OK : RG_ERR_CUDA;

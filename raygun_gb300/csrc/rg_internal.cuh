@@ -24,15 +24,6 @@ constexpr uint32_t kLeaf = 0x80000000u;
 constexpr int kTraversalStack = RG_STACK_DEPTH;
 constexpr int kMaxFrames = 10;  // maxRecursions (<= 8 supported) + primary + masked-miss leaf
 
-// BVH2 node: boxes of BOTH children so one 64-byte node fetch (four 16-byte loads) tests two
-// children.  refs: bit 31 set = leaf (payload = sorted position), else internal node index.
-struct __align__(16) BvhNode {
-    float4 a;  // L.lo.x, L.hi.x, L.lo.y, L.hi.y
-    float4 b;  // L.lo.z, L.hi.z, R.lo.x, R.hi.x
-    float4 c;  // R.lo.y, R.hi.y, R.lo.z, R.hi.z
-    uint4 d;   // left ref, right ref, 0, 0
-};
-static_assert(sizeof(BvhNode) == 64, "node");
 
 // 4-wide record of BVH2 node i: the boxes and refs of i's grandchildren (a leaf child stands in
 // for its own slot).  Traversal visits records only, so it skips every other BVH2 level; the
@@ -52,7 +43,6 @@ struct Box {
 // per-BLAS record read by the traversal kernel
 struct DevBlas {
     const WideNode* wide;
-    const BvhNode* nodes;
     const float4* tris;  // 3 float4 per sorted leaf: v0 (w = primitive id bits), v1, v2
     uint32_t n;          // triangle count
     uint32_t pad;
@@ -82,7 +72,6 @@ static_assert(sizeof(InstRec) == 96, "instance record");
 struct DevScene {
     const DevBlas* blas;
     const DevInstance* inst;
-    const BvhNode* tlasNodes;
     const WideNode* tlasWide;
     const InstRec* tlasLeaves;  // sorted position -> instance record
     uint32_t tlasN;
@@ -138,7 +127,6 @@ struct LbvhBuffers {  // scratch + outputs of one LBVH build, sized by the calle
     uint32_t* left;        // n-1
     uint32_t* right;       // n-1
     float* nodeBoxes;      // (n-1) x 6
-    BvhNode* nodes;        // n-1
     // scratch
     uint32_t* keysA; uint32_t* keysB; uint32_t* valsA; uint32_t* valsB;
     uint32_t* blockHist;   // 256 * numBlocks(n)

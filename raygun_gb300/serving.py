@@ -29,7 +29,7 @@ PATH_SLOT_BYTES = 64 + 8 + 144 * 10 + 2 * 36 + 20
 SAMPLE_BYTES, PIXEL_BYTES, SCRATCH_PIXEL_BYTES = 48, 16, 40
 # device bytes per triangle of a resident BLAS (BVH2 nodes, 4-wide records, build scratch kept for
 # refits, leaf-ordered triangles) and per instance of a TLAS; geometry buffers are counted as uploaded
-BLAS_TRI_BYTES, TLAS_INSTANCE_BYTES = 300, 560
+BLAS_TRI_BYTES, TLAS_INSTANCE_BYTES = 236, 496
 
 
 @dataclasses.dataclass
