@@ -15,7 +15,8 @@ second of the whole frame (TLAS build + refits + trace + post).
          memset) between frames.
   e2e:   the same frames through the C ABI with host buffers: per frame the instance array and the
          refit vertices are copied from pinned host memory and the framebuffer is read back into
-         pinned host memory, all inside the timed region.
+         pinned host memory (rg_download_async: frame f's copy overlaps frame f+1's render), timed
+         by wall clock until the last frame's pixels are in host memory.
 
 --impl reference runs the reference arm: the reference's own GPU path needs a Vulkan ray-tracing
 driver (unavailable on this machine), so it times the CPU restatement of the same shaders (the oracle)
@@ -233,7 +234,8 @@ def run_ours(args):
     inst_host = inst_pin.numpy()
     vert_pin = torch.from_numpy(np.concatenate(vert_chunks) if vert_chunks else np.zeros(16, np.uint8)).pin_memory()
     vert_host = vert_pin.numpy()
-    fb_pin = torch.empty(sc.height * sc.width * 16, dtype=torch.uint8).pin_memory()
+    # two pinned framebuffers: frame f's read-back overlaps frame f+1's render (rg_download_async)
+    fb_pins = [torch.empty(sc.height * sc.width * 16, dtype=torch.uint8).pin_memory() for _ in range(2)]
 
     def step_host(f):
         h2d = 0
@@ -244,9 +246,9 @@ def run_ours(args):
             h2d += nv * 32
         ctx.build_tlas(inst_host[f].view(S.INSTANCE))
         ctx.render(ubo, True)
+        ctx.download_async(fb_pins[f % 2].data_ptr())
         with torch.cuda.stream(ext):
             flush.zero_()
-        ctx.download_to(fb_pin.data_ptr())
         return h2d + stride + S.UBO.itemsize
 
     def barrier():
@@ -293,15 +295,16 @@ def run_ours(args):
     ctx.reset_total_stats()
     h2d = 0
     barrier()
-    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2.record(ext)
+    # wall clock from the first frame's inputs to the last frame's pixels in host memory (the final
+    # barrier waits for the render stream and the read-back copies)
+    t_e2e = time.perf_counter()
     for _ in range(K):
         h2d += step_host(f)
         f += 1
-    e3.record(ext)
     barrier()
+    wall_ms = (time.perf_counter() - t_e2e) * 1e3
     tot2 = ctx.total_stats()
-    e2e_value, ms_e2e = replica_throughput(tot2["primary"] + tot2["shadow"] + tot2["secondary"], e2.elapsed_time(e3), world, dev)
+    e2e_value, ms_e2e = replica_throughput(tot2["primary"] + tot2["shadow"] + tot2["secondary"], wall_ms, world, dev)
     e2e = {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d // K),
            "d2h_bytes_per_step": sc.height * sc.width * 16, "ms_per_step": ms_e2e / K}
 

@@ -183,12 +183,18 @@ rg_status rg_render(rg_ctx* ctx, const rg_ubo* ubo, int32_t fxaa);
 
 /* Framebuffer (width*height*4 floats) to host memory; waits for the frame. */
 rg_status rg_download(rg_ctx* ctx, float* host_rgba);
+/* The same read-back without waiting: the last rendered frame is staged on the device (one of two
+ * slots) and copied to host_rgba (pinned memory for an overlapped copy) on the library's copy stream
+ * while later frames render. host_rgba must stay valid and unread until rg_synchronize returns.
+ * Stands where Raygun blits the frame to its swapchain image and presents it (render_system.cpp:130-161):
+ * the render call returns before the image has left the GPU. */
+rg_status rg_download_async(rg_ctx* ctx, float* host_rgba);
 /* Device pointer of the RGBA32F framebuffer (valid until the next rg_set_resolution). */
 rg_status rg_framebuffer_device(rg_ctx* ctx, float** d_rgba);
 /* Any of the RG_IMAGE_* images as RGBA32F (roughTransition: value in .r). */
 rg_status rg_download_image(rg_ctx* ctx, int32_t which, float* host_rgba);
 
-rg_status rg_synchronize(rg_ctx* ctx);
+rg_status rg_synchronize(rg_ctx* ctx);  /* waits for the render stream and for rg_download_async copies */
 /* Replaces Profiler (raygun/profiler.cpp:55-105): GPU ranges of the last frame. */
 rg_status rg_get_timings(rg_ctx* ctx, rg_timings* out);
 rg_status rg_get_stats(rg_ctx* ctx, rg_stats* out);

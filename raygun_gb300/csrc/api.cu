@@ -125,6 +125,13 @@ struct rg_ctx {
     FrameEvents* evCur = nullptr;  // ranges recorded since the last frame
     rg_timings lastTimings{};
     bool haveFrame = false;
+    // asynchronous read-back (rg_download_async): two device staging slots, copied to the host on
+    // their own stream while the next frame renders; a slot is reused once its last copy finished
+    cudaStream_t copyStream = nullptr;
+    DevBuf readback[2];
+    cudaEvent_t staged[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    bool copyIssued[2] = {false, false};
+    int readbackSlot = 0;
 };
 
 namespace {
@@ -413,7 +420,12 @@ rg_status rg_create(rg_ctx** out, const rg_device_opts* opts) {
     }
     cudaMemsetAsync(c->counters.p, 0, 128, c->stream);
     if (cudaHostAlloc(&c->hostCount, 8 * sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->staged[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->staged[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->copied[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->copied[1], cudaEventDisableTiming) != cudaSuccess) {
         rg_destroy(c);
         return RG_ERR_OUT_OF_MEMORY;
     }
@@ -425,6 +437,14 @@ rg_status rg_destroy(rg_ctx* c) {
     if (!c) return RG_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->copyStream) cudaStreamSynchronize(c->copyStream);
+    release(c, c->readback[0]);
+    release(c, c->readback[1]);
+    for (int k = 0; k < 2; ++k) {
+        if (c->staged[k]) cudaEventDestroy(c->staged[k]);
+        if (c->copied[k]) cudaEventDestroy(c->copied[k]);
+    }
+    if (c->copyStream) cudaStreamDestroy(c->copyStream);
     DevBuf* bufs[] = {&c->keysA, &c->keysB, &c->valsA, &c->valsB, &c->blockHist, &c->bounds, &c->base, &c->normal, &c->rough,
                       &c->finalImg, &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC,
                       &c->tmpD, &c->samples, &c->workCounter, &c->wfPayload, &c->wfMeta, &c->wfFrames, &c->wfQO0, &c->wfQO1,
@@ -715,6 +735,24 @@ rg_status rg_download(rg_ctx* c, float* host) {
     return RG_OK;
 }
 
+rg_status rg_download_async(rg_ctx* c, float* host) {
+    if (!c || !host) return RG_ERR_INVALID_ARG;
+    if (!c->haveFrame) return fail(c, RG_ERR_NOT_READY, "no frame rendered");
+    TRY(set_device(c));
+    const size_t bytes = 16ull * c->W * c->H;
+    const int k = c->readbackSlot;
+    TRY(ensure(c, c->readback[k], bytes));
+    if (c->copyIssued[k]) CK(cudaStreamWaitEvent(c->stream, c->copied[k], 0));  // the slot's previous copy left
+    CK(cudaMemcpyAsync(c->readback[k].p, c->fb.p, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaEventRecord(c->staged[k], c->stream));
+    CK(cudaStreamWaitEvent(c->copyStream, c->staged[k], 0));
+    CK(cudaMemcpyAsync(host, c->readback[k].p, bytes, cudaMemcpyDeviceToHost, c->copyStream));
+    CK(cudaEventRecord(c->copied[k], c->copyStream));
+    c->copyIssued[k] = true;
+    c->readbackSlot = k ^ 1;
+    return RG_OK;
+}
+
 rg_status rg_framebuffer_device(rg_ctx* c, float** d) {
     if (!c || !d) return RG_ERR_INVALID_ARG;
     if (!c->W) return fail(c, RG_ERR_NOT_READY, "rg_set_resolution was not called");
@@ -762,6 +800,7 @@ rg_status rg_synchronize(rg_ctx* c) {
     if (!c) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
     CK(cudaStreamSynchronize(c->stream));
+    CK(cudaStreamSynchronize(c->copyStream));
     TRY(settle_graph(c));
     return RG_OK;
 }

@@ -39,7 +39,7 @@ EXPORTS = [
     "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory", "rg_filter_create", "rg_filter_destroy",
     "rg_filter_last_error", "rg_filter_get_params", "rg_filter_set_params", "rg_filter_get_grads", "rg_filter_forward",
     "rg_filter_train_step", "rg_filter_input", "rg_filter_target", "rg_set_filter", "rg_set_glossy",
-    "rg_bvh_records",
+    "rg_bvh_records", "rg_download_async",
 ]
 FILTER_PARAMS = 78243
 # layer shapes of the learned filter: (out, in) real channel counts
@@ -122,6 +122,7 @@ def load(path: str = LIB_PATH):
         "rg_bvh_info": ([P, U32, ctypes.POINTER(U32), P, P, P, P, P], I32),
         "rg_instance_inverse": ([P, P], I32),
         "rg_bvh_records": ([P, U32, P, U32, ctypes.POINTER(U32)], I32),
+        "rg_download_async": ([P, P], I32),
         "rg_trace_rays": ([P, P, U32, P, P], I32),
         "rg_post_only": ([P, P, P, P, P, I32], I32),
         "rg_lbvh_build_host": ([P, P, U32, P, P, P, P, P], I32),
@@ -256,6 +257,10 @@ class Context:
 
     def download_to(self, host_ptr: int):
         self._ck(self.L.rg_download(self.h, ctypes.c_void_p(host_ptr)))
+
+    def download_async(self, host_ptr: int):
+        """Queue the read-back of the last frame into host_ptr (valid until synchronize())."""
+        self._ck(self.L.rg_download_async(self.h, ctypes.c_void_p(host_ptr)))
 
     def framebuffer_ptr(self) -> int:
         p = ctypes.c_void_p()

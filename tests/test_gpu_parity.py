@@ -183,6 +183,31 @@ def test_samples_and_depths(rg, orc, spp, depth, mega):
     assert_image_close(fin, orc.post(sc.ubo, ob, on, orr), f"spp{spp} depth{depth} mega={mega}")
 
 
+def test_download_async(rg):
+    """Asynchronous read-backs through both staging slots deliver each frame's own pixels, equal to
+    the synchronous read-back of the same frame."""
+    torch = pytest.importorskip("torch")
+    sc = small_two_level()
+    rt = rg.Raytracer(sc).prepare()
+    ubos = [sc.ubo.copy() for _ in range(3)]
+    for k, u in enumerate(ubos):
+        u["clearColor"] = np.array([0.1 * k, 0.2, 0.3], np.float32)
+        u["lightDir"] = np.array([-0.4 + 0.2 * k, -1.0, 0.3], np.float32)
+    want = []
+    for u in ubos:
+        rt.ctx.render(u, True)
+        want.append(rt.ctx.download())
+    bufs = [torch.empty(sc.height * sc.width * 4, dtype=torch.float32).pin_memory() for _ in ubos]
+    for u, b in zip(ubos, bufs):
+        rt.ctx.render(u, True)
+        rt.ctx.download_async(b.data_ptr())
+    rt.ctx.synchronize()
+    for w, b in zip(want, bufs):
+        assert np.array_equal(b.numpy().reshape(w.shape), w)
+    assert not np.array_equal(want[0], want[2])
+    rt.ctx.close()
+
+
 def test_errors_are_status_codes(rg):
     ctx = rg.Context()
     sc = S.spheres_scene(n_spheres=2, width=16, height=16, slices=8, stacks=4)
