@@ -34,50 +34,54 @@ namespace {
 // rounded product, so it is kept as a bracket [cl, ch] around -o*j, and the products-sums are rounded
 // down for entry planes and up for exit planes: every computed entry is at or below the exact one and
 // every exit at or above, and the remaining rounding of 1/d itself is covered by the kInflate margin
-// (Ize 2013).  |j| is clamped to [2^-60, 2^64] so that nothing overflows: past 2^64 (a zero or tiny
-// direction component) the entry plane's t stays a lower bound where it is positive and the exit plane
-// is dropped (ch = +inf); below 2^-60 the exit plane's t stays an upper bound where it is positive and
-// the entry plane is dropped (cl = -inf).  Boxes are therefore never rejected when the exact test
-// accepts them, including rays that start on a plane with a zero direction component.  Which of a
-// box's two planes is the entry one follows from the sign of j (the ray's octant).
+// (Ize 2013).  |j| is clamped to [2^-60, 2^64] so that nothing overflows.  Past 2^64 (a zero or tiny
+// direction component) the entry plane's t stays a lower bound where it is positive.  The exit
+// plane's t is raised by the ray's current far bound tfar (ch = -o*j + tfar, rounded up): an exit
+// plane ahead of the origin then lies at or beyond tfar and never rejects the box, while one behind
+// the origin still does (its exact t is at or below the clamped one, so raising it stays an upper
+// bound).  tfar only shrinks during a traversal, so terms set with an earlier tfar stay valid.
+// Below 2^-60 the exit plane's t stays an upper bound where it is positive and the entry plane is
+// dropped (cl = -inf).  Boxes are therefore never rejected when the exact test accepts them,
+// including rays that start on a plane with a zero direction component.  Which of a box's two
+// planes is the entry one follows from the sign of j (the ray's octant).
 struct Ray {
     float ox, oy, oz;              // origin of the current level (world, or the instance's object space)
     float dx, dy, dz;              // WORLD direction (kept while inside a BLAS: only instance entry reads it)
     float jx, jy, jz;              // 1/d of the current level, magnitude clamped to [2^-60, 2^64]
     float clx, cly, clz;           // -o*j rounded down (-inf: entry planes dropped)
-    float chx, chy, chz;           // -o*j rounded up (+inf: exit planes dropped)
+    float chx, chy, chz;           // -o*j rounded up (plus the far bound where |j| = 2^64)
     float Sx, Sy, Sz;              // shear of the watertight triangle test (BLAS level)
     uint32_t bits;                 // kx | ky << 2 | kz << 4 (triangle test axes) | octant << 6
 };
 
 __device__ __forceinline__ float comp(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
 
-// j, cl, ch and the octant from the origin and 1/d
-__device__ __forceinline__ void box_terms(float o, float inv, float& j, float& cl, float& ch) {
+// j, cl, ch from the origin, 1/d and the ray's current far bound tfar
+__device__ __forceinline__ void box_terms(float o, float inv, float tfar, float& j, float& cl, float& ch) {
     const float ai = fabsf(inv);
     j = copysignf(fminf(fmaxf(ai, 0x1p-60f), 0x1p64f), inv);
     const float c = -(o * j);
     const float err = fabsf(c) * 0x1p-22f;  // |c - (-o j)| <= 2^-24 |c| (one rounding)
-    // the drop rules read j alone (so that a saved j restores the same terms); at exactly 2^64 or
-    // 2^-60 dropping a plane only accepts more
+    // the clamp rules read j alone (so that a saved j restores valid terms); at exactly 2^64 or
+    // 2^-60 they only accept more
     cl = fabsf(j) > 0x1p-60f ? __fsub_rd(c, err) : -INFINITY;
-    ch = fabsf(j) < 0x1p64f ? __fadd_ru(c, err) : INFINITY;
+    ch = fabsf(j) < 0x1p64f ? __fadd_ru(c, err) : __fadd_ru(__fadd_ru(c, err), tfar);
 }
 
 __device__ __forceinline__ uint32_t octant(float jx, float jy, float jz) {
     return (jx < 0.0f ? 1u : 0u) | (jy < 0.0f ? 2u : 0u) | (jz < 0.0f ? 4u : 0u);
 }
 
-__device__ __forceinline__ void set_box_terms(Ray& r, float ix, float iy, float iz) {
-    box_terms(r.ox, ix, r.jx, r.clx, r.chx);
-    box_terms(r.oy, iy, r.jy, r.cly, r.chy);
-    box_terms(r.oz, iz, r.jz, r.clz, r.chz);
+__device__ __forceinline__ void set_box_terms(Ray& r, float ix, float iy, float iz, float tfar) {
+    box_terms(r.ox, ix, tfar, r.jx, r.clx, r.chx);
+    box_terms(r.oy, iy, tfar, r.jy, r.cly, r.chy);
+    box_terms(r.oz, iz, tfar, r.jz, r.clz, r.chz);
     r.bits = (r.bits & 63u) | octant(r.jx, r.jy, r.jz) << 6;
 }
 
 // object-space ray at instance entry: origin, box terms and the triangle test's shear; the world
 // direction in r stays untouched
-__device__ __forceinline__ void ray_pre(Ray& r, float ox, float oy, float oz, float dx, float dy, float dz) {
+__device__ __forceinline__ void ray_pre(Ray& r, float ox, float oy, float oz, float dx, float dy, float dz, float tfar) {
     r.ox = ox; r.oy = oy; r.oz = oz;
     float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
     int kz = 0;
@@ -91,15 +95,15 @@ __device__ __forceinline__ void ray_pre(Ray& r, float ox, float oy, float oz, fl
     r.Sx = comp(dx, dy, dz, kx) / dkz;
     r.Sy = comp(dx, dy, dz, ky) / dkz;
     r.Sz = 1.0f / dkz;
-    set_box_terms(r, 1.0f / dx, 1.0f / dy, 1.0f / dz);
+    set_box_terms(r, 1.0f / dx, 1.0f / dy, 1.0f / dz, tfar);
 }
 
 // the world-space ray at the TLAS level (no triangle is tested there)
-__device__ __forceinline__ void ray_pre_world(Ray& r, float ox, float oy, float oz, float dx, float dy, float dz) {
+__device__ __forceinline__ void ray_pre_world(Ray& r, float ox, float oy, float oz, float dx, float dy, float dz, float tfar) {
     r.ox = ox; r.oy = oy; r.oz = oz;
     r.dx = dx; r.dy = dy; r.dz = dz;
     r.bits = 0u;
-    set_box_terms(r, 1.0f / dx, 1.0f / dy, 1.0f / dz);
+    set_box_terms(r, 1.0f / dx, 1.0f / dy, 1.0f / dz, tfar);
 }
 
 constexpr float kInflate = 1.0000004f;  // 1 + 2*gamma_3 (Ize 2013) rounded up
@@ -254,7 +258,7 @@ __device__ __forceinline__ void trav_begin(Trav& T, const DevScene& sc, float ox
     T.active = false;
     if ((dx == 0.0f && dy == 0.0f && dz == 0.0f) || sc.tlasN == 0) return;
     T.tmin = tmin;
-    ray_pre_world(T.r, ox, oy, oz, dx, dy, dz);
+    ray_pre_world(T.r, ox, oy, oz, dx, dy, dz, tmax);
     if (sc.tlasN > 1 && box_test6(T.r, sc.tlasRoot, sc.tlasRoot + 3, tmin, T.h.t) == INFINITY) return;
     T.sp = 0;
     T.nodes = sc.tlasWide;
@@ -324,7 +328,7 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
             if (!(ex == 0.0f && ey == 0.0f && ez == 0.0f)) {
                 Ray orr;
                 orr.dx = dx; orr.dy = dy; orr.dz = dz;  // the world direction stays in the ray
-                ray_pre(orr, qx, qy, qz, ex, ey, ez);
+                ray_pre(orr, qx, qy, qz, ex, ey, ez, T.h.t);
                 const float blo[3] = {lo.x, lo.y, lo.z}, bhi[3] = {hi.x, hi.y, hi.z};
                 if (box_test6(orr, blo, bhi, tmin, T.h.t) != INFINITY) {
                     if (T.sp < STACK::kDepth) {
@@ -359,9 +363,9 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
         T.inBlas = false;
         T.nodes = sc.tlasWide;
         T.r.ox = stack.w(0); T.r.oy = stack.w(1); T.r.oz = stack.w(2);
-        box_terms(T.r.ox, stack.w(3), T.r.jx, T.r.clx, T.r.chx);
-        box_terms(T.r.oy, stack.w(4), T.r.jy, T.r.cly, T.r.chy);
-        box_terms(T.r.oz, stack.w(5), T.r.jz, T.r.clz, T.r.chz);
+        box_terms(T.r.ox, stack.w(3), T.h.t, T.r.jx, T.r.clx, T.r.chx);
+        box_terms(T.r.oy, stack.w(4), T.h.t, T.r.jy, T.r.cly, T.r.chy);
+        box_terms(T.r.oz, stack.w(5), T.h.t, T.r.jz, T.r.clz, T.r.chz);
         T.r.bits = octant(T.r.jx, T.r.jy, T.r.jz) << 6;
         }
 }
