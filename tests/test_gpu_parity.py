@@ -260,3 +260,25 @@ def test_material_live_edit(rg, orc):
     ob, on, orr, _ = o.render()
     assert_image_close(after, orc.post(sc.ubo, ob, on, orr), "after material edit")
     assert np.abs(after - before).max() > 0.1
+
+
+def test_vertex_material_edit_without_refit(rg, orc):
+    """The closest-hit shader reads v0's matIndex from the vertex buffer every frame
+    (closesthit.rchit:100-109): a vertex update that only reassigns materials reaches the next
+    frame without a refit (the traversal's triangle records carry the material index and are
+    refreshed for the BLASes whose vertices changed)."""
+    sc = S.spheres_scene(n_spheres=10, width=80, height=45, num_samples=1, max_recursions=4, seed=11)
+    rt = rg.Raytracer(sc).prepare()
+    before = rt.render()
+    verts = sc.vertices.copy()
+    nm = len(sc.materials)
+    # reassign the material of every other sphere vertex (positions untouched)
+    sel = np.arange(len(verts)) % 2 == 0
+    verts["matIndex"][sel] = (verts["matIndex"][sel] + 3) % nm
+    rt.ctx.update_vertices(0, verts)
+    after = rt.render()
+    sc.vertices = verts
+    o = orc.OracleScene(sc)
+    ob, on, orr, _ = o.render()
+    assert_image_close(after, orc.post(sc.ubo, ob, on, orr), "after vertex material edit")
+    assert np.abs(after - before).max() > 0.1
