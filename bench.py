@@ -155,7 +155,7 @@ def measured_peak_hbm():
 
 def trace_traffic():
     """DRAM bytes of one trace-kernel launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "k_wf_trace_c1.json")
+    p = os.path.join(ROOT, "profiles", "k_wf_trace_game_frame_1080p.json")
     try:
         d = json.load(open(p))
         return d.get("dram_bytes_per_launch"), d.get("source")
@@ -675,7 +675,7 @@ def run_spheres(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     rgbuild.build()
-    sc = S.c0_scene()
+    sc = S.sphere_scene()
     rt = rgcuda.Raytracer(sc, device=local).prepare()
     ctx = rt.ctx
     K, W = max(args.steps, 10), max(args.warmup, 3)
@@ -730,7 +730,7 @@ def run_reference(args):
         return
     import oracle
     oracle.build()
-    sc = S.c1_scene()
+    sc = S.game_frame_scene()
     o = oracle.OracleScene(sc)
     nthreads = os.cpu_count() or 1
     K, W = args.steps, args.warmup

@@ -185,7 +185,7 @@ def evaluate(flt, n_scenes: int = 4, width: int = 1920, height: int = 1080, seed
 def post_times(flt, frames: int = 20):
     """Post-stage and whole-frame times on the game frame (1080p, 4 spp) with the plain passes and
     with the filter (CUDA events of the library's profiler ranges)."""
-    sc = scenes.c1_scene()
+    sc = scenes.game_frame_scene()
     rt = rg.Raytracer(sc).prepare()
     out = {}
     for name, f in (("plain", None), ("learned", flt)):

@@ -358,9 +358,9 @@ def spheres_scene(n_spheres=64, width=640, height=360, num_samples=1, max_recurs
                    np.concatenate(mats), identity_instance(), ubo, width, height)
 
 
-def c0_scene() -> Scene:
+def sphere_scene() -> Scene:
     """640x360, 1 spp, depth 4, 64 spheres + ground = 61,442 triangles, single-level BVH."""
-    return spheres_scene(name="c0")
+    return spheres_scene(name="spheres")
 
 
 # ----------------------------------------------------------------------------- two-level scene
@@ -383,13 +383,13 @@ def _random_axis(rng: Rng):
     return np.array([s * math.cos(a), s * math.sin(a), z])
 
 
-C1_MESH_COUNTS = (300, 250, 150, 50, 130, 130, 7, 7)
+GAME_FRAME_MESH_COUNTS = (300, 250, 150, 50, 130, 130, 7, 7)
 """Instances per mesh for the game-frame scene, in mesh order
 (ico3, ico4, ico5, ico6, torusA, torusB, heightA, heightB): 1024 instances, ~11.7M triangles."""
 
 
 def instanced_scene(width=1920, height=1080, num_samples=4, max_recursions=5, seed=1,
-                    counts=C1_MESH_COUNTS, hf_n=256, ico_levels=(3, 4, 5, 6), name="c1") -> Scene:
+                    counts=GAME_FRAME_MESH_COUNTS, hf_n=256, ico_levels=(3, 4, 5, 6), name="game-frame") -> Scene:
     """The two-level game-frame scene: 8 meshes (icospheres subdiv 3..6, two 64x32 tori,
     two 256x256 unit-spaced heightfields with U[0,0.5] displacement), instanced ``sum(counts)`` times.
 
@@ -433,7 +433,7 @@ def instanced_scene(width=1920, height=1080, num_samples=4, max_recursions=5, se
     return _finish(name, parts, mats, inst, ubo, width, height)
 
 
-def c1_scene() -> Scene:
+def game_frame_scene() -> Scene:
     return instanced_scene()
 
 
@@ -492,7 +492,7 @@ def mesh_vertex_count(scene: Scene, b: int) -> int:
 
 # ----------------------------------------------------------------------------- batched scenes
 
-C2_RESOLUTIONS = ((320, 180), (640, 360), (1280, 720), (1920, 1080))
+BATCH_RESOLUTIONS = ((320, 180), (640, 360), (1280, 720), (1920, 1080))
 _MESH_CACHE: dict = {}
 
 
@@ -508,8 +508,8 @@ def _catalog_mesh(kind: str) -> Mesh:
     return _MESH_CACHE[kind]
 
 
-C2_KINDS = ("ico3", "ico4", "ico5", "ico6", "torus_a", "torus_b", "heightfield")
-C2_KIND_TRIS = (1280, 5120, 20480, 81920, 4096, 4096, 130050)
+BATCH_KINDS = ("ico3", "ico4", "ico5", "ico6", "torus_a", "torus_b", "heightfield")
+BATCH_KIND_TRIS = (1280, 5120, 20480, 81920, 4096, 4096, 130050)
 
 
 def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int, num_samples: int,
@@ -526,17 +526,17 @@ def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int
     heightfields are terrain tiles (48 x 48 world units) laid on a grid around the origin.  The
     camera looks at the centre from (0, 0.5R + 6, -1.6R - 8) with a 60 degree vertical field of view.
     """
-    kinds_tris = dict(zip(C2_KINDS, C2_KIND_TRIS))
+    kinds_tris = dict(zip(BATCH_KINDS, BATCH_KIND_TRIS))
     if hf_n != 256:
         kinds_tris["heightfield"] = 2 * (hf_n - 1) ** 2
     chosen = []
     remaining = float(target_tris)
     while True:
-        fits = [k for k in C2_KINDS if kinds_tris[k] <= remaining]
+        fits = [k for k in BATCH_KINDS if kinds_tris[k] <= remaining]
         if not fits:
             if chosen:
                 break
-            fits = [min(C2_KINDS, key=lambda k: kinds_tris[k])]
+            fits = [min(BATCH_KINDS, key=lambda k: kinds_tris[k])]
         kind = fits[min(int(rng.uniform(1, 0, len(fits))[0]), len(fits) - 1)]
         chosen.append(kind)
         remaining -= kinds_tris[kind]
@@ -582,7 +582,7 @@ def batch_scene(rng: Rng, name: str, target_tris: float, width: int, height: int
     return _finish(name, parts, mats, inst, ubo, width, height)
 
 
-def batch_scenes(n=64, seed=2, tri_range=(1e3, 4e6), resolutions=C2_RESOLUTIONS, samples=(1, 4), depths=(1, 6),
+def batch_scenes(n=64, seed=2, tri_range=(1e3, 4e6), resolutions=BATCH_RESOLUTIONS, samples=(1, 4), depths=(1, 6),
                  hf_n=256) -> list:
     """The batched-rendering workload: ``n`` independent scenes with triangle counts log-uniform in
     ``tri_range``, resolution uniform over ``resolutions``, samples uniform in ``samples`` and
@@ -602,13 +602,13 @@ def batch_scenes(n=64, seed=2, tri_range=(1e3, 4e6), resolutions=C2_RESOLUTIONS,
     return out
 
 
-def c2_scenes() -> list:
+def default_batch_scenes() -> list:
     return batch_scenes()
 
 
 # ----------------------------------------------------------------------------- large terrain scenes
 
-SERVE_RESOLUTIONS = C2_RESOLUTIONS + ((3840, 2160),)
+SERVE_RESOLUTIONS = BATCH_RESOLUTIONS + ((3840, 2160),)
 _FIELD_CACHE: dict = {}
 
 

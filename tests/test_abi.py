@@ -47,15 +47,15 @@ def test_no_device_is_an_error_not_a_fallback(rg):
 
 
 def test_scene_generators_deterministic():
-    a, b = S.c0_scene(), S.c0_scene()
+    a, b = S.sphere_scene(), S.sphere_scene()
     assert a.tri_count == 61442 and len(a.materials) == 65
     assert np.array_equal(a.vertices, b.vertices) and np.array_equal(a.materials, b.materials)
     c = S.instanced_scene(width=64, height=36, counts=(3, 2, 1, 0, 2, 2, 1, 1), hf_n=16, ico_levels=(1, 1, 2, 2))
     assert len(c.instances) == 12 and set(c.instances["mask"]) == {0xFF}
 
 
-def test_c1_scene_sizes():
-    s = S.c1_scene()
+def test_game_frame_scene_sizes():
+    s = S.game_frame_scene()
     assert len(s.instances) == 1024
     assert 11_000_000 < s.instanced_tri_count < 13_000_000
     assert s.meshes["triCount"].tolist() == [1280, 5120, 20480, 81920, 4096, 4096, 130050, 130050]
@@ -67,16 +67,16 @@ def test_batch_scene_generators():
     assert len({(s.width, s.height) for s in scenes}) >= 3
     assert len({int(s.ubo["maxRecursions"][0]) for s in scenes}) >= 3
     assert all(1 <= int(s.ubo["numSamples"][0]) <= 3 for s in scenes)
-    c2 = S.c2_scenes()
-    assert len(c2) == 64
-    assert {(s.width, s.height) for s in c2} <= set(S.C2_RESOLUTIONS)
-    assert {int(s.ubo["numSamples"][0]) for s in c2} == {1, 2, 3, 4}
-    assert {int(s.ubo["maxRecursions"][0]) for s in c2} == {1, 2, 3, 4, 5, 6}
-    tris = np.array([s.instanced_tri_count for s in c2])
+    scs = S.default_batch_scenes()
+    assert len(scs) == 64
+    assert {(s.width, s.height) for s in scs} <= set(S.BATCH_RESOLUTIONS)
+    assert {int(s.ubo["numSamples"][0]) for s in scs} == {1, 2, 3, 4}
+    assert {int(s.ubo["maxRecursions"][0]) for s in scs} == {1, 2, 3, 4, 5, 6}
+    tris = np.array([s.instanced_tri_count for s in scs])
     assert tris.min() >= 1000 and tris.max() <= 4_000_000
     assert np.median(np.log10(tris)) > 3.5  # log-uniform over [3, 6.6]
-    again = S.c2_scenes()
-    assert all(np.array_equal(a.instances, b.instances) for a, b in zip(c2, again))
+    again = S.default_batch_scenes()
+    assert all(np.array_equal(a.instances, b.instances) for a, b in zip(scs, again))
 
 
 def test_job_layout(rg):

@@ -59,18 +59,18 @@ def test_lbvh_all_equal_keys(rg, orc):
 
 def small_two_level():
     return S.instanced_scene(width=96, height=54, counts=(6, 5, 3, 1, 4, 4, 1, 1), hf_n=32, ico_levels=(1, 2, 3, 3),
-                             num_samples=2, max_recursions=5, name="mini-c1")
+                             num_samples=2, max_recursions=5, name="mini-game-frame")
 
 
 @pytest.fixture(scope="module")
-def c0_pair(rg, orc):
-    sc = S.c0_scene()
+def spheres_pair(rg, orc):
+    sc = S.sphere_scene()
     rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES).prepare()
     return sc, rt, orc.OracleScene(sc)
 
 
 @pytest.fixture(scope="module")
-def c1_pair(rg, orc):
+def game_pair(rg, orc):
     # the LBVH TLAS, whose topology the oracle pins (the default binned-SAH TLAS is checked in
     # test_gpu_records.py)
     sc = small_two_level()
@@ -78,25 +78,25 @@ def c1_pair(rg, orc):
     return sc, rt, orc.OracleScene(sc)
 
 
-def test_blas_tlas_c0(c0_pair):
-    sc, rt, o = c0_pair
+def test_blas_tlas_spheres(spheres_pair):
+    sc, rt, o = spheres_pair
     lbvh_equal(rt.ctx.bvh(0), o.bvh(0))
     g, r = rt.ctx.bvh(-1), o.bvh(-1)
     assert np.array_equal(g["morton"], r["morton"]) and np.array_equal(g["order"], r["order"])
 
 
-def test_two_level_bvh(c1_pair):
-    sc, rt, o = c1_pair
+def test_two_level_bvh(game_pair):
+    sc, rt, o = game_pair
     for b in range(len(sc.meshes)):
         lbvh_equal(rt.ctx.bvh(b), o.bvh(b))
     lbvh_equal(rt.ctx.bvh(-1), o.bvh(-1))
     assert np.array_equal(rt.ctx.instance_inverse(len(sc.instances)), o.instance_inverse())
 
 
-@pytest.mark.parametrize("which", ["c0", "c1"])
-def test_closest_hit_bit_exact(which, c0_pair, c1_pair):
-    sc, rt, o = c0_pair if which == "c0" else c1_pair
-    if which == "c0":
+@pytest.mark.parametrize("which", ["spheres", "game-frame"])
+def test_closest_hit_bit_exact(which, spheres_pair, game_pair):
+    sc, rt, o = spheres_pair if which == "spheres" else game_pair
+    if which == "spheres":
         rays = np.concatenate([camera_rays(sc, stride=2), random_rays(20000, 3)])
     else:
         rays = np.concatenate([camera_rays(sc), random_rays(20000, 4, lo=(-60, 0, -60), hi=(60, 14, 60))])
@@ -106,16 +106,16 @@ def test_closest_hit_bit_exact(which, c0_pair, c1_pair):
     assert np.array_equal(ig, io)
     assert np.array_equal(tg, to)
     assert (ig[-5:, 0] == 0xFFFFFFFF).all()
-    assert (ig[:, 0] != 0xFFFFFFFF).mean() > (0.2 if which == "c0" else 0.03)
+    assert (ig[:, 0] != 0xFFFFFFFF).mean() > (0.2 if which == "spheres" else 0.03)
 
 
 def _gbuffers(rt):
     return [rt.ctx.download_image(k) for k in ("base", "normal", "rough")]
 
 
-@pytest.mark.parametrize("which", ["c0", "c1"])
-def test_gbuffer_and_frame_parity(which, c0_pair, c1_pair, orc):
-    sc, rt, o = c0_pair if which == "c0" else c1_pair
+@pytest.mark.parametrize("which", ["spheres", "game-frame"])
+def test_gbuffer_and_frame_parity(which, spheres_pair, game_pair, orc):
+    sc, rt, o = spheres_pair if which == "spheres" else game_pair
     rt.do_raytracing(fxaa=False)
     gb = _gbuffers(rt)
     st = rt.ctx.stats()
@@ -132,8 +132,8 @@ def test_gbuffer_and_frame_parity(which, c0_pair, c1_pair, orc):
 
 
 @pytest.mark.parametrize("show_alpha,fade", [(0, (0, 0, 0, 0)), (1, (0, 0, 0, 0)), (0, (0.2, 0.4, 0.6, 0.5))])
-def test_post_passes_bit_exact(c0_pair, orc, show_alpha, fade):
-    sc, rt, o = c0_pair
+def test_post_passes_bit_exact(spheres_pair, orc, show_alpha, fade):
+    sc, rt, o = spheres_pair
     ob, on, orr, _ = o.render()
     u = sc.ubo.copy()
     u["showAlpha"], u["fadeColor"] = show_alpha, fade

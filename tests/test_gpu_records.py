@@ -25,12 +25,12 @@ EMPTY = 0xFFFFFFFE
 
 def small_two_level():
     return S.instanced_scene(width=96, height=54, counts=(6, 5, 3, 1, 4, 4, 1, 1), hf_n=32, ico_levels=(1, 2, 3, 3),
-                             num_samples=2, max_recursions=5, name="mini-c1")
+                             num_samples=2, max_recursions=5, name="mini-game-frame")
 
 
-@pytest.fixture(scope="module", params=["c0", "c1"])
+@pytest.fixture(scope="module", params=["spheres", "game-frame"])
 def scene_pair(request, rg, orc):
-    sc = S.c0_scene() if request.param == "c0" else small_two_level()
+    sc = S.sphere_scene() if request.param == "spheres" else small_two_level()
     rt = rg.Raytracer(sc).prepare()
     yield sc, rt, orc.OracleScene(sc)
     rt.ctx.close()
@@ -119,7 +119,7 @@ def check_bvh2(bvh):
 def test_sah_tlas(rg, orc):
     """The default TLAS (binned SAH) is a valid BVH2 over all instances with a lower surface-area cost
     than the LBVH over the same instances, and both trace the same hits."""
-    sc = S.instanced_scene(width=96, height=54, num_samples=1, max_recursions=2, name="c1-instances")
+    sc = S.instanced_scene(width=96, height=54, num_samples=1, max_recursions=2, name="game-frame-instances")
     rt = rg.Raytracer(sc).prepare()
     rl = rg.Raytracer(sc, flags=rg.RG_FLAG_TLAS_LBVH).prepare()
     sah, lb = rt.ctx.bvh(-1), rl.ctx.bvh(-1)
