@@ -4,7 +4,8 @@
  * The library owns all device memory; inputs are copied; work is ordered on the context's stream
  * and rg_render() is asynchronous until rg_download()/rg_synchronize().  One context per host
  * thread, calls serialized per context (Raygun calls the renderer from its main loop only,
- * raygun/raygun.cpp:91-133).
+ * raygun/raygun.cpp:91-133); contexts on different threads run concurrently (the library's only
+ * process-wide state, launch-shape caches and a launch counter, is locked or atomic).
  *
  * Data layouts are byte-identical to Raygun's shared GLSL/C++ structs.
  */

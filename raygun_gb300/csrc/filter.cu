@@ -17,6 +17,7 @@
 // Descriptor conventions (no swizzle): core matrix = 8 rows x 16 bytes; the leading-byte offset is
 // the stride between core matrices along K, the stride-byte offset the stride along M / N.
 #include <algorithm>
+#include <atomic>
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -787,7 +788,8 @@ int ctas_per_sm(K kernel, int smem, uint32_t tmemCols, int threads) {
 template <int CIN, int COUT>
 cudaError_t conv_launch(const FilterConvArgs& a, cudaStream_t s) {
     using S = ConvShape<CIN, COUT>;
-    static int grid = 0;
+    static std::atomic<int> gridCache{0};
+    int grid = gridCache.load(std::memory_order_acquire);
     if (!grid) {
         cudaError_t e = cudaFuncSetAttribute(k_filter_conv<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
         if (e != cudaSuccess) return e;
@@ -795,6 +797,7 @@ cudaError_t conv_launch(const FilterConvArgs& a, cudaStream_t s) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         grid = sms * ctas_per_sm(k_filter_conv<CIN, COUT>, S::kSmem, S::kCols, kConvThreads);
+        gridCache.store(grid, std::memory_order_release);
     }
     if (a.B <= 0 || a.H <= 0 || a.W <= 0) return cudaSuccess;
     CUtensorMap map;
@@ -815,11 +818,11 @@ template <int CIN, int COUT>
 cudaError_t dw_launch(const bf16* x, const bf16* x2, const bf16* g, int B, int H, int W, float* partial, int ctas, int* status,
                       cudaStream_t s) {
     using S = DwShape<CIN, COUT>;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> attr{false};
+    if (!attr.load(std::memory_order_acquire)) {
         cudaError_t e = cudaFuncSetAttribute(k_filter_dw<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
         if (e != cudaSuccess) return e;
-        attr = true;
+        attr.store(true, std::memory_order_release);
     }
     k_filter_dw<CIN, COUT><<<dim3(ctas, S::kGroups), 128, S::kSmem, s>>>(x, x2, g, B, H, W, partial, status);
     count_launch();

@@ -12,6 +12,8 @@
 // of the reference image (RGBA16F, R8_SNORM for the transition mask) so the values match the
 // reference's pass-by-pass evaluation.  Out-of-image loads read 0 as robust image access does.
 // FXAA runs as a second kernel: its edge search reaches ~27 pixels, too far for a halo.
+#include <atomic>
+
 #include "rg_internal.cuh"
 
 namespace rg {
@@ -382,12 +384,12 @@ cudaError_t r32_to_rgba(const float* in, float4* out, size_t n, cudaStream_t s) 
 }
 
 cudaError_t launch_rough_post(const PostParams& p, cudaStream_t s) {
-    static bool attr = false;
+    static std::atomic<bool> attr{false};
     const int smem = (int)sizeof(RoughSmem);
-    if (!attr) {
+    if (!attr.load(std::memory_order_acquire)) {
         cudaError_t e = cudaFuncSetAttribute(k_rough_post, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        attr = true;
+        attr.store(true, std::memory_order_release);
     }
     dim3 grid((p.W + TW - 1) / TW, (p.H + TH - 1) / TH);
     k_rough_post<<<grid, kPostThreads, smem, s>>>(p);

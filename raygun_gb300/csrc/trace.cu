@@ -20,7 +20,9 @@
 // GLSL-undefined cases follow fixed policies: r/(tr+r) with tr+r == 0 -> 0; pow(x, n) with
 // integer n -> repeated multiply; a zero direction (refract at total internal reflection) -> no
 // traversal, miss shader; clamp/min/max treat a NaN operand as absent (fminf/fmaxf).
+#include <atomic>
 #include <cstring>
+#include <mutex>
 
 #include "rg_internal.cuh"
 
@@ -1566,9 +1568,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(const DevScene sc,
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s) {
-    static int gridBlocks[2] = {0, 0};
+    static std::atomic<int> gridBlocks[2];  // zero-initialised (static storage); first use computes them
     const int c = p.countVisits ? 1 : 0;
-    if (!gridBlocks[c]) {
+    if (!gridBlocks[c].load(std::memory_order_acquire)) {
         int dev = 0, sms = 0, perSm = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1576,12 +1578,13 @@ cudaError_t launch_trace(const TraceParams& p, cudaStream_t s) {
             e = c ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace<true>, kTraceThreads, 0)
                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace<false>, kTraceThreads, 0);
         if (e != cudaSuccess) return e;
-        gridBlocks[c] = sms * (perSm > 0 ? perSm : 1);
+        gridBlocks[c].store(sms * (perSm > 0 ? perSm : 1), std::memory_order_release);
     }
+    const int gBlocks = gridBlocks[c].load(std::memory_order_acquire);
     cudaError_t e = cudaMemsetAsync(p.workCounter, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    if (p.countVisits) k_trace<true><<<gridBlocks[c], kTraceThreads, 0, s>>>(p);
-    else k_trace<false><<<gridBlocks[c], kTraceThreads, 0, s>>>(p);
+    if (p.countVisits) k_trace<true><<<gBlocks, kTraceThreads, 0, s>>>(p);
+    else k_trace<false><<<gBlocks, kTraceThreads, 0, s>>>(p);
     count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -1599,11 +1602,14 @@ static int persistent_grid(const void* fn, int threads, int smem) {
     return sms * (perSm > 0 ? perSm : 1);
 }
 
-// persistent grid sizes, one per kernel (computed on first use)
+// persistent grid sizes, one per kernel (computed on first use; contexts on several host threads
+// share the table)
 static int grid_of(const void* fn, int threads) {
+    static std::mutex mu;
     static const void* fns[64];
     static int grids[64];
     static int n = 0;
+    std::lock_guard<std::mutex> lock(mu);
     for (int k = 0; k < n; ++k)
         if (fns[k] == fn) return grids[k];
     const int g = persistent_grid(fn, threads, 0);

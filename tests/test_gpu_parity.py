@@ -282,3 +282,40 @@ def test_vertex_material_edit_without_refit(rg, orc):
     ob, on, orr, _ = o.render()
     assert_image_close(after, orc.post(sc.ubo, ob, on, orr), "after vertex material edit")
     assert np.abs(after - before).max() > 0.1
+
+
+def test_contexts_on_two_host_threads(rg):
+    """One context per host thread (the reference's single-threaded use, raygun.cpp:91-133, once per
+    thread): two contexts rendering at the same time on two threads give the frames each gives
+    alone, bit for bit."""
+    import threading
+    scs = [S.spheres_scene(n_spheres=8, width=96, height=54, num_samples=2, max_recursions=4, seed=21),
+           S.instanced_scene(width=96, height=54, counts=(3, 2, 1, 1, 2, 2, 1, 1), hf_n=32, ico_levels=(1, 2, 3, 3),
+                             num_samples=2, max_recursions=5, name="mini-game-frame-threads")]
+    alone = []
+    for sc in scs:
+        rt = rg.Raytracer(sc).prepare()
+        alone.append(rt.render())
+        rt.ctx.close()
+    rts = [rg.Raytracer(sc).prepare() for sc in scs]
+    out = [[None] * 4 for _ in scs]
+    errors = []
+
+    def run(k):
+        try:
+            for i in range(4):
+                out[k][i] = rts[k].render()
+        except Exception as e:  # reported on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(len(scs))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for k in range(len(scs)):
+        for i in range(4):
+            assert np.array_equal(out[k][i], alone[k]), (k, i)
+    for rt in rts:
+        rt.ctx.close()
