@@ -46,6 +46,8 @@ typedef struct {
 #define RG_FLAG_HOST_LOOP 16u    /* rg_render_batch: host-polled round loop instead of the CUDA graph */
 #define RG_FLAG_TLAS_LBVH 32u    /* build the TLAS as an LBVH (Morton order) instead of by binned SAH; TLASes of more
                                     than 8192 instances are always LBVHs */
+#define RG_FLAG_BLAS_LBVH 64u    /* build BLASes as LBVHs instead of by binned SAH; BLASes of more than 2^18 triangles,
+                                    or whose SAH tree would be deeper than 28 levels, are always LBVHs */
 
 /* resources/shaders/vertex.def:3-7 (render/vertex.hpp:27-29): 32 B */
 typedef struct {

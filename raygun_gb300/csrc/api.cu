@@ -320,7 +320,8 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
     CK(cudaEventRecord(fe->ev[EV_AS0], c->stream));
     CK(setup_instances(c->sc->instIn.as<rg_instance>(), n, c->sc->blasTable.as<DevBlas>(), (uint32_t)c->sc->blas.size(),
                        c->sc->instDev.as<DevInstance>(), c->sc->tlas.primBoxes.as<float>(), c->stream));
-    if (!(c->flags & RG_FLAG_TLAS_LBVH) && n > 1 && n <= kSahMaxPrims) CK(tlas_sah_build(buffers(c, c->sc->tlas), c->stream));
+    if (!(c->flags & RG_FLAG_TLAS_LBVH) && n > 1 && n <= kSahMaxPrims)
+        CK(sah_build(buffers(c, c->sc->tlas), false, 0xFFFFFFFFu, nullptr, c->stream));
     else CK(lbvh_build(buffers(c, c->sc->tlas), c->stream));
     CK(wide_records(buffers(c, c->sc->tlas), c->sc->tlas.wide.as<WideNode>(), c->stream));
     CK(inst_records(c->sc->tlas.order.as<uint32_t>(), n, c->sc->instDev.as<DevInstance>(), c->sc->blasTable.as<DevBlas>(),
@@ -539,7 +540,18 @@ rg_status rg_build_blas(rg_ctx* c, uint32_t vOff, uint32_t iOff, uint32_t triCou
     TRY(ensure(c, r.tris, 48ull * (triCount ? triCount : 1)));
     if (triCount) {
         CK(tri_boxes(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), vOff, iOff, triCount, r.bvh.primBoxes.as<float>(), c->stream));
-        CK(lbvh_build(buffers(c, r.bvh), c->stream));
+        // binned SAH where it fits (once per scene load; refits keep its topology), else the LBVH
+        bool sah = !(c->flags & RG_FLAG_BLAS_LBVH) && triCount > 1 && triCount <= kSahBlasMaxPrims;
+        if (sah) {
+            TRY(ensure(c, c->tmpD, 4));
+            uint32_t levels = 0;
+            CK(sah_build(buffers(c, r.bvh), true, kSahMaxLevels, c->tmpD.as<uint32_t>(), c->stream));
+            CK(cudaMemcpyAsync(&levels, c->tmpD.p, 4, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            sah = levels <= kSahMaxLevels;
+            if (sah) CK(cudaMemsetAsync(r.bvh.morton.p, 0, 4ull * triCount, c->stream));  // no Morton order in an SAH tree
+        }
+        if (!sah) CK(lbvh_build(buffers(c, r.bvh), c->stream));
         CK(wide_records(buffers(c, r.bvh), r.bvh.wide.as<WideNode>(), c->stream));
         CK(tri_records(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), vOff, iOff, r.bvh.order.as<uint32_t>(), triCount,
                        r.tris.as<float4>(), c->stream));

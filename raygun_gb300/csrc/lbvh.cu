@@ -342,13 +342,16 @@ __global__ void k_wide_records(const float* __restrict__ primBoxes, const uint32
     out[i] = w;
 }
 
-// ---- binned-SAH TLAS ------------------------------------------------------------------------------
-// One CTA builds a BVH2 over at most kSahMaxPrims instance boxes, top-down, level by level: each warp
-// takes a node task (a range of the order array), reduces the range's box and centroid box, bins the
-// centroids into 16 bins per axis (shared-memory atomics on order-preserving integer images of the
-// bounds), evaluates the 45 surface-area-heuristic splits, partitions the range stably with ballots,
-// and emits its children (single primitives become leaf refs, the rest next-level tasks).  The
-// result has the LBVH's layout (order, left, right, nodeBoxes), so records and traversal are shared.
+// ---- binned-SAH BVH2 (TLAS, and BLASes up to kSahBlasMaxPrims triangles) ------------------------
+// One CTA builds a BVH2 over the primitive boxes, top-down, level by level: each warp takes a node
+// task (a range of the order array), reduces the range's box and centroid box, bins the centroids into
+// 16 bins per axis (shared-memory atomics on order-preserving integer images of the bounds), evaluates
+// the 45 surface-area-heuristic splits, partitions the range stably with ballots, and emits its
+// children (single primitives become leaf refs, the rest next-level tasks).  Every split leaves both
+// sides non-empty, so each level shortens every range and the build ends after at most n - 1 levels.
+// Internal nodes are numbered in level order (a level's tasks follow the previous levels' nodes), so
+// a task is just its range.  The result has the LBVH's layout (order, left, right, nodeBoxes), so
+// records, refits and traversal are shared.
 constexpr int kSahBins = 16;
 constexpr int kSahWarps = 32;
 
@@ -362,20 +365,23 @@ __device__ __forceinline__ float half_area3(const float* lo, const float* hi) {
     return dx * dy + dy * dz + dz * dx;
 }
 
-__global__ void __launch_bounds__(kSahWarps * 32, 1) k_tlas_sah(const float* __restrict__ boxes, uint32_t n, uint32_t* __restrict__ order,
-                                                                uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
-                                                                uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
-                                                                uint2* __restrict__ tasksA, uint2* __restrict__ tasksB) {
+__global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __restrict__ boxes, uint32_t n, uint32_t* __restrict__ order,
+                                                                 uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
+                                                                 uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
+                                                                 uint2* __restrict__ tasksA, uint2* __restrict__ tasksB,
+                                                                 uint32_t maxLevels, uint32_t* __restrict__ levelsOut) {
     __shared__ int bLo[kSahWarps][3][kSahBins][3], bHi[kSahWarps][3][kSahBins][3];
     __shared__ int bCnt[kSahWarps][3][kSahBins];
-    __shared__ uint32_t nCur, nNext, nodeCounter;
+    __shared__ uint32_t nCur, nNext, baseCur, baseNext, levels;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) order[i] = i;
     if (threadIdx.x == 0) {
-        tasksA[0] = make_uint2(n << 16, 0u);  // range [0, n), node 0
+        tasksA[0] = make_uint2(0u, n);  // range [0, n): node 0
         nCur = 1;
         nNext = 0;
-        nodeCounter = 1;
+        baseCur = 0;   // node id of the current level's first task
+        baseNext = 1;  // node id of the next level's first task
+        levels = 0;
     }
     __syncthreads();
     uint2* cur = tasksA;
@@ -383,9 +389,13 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_tlas_sah(const float* __r
     for (;;) {
         const uint32_t count = nCur;
         if (count == 0) break;
+        if (levels >= maxLevels) {  // deeper than the caller accepts: report and stop (the tree is unfinished)
+            if (threadIdx.x == 0 && levelsOut) *levelsOut = 0xFFFFFFFFu;
+            return;
+        }
         for (uint32_t t = warp; t < count; t += kSahWarps) {
             const uint2 tk = cur[t];
-            const uint32_t b = tk.x & 0xFFFFu, e = tk.x >> 16, node = tk.y;
+            const uint32_t b = tk.x, e = tk.y, node = baseCur + t;
             float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
             float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
             for (uint32_t i = b + lane; i < e; i += 32) {
@@ -520,9 +530,9 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_tlas_sah(const float* __r
                     if (re0[c] - rb0[c] == 1) {
                         ref[c] = kLeaf | rb0[c];
                     } else {
-                        const uint32_t id = atomicAdd(&nodeCounter, 1u);
-                        nxt[atomicAdd(&nNext, 1u)] = make_uint2(rb0[c] | (re0[c] << 16), id);
-                        ref[c] = id;
+                        const uint32_t idx = atomicAdd(&nNext, 1u);
+                        nxt[idx] = make_uint2(rb0[c], re0[c]);
+                        ref[c] = baseNext + idx;
                     }
                 }
                 left[node] = ref[0];
@@ -532,14 +542,30 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_tlas_sah(const float* __r
         }
         __syncthreads();
         if (threadIdx.x == 0) {
+            baseCur = baseNext;
+            baseNext += nNext;
             nCur = nNext;
             nNext = 0;
+            ++levels;
         }
         uint2* sw = cur;
         cur = nxt;
         nxt = sw;
         __syncthreads();
     }
+    if (threadIdx.x == 0 && levelsOut) *levelsOut = levels;
+}
+
+// parents of a BVH2 in the LBVH layout (internal node i at parents[i], the leaf at sorted position k
+// at parents[n - 1 + k], the root's 0xFFFFFFFF), which the bottom-up refit walks
+__global__ void k_parents(const uint32_t* __restrict__ left, const uint32_t* __restrict__ right, uint32_t n,
+                          uint32_t* __restrict__ parents) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1 >= n) return;
+    const uint32_t L = left[i], R = right[i];
+    parents[(L & kLeaf) ? (n - 1) + (L & ~kLeaf) : L] = i;
+    parents[(R & kLeaf) ? (n - 1) + (R & ~kLeaf) : R] = i;
+    if (i == 0) parents[0] = 0xFFFFFFFFu;
 }
 
 // ---- instances ----------------------------------------------------------------------------------
@@ -638,13 +664,17 @@ cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t tlas_sah_build(const LbvhBuffers& b, cudaStream_t s) {
+cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t maxLevels, uint32_t* levels, cudaStream_t s) {
     if (b.n <= 1) return cudaSuccess;
-    if (b.n > kSahMaxPrims) return cudaErrorInvalidValue;
     // scratch: the sort buffers (n words each); at most n / 2 tasks per level, 2 words each
-    k_tlas_sah<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes,
-                                             reinterpret_cast<uint2*>(b.valsA), reinterpret_cast<uint2*>(b.valsB));
+    k_sah_build<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes,
+                                              reinterpret_cast<uint2*>(b.valsA), reinterpret_cast<uint2*>(b.valsB), maxLevels,
+                                              levels);
     count_launch();
+    if (parents) {
+        k_parents<<<blocks(b.n - 1, 256), 256, 0, s>>>(b.left, b.right, b.n, b.parents);
+        count_launch();
+    }
     return cudaGetLastError();
 }
 

@@ -140,9 +140,15 @@ cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s);  // topology kept, primBoxes changed
 cudaError_t wide_records(const LbvhBuffers& b, WideNode* out, cudaStream_t s);  // after build / refit
 // binned-SAH BVH2 over b.primBoxes in the LBVH's layout (order, left, right, nodeBoxes), one CTA;
-// n <= kSahMaxPrims
+// parents (for refits) on request.  *levels (device word, nullable) receives the number of levels, or
+// 0xFFFFFFFF when the tree would have more than maxLevels (the build then stops unfinished).  The
+// TLAS uses it up to kSahMaxPrims instances (it is rebuilt every frame), BLASes up to
+// kSahBlasMaxPrims triangles (built once per scene load) when the tree has at most kSahMaxLevels
+// levels (within the traversal stack's reach), the LBVH otherwise.
 constexpr uint32_t kSahMaxPrims = 8192;
-cudaError_t tlas_sah_build(const LbvhBuffers& b, cudaStream_t s);
+constexpr uint32_t kSahBlasMaxPrims = 1u << 18;
+constexpr uint32_t kSahMaxLevels = 28;
+cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t maxLevels, uint32_t* levels, cudaStream_t s);
 cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes,
                       cudaStream_t s);
 cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, const uint32_t* order, uint32_t n,

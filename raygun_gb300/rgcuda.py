@@ -25,6 +25,7 @@ RG_FLAG_MEGAKERNEL = 4
 RG_FLAG_KERNEL_TIMING = 8
 RG_FLAG_HOST_LOOP = 16
 RG_FLAG_TLAS_LBVH = 32
+RG_FLAG_BLAS_LBVH = 64
 IMAGES = {"final": 0, "base": 1, "normal": 2, "rough": 3, "rough_transition": 4, "rough_colors_a": 5,
           "rough_colors_b": 6, "pre_fxaa": 7, "filter_out": 8}
 

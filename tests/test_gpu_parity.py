@@ -65,16 +65,18 @@ def small_two_level():
 @pytest.fixture(scope="module")
 def spheres_pair(rg, orc):
     sc = S.sphere_scene()
-    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES).prepare()
+    # the LBVH BLAS, whose topology the oracle pins (the default binned-SAH BLAS is checked in
+    # test_gpu_records.py)
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES | rg.RG_FLAG_BLAS_LBVH).prepare()
     return sc, rt, orc.OracleScene(sc)
 
 
 @pytest.fixture(scope="module")
 def game_pair(rg, orc):
-    # the LBVH TLAS, whose topology the oracle pins (the default binned-SAH TLAS is checked in
-    # test_gpu_records.py)
+    # the LBVH TLAS and BLASes, whose topology the oracle pins (the default binned-SAH trees are
+    # checked in test_gpu_records.py)
     sc = small_two_level()
-    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES | rg.RG_FLAG_TLAS_LBVH).prepare()
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES | rg.RG_FLAG_TLAS_LBVH | rg.RG_FLAG_BLAS_LBVH).prepare()
     return sc, rt, orc.OracleScene(sc)
 
 
@@ -150,7 +152,7 @@ def test_post_passes_bit_exact(spheres_pair, orc, show_alpha, fade):
 
 def test_animation_refit_and_tlas_rebuild(rg, orc):
     sc = small_two_level()
-    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_TLAS_LBVH).prepare()
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_TLAS_LBVH | rg.RG_FLAG_BLAS_LBVH).prepare()
     o = orc.OracleScene(sc)
     anim = S.FrameAnimator(sc, seed=7, refit_prob=0.5)
     for frame in range(3):
@@ -319,3 +321,26 @@ def test_contexts_on_two_host_threads(rg):
             assert np.array_equal(out[k][i], alone[k]), (k, i)
     for rt in rts:
         rt.ctx.close()
+
+
+def test_large_blas_is_lbvh(rg, orc):
+    """BLASes of more than 2^18 triangles are built as LBVHs (the binned-SAH builder runs in one CTA
+    and is kept for meshes up to that size): the oracle's LBVH, bit for bit."""
+    g = 364  # 2 * 363^2 = 263,538 triangles
+    ys, xs = np.meshgrid(np.arange(g, dtype=np.float32), np.arange(g, dtype=np.float32), indexing="ij")
+    rng = np.random.RandomState(17)
+    verts = np.zeros(g * g, S.VERTEX)
+    verts["position"] = np.stack([xs.ravel(), rng.uniform(0, 0.5, g * g).astype(np.float32), ys.ravel()], 1)
+    verts["normal"] = (0, 1, 0)
+    q = (np.arange(g - 1)[:, None] * g + np.arange(g - 1)[None, :]).ravel().astype(np.uint32)
+    idx = np.stack([q, q + g, q + 1, q + 1, q + g, q + g + 1], 1).astype(np.uint32).ravel()
+    n = len(idx) // 3
+    assert n > (1 << 18)
+    sc = S.spheres_scene(n_spheres=1, width=8, height=8)
+    ctx = rg.Context()
+    ctx.upload_geometry(verts, idx, sc.materials)
+    b = ctx.build_blas(0, 0, n)
+    p = verts["position"][idx.astype(np.int64)].reshape(n, 3, 3)
+    boxes = np.ascontiguousarray(np.concatenate([p.min(1), p.max(1)], 1), np.float32)
+    lbvh_equal(ctx.bvh(b), orc.lbvh(boxes))
+    ctx.close()

@@ -176,3 +176,48 @@ def test_records_follow_refit(rg, orc):
     to, io = o.trace(rays)
     assert np.array_equal(ig, io) and np.array_equal(tg, to)
     rt.ctx.close()
+
+
+def test_sah_blas(rg, orc):
+    """The default BLASes (binned SAH) are valid BVH2s with a lower surface-area cost than the LBVHs
+    over the same triangles, their records hold the exact boxes, they follow refits, and they trace
+    the oracle's hits."""
+    sc = small_two_level()
+    rt = rg.Raytracer(sc).prepare()
+    rl = rg.Raytracer(sc, flags=rg.RG_FLAG_BLAS_LBVH).prepare()
+    cost = lambda b: half_area(b["nodeboxes"]).sum() / half_area(b["nodeboxes"][0])
+    tot_sah = tot_lbvh = 0.0
+    for b in range(len(sc.meshes)):
+        sah, lb = rt.ctx.bvh(b), rl.ctx.bvh(b)
+        if len(sah["order"]) < 2:
+            continue
+        check_bvh2(sah)
+        check_records(rt.ctx.bvh_records(b), sah, tri_boxes(sc, b)[sah["order"]])
+        tot_sah += cost(sah)
+        tot_lbvh += cost(lb)
+    assert tot_sah < 0.97 * tot_lbvh, (tot_sah, tot_lbvh)
+    o = orc.OracleScene(sc)
+    rays = np.concatenate([camera_rays(sc), random_rays(20000, 12, lo=(-60, 0, -60), hi=(60, 14, 60)),
+                           degenerate_rays(sc, 4000, 13)])
+    tg, ig = rt.ctx.trace_rays(rays)
+    to, io = o.trace(rays)
+    assert np.array_equal(ig, io) and np.array_equal(tg, to)
+    # refit of the SAH topology: records carry the moved boxes and hits still match
+    anim = S.FrameAnimator(sc, seed=5, refit_prob=1.0)
+    refits = anim.step()
+    for b, vo, nv in refits:
+        rt.ctx.update_vertices(vo, sc.vertices[vo:vo + nv])
+        rt.ctx.refit_blas(rt.blas_ids[b])
+        o.refit(b, sc.vertices[vo:vo + nv], vo)
+    rt.setup_top_level_as()
+    o.set_instances(sc.instances)
+    for b, _, _ in refits:
+        bvh = rt.ctx.bvh(b)
+        if len(bvh["order"]) > 1:
+            check_bvh2(bvh)
+            check_records(rt.ctx.bvh_records(b), bvh, tri_boxes(sc, b)[bvh["order"]])
+    tg, ig = rt.ctx.trace_rays(rays)
+    to, io = o.trace(rays)
+    assert np.array_equal(ig, io) and np.array_equal(tg, to)
+    rt.ctx.close()
+    rl.ctx.close()
