@@ -312,13 +312,14 @@ rg_status rg_autotune_batch(rg_ctx* ctx, const rg_job* jobs, uint32_t n, uint32_
 
 /* ---- parity / inspection entry points (no reference counterpart: the Vulkan driver's BVHs are
  * opaque) ---- */
-/* LBVH of a BLAS (blas) or of the TLAS (blas = 0xFFFFFFFF): Morton codes per primitive, sorted
- * order, children of the n-1 internal nodes (bit 31 = leaf, payload = sorted position) and the
- * internal node boxes (6 floats: lo xyz, hi xyz).  Pointers may be NULL.  *n_out = primitive count. */
+/* BVH2 of a BLAS (blas) or of the TLAS (blas = 0xFFFFFFFF): Morton codes per primitive (LBVHs; zero
+ * for a binned-SAH BLAS, unspecified for a binned-SAH TLAS), sorted order, children of the n-1
+ * internal nodes (bit 31 = leaf, payload = sorted position) and the internal node boxes (6 floats: lo
+ * xyz, hi xyz).  Pointers may be NULL.  *n_out = primitive count. */
 rg_status rg_bvh_info(rg_ctx* ctx, uint32_t blas, uint32_t* n_out, uint32_t* morton, uint32_t* order, uint32_t* left,
                       uint32_t* right, float* nodeboxes);
 /* The traversal's 4-wide records of a BLAS (blas) or of the TLAS (blas = 0xFFFFFFFF), one per
- * internal LBVH node, 112 bytes each: float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4] (the
+ * internal BVH2 node, 112 bytes each: float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4] (the
  * boxes of the node's grandchildren, a leaf child standing in for its own slot); uint32 ref[4] (bit 31 =
  * leaf; 0xFFFFFFFE = empty slot, box lo = +inf, hi = -inf).  Copies min(capacity, n - 1) records to
  * out (may be NULL); *n_out = n - 1. */
