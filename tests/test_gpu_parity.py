@@ -344,3 +344,25 @@ def test_large_blas_is_lbvh(rg, orc):
     boxes = np.ascontiguousarray(np.concatenate([p.min(1), p.max(1)], 1), np.float32)
     lbvh_equal(ctx.bvh(b), orc.lbvh(boxes))
     ctx.close()
+
+
+def test_deep_sah_blas_falls_back_to_lbvh(rg, orc):
+    """Small triangles at x = 17^k: every surface-area split takes one triangle off the far end, so
+    the binned-SAH tree would have 29 levels. Past 28 the build stops and the BLAS is the LBVH
+    instead, bit for bit the oracle's."""
+    n = 30
+    verts = np.zeros(3 * n, S.VERTEX)
+    for k in range(n):
+        x = np.float32(17.0 ** k)
+        verts["position"][3 * k:3 * k + 3] = [(x, 0, 0), (x, 0, 0.5), (x, 0.5, 0)]
+        verts["normal"][3 * k:3 * k + 3] = (1, 0, 0)
+    assert np.isfinite(verts["position"]).all()
+    idx = np.arange(3 * n, dtype=np.uint32)
+    sc = S.spheres_scene(n_spheres=1, width=8, height=8)
+    ctx = rg.Context()
+    ctx.upload_geometry(verts, idx, sc.materials)
+    b = ctx.build_blas(0, 0, n)
+    p = verts["position"].reshape(n, 3, 3)
+    boxes = np.ascontiguousarray(np.concatenate([p.min(1), p.max(1)], 1), np.float32)
+    lbvh_equal(ctx.bvh(b), orc.lbvh(boxes))
+    ctx.close()
