@@ -35,6 +35,8 @@ def lib():
         P, U32, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
         L.orc_lbvh.argtypes = [P, U32, P, P, P, P, P]
         L.orc_lbvh.restype = U32
+        L.orc_sah.argtypes = [P, U32, U32, P, P, P, P]
+        L.orc_sah.restype = U32
         L.orc_scene_create.argtypes = [P, U32, P, U32, P, U32, P, U32, P, U32]
         L.orc_scene_create.restype = P
         L.orc_scene_destroy.argtypes = [P]
@@ -71,6 +73,47 @@ def lbvh(boxes: np.ndarray):
     lib().orc_lbvh(_p(boxes), n, _p(out["morton"]), _p(out["order"]), _p(out["left"]), _p(out["right"]),
                    _p(out["nodeboxes"]))
     return out
+
+
+def sah(boxes: np.ndarray, max_levels: int = 0xFFFFFFFF):
+    """Binned-SAH BVH2 over boxes (n, 6) -> dict(order, left, right, nodeboxes, levels), or None when
+    the tree would have more than max_levels levels."""
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    n = len(boxes)
+    out = dict(order=np.zeros(n, np.uint32), left=np.zeros(max(n - 1, 0), np.uint32),
+               right=np.zeros(max(n - 1, 0), np.uint32), nodeboxes=np.zeros((max(n - 1, 0), 6), np.float32))
+    levels = lib().orc_sah(_p(boxes), n, max_levels, _p(out["order"]), _p(out["left"]), _p(out["right"]),
+                           _p(out["nodeboxes"]))
+    if levels == 0xFFFFFFFF:
+        return None
+    out["levels"] = int(levels)
+    return out
+
+
+def same_tree(a, b):
+    """Two BVH2s in the LBVH layout are the same tree when their leaf order agrees and a walk from both
+    roots meets the same structure and node boxes; internal node numbering may differ (the GPU
+    numbers a level's nodes in the order its warps emit them)."""
+    if not np.array_equal(a["order"], b["order"]):
+        return False
+    n = len(a["order"])
+    if n <= 1:
+        return True
+    LEAF = 0x80000000
+    st = [(0, 0)]
+    while st:
+        i, j = st.pop()
+        if not np.array_equal(a["nodeboxes"][i], b["nodeboxes"][j]):
+            return False
+        for ca, cb in ((int(a["left"][i]), int(b["left"][j])), (int(a["right"][i]), int(b["right"][j]))):
+            if (ca & LEAF) != (cb & LEAF):
+                return False
+            if ca & LEAF:
+                if ca != cb:
+                    return False
+            else:
+                st.append((ca, cb))
+    return True
 
 
 class OracleScene:

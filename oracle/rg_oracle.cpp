@@ -311,6 +311,149 @@ static void lbvh_build(Lbvh& b, const std::vector<Box>& prim) {
     lbvh_refit(b);
 }
 
+// Binned-SAH BVH2 (the default BLAS and TLAS builder of the CUDA library), in the LBVH's layout.  Top
+// down, level by level: a node's range of the order array gets its box and centroid box; centroids
+// fall into 16 bins per axis (bin = trunc((c - clo) * 16 / ext), clamped); the 45 splits between
+// bins are scored by half-area(left) * count(left) + half-area(right) * count(right) and the
+// cheapest wins, ties to the lowest (axis, split); the range is partitioned stably; a range with no
+// usable split (coincident centroids, or every cost infinite) is halved.  Children of one primitive
+// are leaf refs.  Internal nodes are numbered in level order, tasks of a level in order (the GPU
+// numbers a level's nodes in the order its warps emit them, so trees compare up to that numbering).
+// Returns the number of levels, or 0xFFFFFFFF when it would exceed maxLevels (tree unfinished).
+static float half_area3(const float* lo, const float* hi) {
+    const float dx = std::fmax(hi[0] - lo[0], 0.0f), dy = std::fmax(hi[1] - lo[1], 0.0f), dz = std::fmax(hi[2] - lo[2], 0.0f);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+static uint32_t sah_build(Lbvh& l, const std::vector<Box>& prim, uint32_t maxLevels) {
+    const int kBins = 16;
+    const uint32_t n = (uint32_t)prim.size();
+    l.n = n;
+    l.order.resize(n);
+    for (uint32_t i = 0; i < n; ++i) l.order[i] = i;
+    l.left.assign(n > 1 ? n - 1 : 0, 0u);
+    l.right.assign(n > 1 ? n - 1 : 0, 0u);
+    l.nodeBox.assign(n > 1 ? n - 1 : 0, Box{});
+    l.leafBox.resize(n);
+    if (n <= 1) {
+        for (uint32_t i = 0; i < n; ++i) l.leafBox[i] = prim[i];
+        return 0;
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> cur{{0u, n}}, nxt;
+    std::vector<uint32_t> tmp(n);
+    uint32_t baseCur = 0, baseNext = 1, levels = 0;
+    while (!cur.empty()) {
+        if (levels >= maxLevels) return 0xFFFFFFFFu;
+        nxt.clear();
+        for (uint32_t t = 0; t < cur.size(); ++t) {
+            const uint32_t b = cur[t].first, e = cur[t].second, node = baseCur + t;
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (uint32_t i = b; i < e; ++i) {
+                const Box& x = prim[l.order[i]];
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::fmin(lo[a], x.lo[a]);
+                    hi[a] = std::fmax(hi[a], x.hi[a]);
+                    const float c = 0.5f * (x.lo[a] + x.hi[a]);
+                    clo[a] = std::fmin(clo[a], c);
+                    chi[a] = std::fmax(chi[a], c);
+                }
+            }
+            for (int a = 0; a < 3; ++a) {
+                l.nodeBox[node].lo[a] = lo[a];
+                l.nodeBox[node].hi[a] = hi[a];
+            }
+            float scale[3];
+            for (int a = 0; a < 3; ++a) {
+                const float ext = chi[a] - clo[a];
+                scale[a] = ext > 0.0f ? (float)kBins / ext : 0.0f;
+            }
+            auto bin_of = [&](const Box& x, int a) {
+                const float c = 0.5f * (x.lo[a] + x.hi[a]);
+                return std::max(0, std::min((int)((c - clo[a]) * scale[a]), kBins - 1));
+            };
+            int cnt[3][kBins] = {};
+            float blo[3][kBins][3], bhi[3][kBins][3];
+            for (int a = 0; a < 3; ++a)
+                for (int k = 0; k < kBins; ++k)
+                    for (int c = 0; c < 3; ++c) {
+                        blo[a][k][c] = INFINITY;
+                        bhi[a][k][c] = -INFINITY;
+                    }
+            for (uint32_t i = b; i < e; ++i) {
+                const Box& x = prim[l.order[i]];
+                for (int a = 0; a < 3; ++a) {
+                    if (scale[a] <= 0.0f) continue;
+                    const int k = bin_of(x, a);
+                    cnt[a][k]++;
+                    for (int c = 0; c < 3; ++c) {
+                        blo[a][k][c] = std::fmin(blo[a][k][c], x.lo[c]);
+                        bhi[a][k][c] = std::fmax(bhi[a][k][c], x.hi[c]);
+                    }
+                }
+            }
+            float bestCost = INFINITY;
+            int bestCand = -1;
+            for (int cand = 0; cand < 3 * (kBins - 1); ++cand) {
+                const int a = cand / (kBins - 1), sp = cand % (kBins - 1) + 1;
+                if (scale[a] <= 0.0f) continue;
+                float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                int nl = 0, nr = 0;
+                for (int k = 0; k < kBins; ++k) {
+                    if (!cnt[a][k]) continue;
+                    float* X0 = k < sp ? L0 : R0;
+                    float* X1 = k < sp ? L1 : R1;
+                    for (int c = 0; c < 3; ++c) {
+                        X0[c] = std::fmin(X0[c], blo[a][k][c]);
+                        X1[c] = std::fmax(X1[c], bhi[a][k][c]);
+                    }
+                    if (k < sp) nl += cnt[a][k];
+                    else nr += cnt[a][k];
+                }
+                if (!nl || !nr) continue;
+                const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
+                if (cost < bestCost) {
+                    bestCost = cost;
+                    bestCand = cand;
+                }
+            }
+            uint32_t mid = b + (e - b) / 2;
+            if (bestCand >= 0) {
+                const int a = bestCand / (kBins - 1), sp = bestCand % (kBins - 1) + 1;
+                uint32_t nl = 0;
+                for (uint32_t i = b; i < e; ++i) nl += bin_of(prim[l.order[i]], a) < sp ? 1u : 0u;
+                uint32_t lb = 0, rb = 0;
+                for (uint32_t i = b; i < e; ++i) {
+                    const uint32_t p = l.order[i];
+                    if (bin_of(prim[p], a) < sp) tmp[b + lb++] = p;
+                    else tmp[b + nl + rb++] = p;
+                }
+                for (uint32_t i = b; i < e; ++i) l.order[i] = tmp[i];
+                mid = b + nl;
+            }
+            const uint32_t rb0[2] = {b, mid}, re0[2] = {mid, e};
+            uint32_t ref[2];
+            for (int c = 0; c < 2; ++c) {
+                if (re0[c] - rb0[c] == 1) {
+                    ref[c] = 0x80000000u | rb0[c];
+                } else {
+                    ref[c] = baseNext + (uint32_t)nxt.size();
+                    nxt.push_back({rb0[c], re0[c]});
+                }
+            }
+            l.left[node] = ref[0];
+            l.right[node] = ref[1];
+        }
+        baseCur = baseNext;
+        baseNext += (uint32_t)nxt.size();
+        cur.swap(nxt);
+        ++levels;
+    }
+    for (uint32_t k = 0; k < n; ++k) l.leafBox[k] = prim[l.order[k]];
+    return levels;
+}
+
 // ------------------------------------------------------------------------------------------------
 // scene
 struct Blas {
@@ -1214,6 +1357,23 @@ uint32_t orc_lbvh(const float* boxes, uint32_t n, uint32_t* morton, uint32_t* or
         if (nodeboxes) std::memcpy(nodeboxes, l.nodeBox.data(), 24 * (size_t)(n - 1));
     }
     return n;
+}
+
+// binned-SAH BVH2 over n boxes (sah_build above); returns the number of levels, or 0xFFFFFFFF when
+// the tree would have more than maxLevels
+uint32_t orc_sah(const float* boxes, uint32_t n, uint32_t maxLevels, uint32_t* order, uint32_t* left, uint32_t* right, float* nodeboxes) {
+    std::vector<Box> b(n);
+    for (uint32_t i = 0; i < n; ++i) std::memcpy(&b[i], boxes + 6 * (size_t)i, 24);
+    Lbvh l;
+    const uint32_t levels = sah_build(l, b, maxLevels);
+    if (levels == 0xFFFFFFFFu) return levels;
+    if (order) std::memcpy(order, l.order.data(), 4 * (size_t)n);
+    if (n > 1) {
+        if (left) std::memcpy(left, l.left.data(), 4 * (size_t)(n - 1));
+        if (right) std::memcpy(right, l.right.data(), 4 * (size_t)(n - 1));
+        if (nodeboxes) std::memcpy(nodeboxes, l.nodeBox.data(), 24 * (size_t)(n - 1));
+    }
+    return levels;
 }
 
 orc_scene* orc_scene_create(const void* vertices, uint32_t nv, const uint32_t* indices, uint32_t ni, const void* materials, uint32_t nm,

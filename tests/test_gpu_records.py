@@ -221,3 +221,21 @@ def test_sah_blas(rg, orc):
     assert np.array_equal(ig, io) and np.array_equal(tg, to)
     rt.ctx.close()
     rl.ctx.close()
+
+
+def test_sah_blas_matches_oracle(rg, orc):
+    """The default BLASes are the oracle's binned-SAH trees (oracle/rg_oracle.cpp sah_build): the same
+    leaf order, structure and node boxes, up to the numbering of a level's nodes."""
+    for sc in (small_two_level(), S.sphere_scene()):
+        rt = rg.Raytracer(sc).prepare()
+        compared = 0
+        for b in range(len(sc.meshes)):
+            boxes = tri_boxes(sc, b)
+            if len(boxes) < 2:
+                continue
+            ref = orc.sah(boxes, 28)
+            assert ref is not None
+            assert orc.same_tree(rt.ctx.bvh(b), ref), b
+            compared += 1
+        assert compared >= 1
+        rt.ctx.close()

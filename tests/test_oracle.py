@@ -207,3 +207,56 @@ def test_show_alpha_and_fade(orc):
     u["fadeColor"] = (1.0, 0.0, 0.0, 1.0)
     fin = orc.post(u, b, n, r, fxaa=False)
     assert np.allclose(fin[..., :3], [1.0, 0.0, 0.0])
+
+
+def _check_bvh2(t, boxes):
+    """A BVH2 in the LBVH layout: every primitive in one leaf, every internal node reached once, each
+    node box the exact union of its children's boxes."""
+    n = len(t["order"])
+    assert sorted(t["order"].tolist()) == list(range(n))
+    if n < 2:
+        return
+    L, R, nb = t["left"].astype(np.int64), t["right"].astype(np.int64), t["nodeboxes"]
+    leaf_box = lambda c: boxes[t["order"][c & ~0x80000000]]
+    seen, leaves, st = set(), set(), [0]
+    while st:
+        i = st.pop()
+        assert i not in seen
+        seen.add(i)
+        kids = []
+        for c in (L[i], R[i]):
+            if c & 0x80000000:
+                leaves.add(int(c & ~0x80000000))
+                kids.append(leaf_box(c))
+            else:
+                st.append(int(c))
+                kids.append(nb[c])
+        u = np.concatenate([np.minimum(kids[0][:3], kids[1][:3]), np.maximum(kids[0][3:], kids[1][3:])])
+        assert np.array_equal(nb[i], u)
+    assert len(seen) == n - 1 and len(leaves) == n
+
+
+def test_oracle_sah_tree(orc):
+    """The oracle's binned-SAH builder (the CUDA library's default BLAS/TLAS builder restated): valid
+    BVH2s with exact node boxes, a lower surface-area cost than the LBVH over the same boxes, and the
+    level limit the library falls back to the LBVH at."""
+    def half(b):
+        d = np.maximum(b[..., 3:] - b[..., :3], 0).astype(np.float64)
+        return d[..., 0] * d[..., 1] + d[..., 1] * d[..., 2] + d[..., 2] * d[..., 0]
+    for n, dup in ((1, False), (2, False), (3, False), (257, False), (4000, True), (20000, False)):
+        boxes = random_boxes(n, 100 + n, dup)
+        t = orc.sah(boxes)
+        _check_bvh2(t, boxes)
+        assert orc.same_tree(t, orc.sah(boxes))  # deterministic
+        if n >= 257:
+            lb = orc.lbvh(boxes)
+            cost = lambda b: half(b["nodeboxes"]).sum() / half(b["nodeboxes"][0])
+            assert cost(t) < cost(lb), (n, cost(t), cost(lb))
+    # small triangles at x = 17^k: every split takes one off the far end -> n - 1 levels
+    n = 30
+    x = (17.0 ** np.arange(n)).astype(np.float32)
+    boxes = np.zeros((n, 6), np.float32)
+    boxes[:, 0], boxes[:, 3] = x, x
+    boxes[:, 4], boxes[:, 5] = 0.5, 0.5
+    assert orc.sah(boxes)["levels"] == n - 1
+    assert orc.sah(boxes, 28) is None
