@@ -11,8 +11,9 @@
 //
 // It is a scalar C++ restatement of the reference's per-frame path:
 //   * LBVH over triangle / instance boxes (30-bit Morton, stable sort, Karras 2012 hierarchy,
-//     bottom-up boxes).  The reference leaves BVHs to the Vulkan driver
-//     (render/acceleration_structure.cpp:55-194), so this part has no reference counterpart.
+//     bottom-up boxes), and the binned-SAH BVH2 the CUDA library builds by default.  The reference
+//     leaves BVHs to the Vulkan driver (render/acceleration_structure.cpp:55-194), so this part has
+//     no reference counterpart.
 //   * watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2013) with closest-hit ties broken
 //     by the smaller (instance, primitive) pair.
 //   * raygen / closest-hit / miss / shadow-miss (resources/shaders/raygen.h:69-115,
