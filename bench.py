@@ -57,9 +57,10 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="rows per render of the CPU-baseline sample (0: full frames)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", default="1920x1080", help="WxH; smaller sizes are for profiling captures only")
-    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch", "serve", "filter", "spheres"],
+    ap.add_argument("--workload", default="game-frame", choices=["game-frame", "batch", "serve", "filter", "spheres", "dist-check"],
                     help="game-frame: the 1080p 4x SSAA frame loop; batch: 64 independent scenes per step; "
-                         "serve: Poisson render requests through the render server")
+                         "serve: Poisson render requests through the render server; dist-check: the --gpus N "
+                         "launcher and the cross-rank aggregation alone, on CPU (gloo), with synthetic counts")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-rate", type=float, default=400.0, help="mean arrivals per second")
     ap.add_argument("--serve-large", type=int, default=12, help="large terrain scenes in the catalog")
@@ -153,6 +154,103 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def measure_l2_peak(dev, reps=40, trials=5):
+    """Copy bandwidth of a working set that stays in L2: two 24 MiB buffers (48 MiB, well inside the
+    126 MB L2), b.copy_(a) repeated back to back and timed with CUDA events, best of `trials`;
+    read + write bytes.  The same kind of copy as the measured HBM peak, only L2-resident."""
+    import torch
+    n = (24 << 20) // 4
+    a = torch.rand(n, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    best = 0.0
+    for _ in range(trials):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        for _ in range(reps):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        best = max(best, 2 * a.numel() * 4 * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    return best
+
+
+def camera_rays_device(ubo, width, height, dev):
+    """Pixel-centre camera rays of raygen.h:84-90 (origin, tmin 0.001, direction, tmax 1e4) for a
+    width x height image, on the device: n x 8 float32."""
+    import torch
+    u = ubo[0] if ubo.shape else ubo
+    vi = torch.tensor(u["viewInverse"].reshape(4, 4), dtype=torch.float32, device=dev)  # [col][row]
+    pi = torch.tensor(u["projInverse"].reshape(4, 4), dtype=torch.float32, device=dev)
+    ys, xs = torch.meshgrid(torch.arange(height, device=dev, dtype=torch.float32),
+                            torch.arange(width, device=dev, dtype=torch.float32), indexing="ij")
+    d = torch.stack([(xs + 0.5) / width * 2 - 1, (ys + 0.5) / height * 2 - 1, torch.ones_like(xs), torch.ones_like(xs)], -1)
+    t = (d.reshape(-1, 4) @ pi)[:, :3]
+    t = t / t.norm(dim=1, keepdim=True)
+    dirs = t @ vi[:3, :3]
+    rays = torch.zeros(len(dirs), 8, device=dev)
+    rays[:, :3] = vi[3, :3]
+    rays[:, 3], rays[:, 7] = 0.001, 10000.0
+    rays[:, 4:7] = dirs
+    return rays
+
+
+def first_bounce_secondary(ctx, sc, instances, dev, width, height):
+    """The frame's first-bounce GENERIC secondary rays (closesthit.rchit:206-250): camera rays at
+    width x height pixel centres traced on the GPU, then at every hit the reflection ray (material
+    reflectivity > 0) and the refraction ray (transparency > 0, front face eta = 1/ior, back face eta =
+    ior), from the hit point with tmin 0.01, tmax 1000, along the shading normal (object-to-world
+    3x3 times the interpolated vertex normal, flipped toward the ray).  Total internal reflection
+    (a zero direction) traverses nothing and is left out.  The grid effect's per-point material
+    changes are not applied.  Returns n x 8 float32 on the device."""
+    import torch
+    cam = camera_rays_device(sc.ubo, width, height, dev).contiguous()
+    n = len(cam)
+    tuv = torch.empty(n, 3, device=dev)
+    ids = torch.empty(n, 2, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize(dev)
+    ctx.trace_rays_device(cam.data_ptr(), n, tuv.data_ptr(), ids.data_ptr())
+    ctx.synchronize()
+    inst_id = ids[:, 0].to(torch.int64) & 0xFFFFFFFF
+    hit = inst_id != 0xFFFFFFFF
+    cam, tuv, inst_id, prim = cam[hit], tuv[hit], inst_id[hit], ids[hit, 1].to(torch.int64) & 0xFFFFFFFF
+    inst = instances
+    xf = torch.tensor(inst["transform"], dtype=torch.float32, device=dev)[inst_id]            # (m, 3, 4)
+    voff = torch.tensor(inst["vertexBufferOffset"].astype(np.int64), device=dev)[inst_id]
+    ioff = torch.tensor(inst["indexBufferOffset"].astype(np.int64), device=dev)[inst_id]
+    moff = torch.tensor(inst["materialBufferOffset"].astype(np.int64), device=dev)[inst_id]
+    idx = torch.tensor(sc.indices.astype(np.int64), device=dev)
+    vn = torch.tensor(sc.vertices["normal"], dtype=torch.float32, device=dev)
+    vmat = torch.tensor(sc.vertices["matIndex"].astype(np.int64), device=dev)
+    tri = torch.stack([idx[ioff + 3 * prim + k] for k in range(3)], 1) + voff[:, None]
+    u, v = tuv[:, 1:2], tuv[:, 2:3]
+    nrm = (1 - u - v) * vn[tri[:, 0]] + u * vn[tri[:, 1]] + v * vn[tri[:, 2]]
+    nrm = torch.einsum("mij,mj->mi", xf[:, :, :3], nrm)
+    nrm = nrm / nrm.norm(dim=1, keepdim=True)
+    mats = sc.materials
+    mi = moff + vmat[tri[:, 0]]
+    refl = torch.tensor(mats["reflectivity"], dtype=torch.float32, device=dev)[mi]
+    trans = torch.tensor(mats["transparency"], dtype=torch.float32, device=dev)[mi]
+    ior = torch.tensor(mats["ior"], dtype=torch.float32, device=dev)[mi]
+    o, d = cam[:, :3], cam[:, 4:7]
+    p = o + d * tuv[:, :1]
+    front = (-(d * nrm).sum(1)) > 0
+    nrm = torch.where(front[:, None], nrm, -nrm)
+    dn = (d * nrm).sum(1, keepdim=True)
+    r_dir = d - 2 * dn * nrm
+    eta = torch.where(front, 1.0 / ior, ior)[:, None]
+    k = 1 - eta * eta * (1 - dn * dn)
+    t_dir = torch.where(k >= 0, eta * d - (eta * dn + torch.sqrt(k.clamp_min(0))) * nrm, torch.zeros_like(d))
+    out = []
+    for sel, dd in ((refl > 0, r_dir), ((trans > 0) & (t_dir.abs().sum(1) > 0), t_dir)):
+        r = torch.zeros(int(sel.sum()), 8, device=dev)
+        r[:, :3], r[:, 3], r[:, 4:7], r[:, 7] = p[sel], 0.01, dd[sel], 1000.0
+        out.append(r)
+    return torch.cat(out).contiguous()
+
+
 def trace_traffic():
     """DRAM bytes of one trace-kernel launch from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "k_wf_trace_game_frame_1080p.json")
@@ -161,6 +259,15 @@ def trace_traffic():
         return d.get("dram_bytes_per_launch"), d.get("source")
     except (OSError, ValueError):
         return None, None
+
+
+def game_config(sc, world):
+    """The game-frame workload's identity, the same for both arms."""
+    return {"workload": WORKLOAD.format(w=sc.width, h=sc.height), "width": sc.width, "height": sc.height,
+            "spp": int(sc.ubo["numSamples"][0]), "max_recursions": int(sc.ubo["maxRecursions"][0]),
+            "instances": len(sc.instances), "instanced_tris": sc.instanced_tri_count, "unique_tris": sc.tri_count,
+            "frames": "seeded animation (FrameAnimator seed 101): frames 0 .. warmup+steps-1",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
 class FrameInputs:
@@ -331,15 +438,48 @@ def run_ours(args):
                 "trace_kernel_ms_per_frame": trace_ms, "trace_stage_ms_per_frame": tm["rtOnlySum"] / max(tm["frames"], 1),
                 "traffic_source": traffic_src}
 
+    # the L2 bound: the scene's records, triangles and vertices (~64 MB) stay in the 126 MB L2 through
+    # a frame, so the traversal's roofline is the L2's copy bandwidth, measured here
+    l2 = measure_l2_peak(dev)
+    roofline["l2"] = {"peak": l2, "frac": achieved / l2, "unit": "GB/s",
+                      "source": "measured in this run: torch copy of a 48 MiB L2-resident working set, best of 5 x 40 copies"}
+
+    # ---------------- incoherent secondary closest-hit throughput ----------------
+    # the frame's first-bounce reflection / refraction rays (closesthit.rchit:215,232,244), traced by one
+    # launch of the frame loop's traversal kernel per step (rg_trace_rays_device), L2 flushed between
+    sec = first_bounce_secondary(ctx, sc, frames.instances[f - 1], dev, 2 * sc.width, 2 * sc.height)
+    nsec = len(sec)
+    d_tuv = torch.empty(nsec, 3, device=dev)
+    d_ids = torch.empty(nsec, 2, dtype=torch.int32, device=dev)
+    barrier()
+    for _ in range(3):
+        ctx.trace_rays_device(sec.data_ptr(), nsec, d_tuv.data_ptr(), d_ids.data_ptr())
+    sec_ms = []
+    for _ in range(max(5, min(K, 20))):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(ext)
+        ctx.trace_rays_device(sec.data_ptr(), nsec, d_tuv.data_ptr(), d_ids.data_ptr())
+        a1.record(ext)
+        barrier()
+        sec_ms.append(a0.elapsed_time(a1))
+    sst = ctx.stats()
+    sec_med = statistics.median(sec_ms)
+    secondary = {"value": nsec / (sec_med * 1e-3) / 1e9, "unit": "Grays/s", "rays": nsec, "ms_median": sec_med,
+                 "stack_overflows": sst["stack_overflows"],
+                 "rays_def": "GENERIC reflection + refraction rays at the hits of 3840x2160 pixel-centre camera rays "
+                             "(the 4-spp frame's primary-ray count), materials as uploaded",
+                 "kernel": "rg_trace_rays_device: queue fill + one k_wf_trace launch + hit read-out, CUDA events on the "
+                           "library stream, L2 flushed before each launch"}
+
     out = {
         "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded procedural scene (no dataset)",
-        "config": {"workload": WORKLOAD.format(w=sc.width, h=sc.height), "width": sc.width, "height": sc.height, "spp": int(sc.ubo["numSamples"][0]),
-                   "max_recursions": int(sc.ubo["maxRecursions"][0]), "instances": ninst,
-                   "instanced_tris": sc.instanced_tri_count, "unique_tris": sc.tri_count,
-                   "l2": "flushed between frames (256 MiB memset on the library stream)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "secondary_grays_per_s": secondary,
+        "config": game_config(sc, world),
+        "l2": "flushed between frames (256 MiB memset on the library stream)",
         "frames_per_s": K / (ms * 1e-3),
         "rays_per_frame": rays / K,
         "profiler_ranges_ms": {k: tm[k + "Sum"] / max(tm["frames"], 1) for k in
@@ -724,49 +864,121 @@ def run_spheres(args):
 
 
 def run_reference(args):
-    """Reference arm: the CPU restatement of the reference shaders on all host cores."""
+    """Reference arm: the reference's path on the host cores.  Raygun's own GPU path needs a Vulkan
+    ray-tracing driver (unavailable on this machine), so each step is the frame on the CPU: the frame's
+    BLAS refits and TLAS rebuild (the oracle's, standing in for the driver's), then the reference's
+    own raygen / closest-hit / miss shaders over every pixel and its compute post passes (the
+    reference-compiled checker, oracle/_ref: Raygun's GLSL compiled as C++), on all host threads.
+    Where that checker is not built, the oracle's restatement of the same shaders runs instead
+    (kind "port").  The frames are the GPU arm's frames (same animation, frames 0 .. W+K-1).  Whole
+    frames are traced; only if K + W whole frames would take more than 4 minutes are rows sampled,
+    with the refit, TLAS and post time scaled to the rows traced."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import oracle
     oracle.build()
-    sc = S.game_frame_scene()
+    from oracle import ref as oref
+    kind, note = "port", "oracle restatement of the reference shaders (reference-compiled checker not built here)"
+    if oref.reference_present() or oref.staged_present():
+        try:
+            oref.build()
+            oref.lib()
+            kind, note = "reference", "the reference's own shaders compiled as C++ (oracle/_ref)"
+        except Exception as e:  # the port stands in
+            note = f"oracle restatement (reference-compiled checker failed to build: {str(e)[:120]})"
+    w, h = (int(x) for x in args.res.split("x"))
+    sc = S.instanced_scene(width=w, height=h)
     o = oracle.OracleScene(sc)
     nthreads = os.cpu_count() or 1
     K, W = args.steps, args.warmup
     frames = FrameInputs(sc, W + K)
-    rows = CPU_ROWS_PER_STEP
 
-    def step(f):
+    def step(f, row_step):
+        t0 = time.perf_counter()
         for b, vo, nv, arr in frames.refits[f]:
             o.refit(b, arr, vo)
         o.set_instances(frames.instances[f])
-        step_rows = sc.height // rows
-        _, _, _, st = o.render(rows=(f % step_rows, sc.height), row_step=step_rows, nthreads=nthreads)
-        return st["primary"] + st["shadow"] + st["secondary"]
+        t1 = time.perf_counter()
+        r0 = f % row_step
+        if kind == "reference":
+            base, nrm, rough, rays = oref.render_scene(o, sc.ubo, w, h, nthreads=nthreads, rows=(r0, row_step))
+        else:
+            base, nrm, rough, st = o.render(rows=(r0, h), row_step=row_step, nthreads=nthreads)
+            rays = st["primary"] + st["shadow"] + st["secondary"]
+        t2 = time.perf_counter()
+        if kind == "reference":
+            oref.post(sc.ubo, base, nrm, rough, fxaa=True, nthreads=nthreads)
+        else:
+            oracle.post(sc.ubo, base, nrm, rough, fxaa=True, nthreads=nthreads)
+        t3 = time.perf_counter()
+        frac = len(range(r0, h, row_step)) / h
+        return rays, ((t1 - t0) + (t3 - t2)) * frac + (t2 - t1)
 
-    for f in range(W):
-        step(f)
-    t = time.perf_counter()
-    rays = sum(step(W + k) for k in range(K))
-    dt = time.perf_counter() - t
+    # the first warm-up frame (whole) sizes the sample
+    _, t_frame = step(0, 1)
+    budget = 240.0
+    row_step = 1 if t_frame * (W + K) <= budget else int(np.ceil(t_frame * (W + K) / budget))
+    for f in range(1, W):
+        step(f, row_step)
+    rays, dt = 0, 0.0
+    for k in range(K):
+        r, t = step(W + k, row_step)
+        rays += r
+        dt += t
     v = rays / dt / 1e6
+    what = "whole frames" if row_step == 1 else f"every {row_step}th row (refit, TLAS and post time scaled to the rows traced)"
     out = {"metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": world, "steps": K, "warmup": W,
            "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic: seeded procedural scene (no dataset)", "impl": "reference",
-           "config": {"workload": WORKLOAD.format(w=sc.width, h=sc.height), "width": sc.width, "height": sc.height, "spp": int(sc.ubo["numSamples"][0]),
-                      "max_recursions": int(sc.ubo["maxRecursions"][0]), "instances": len(sc.instances)},
-           "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
-                            "sample": f"per step: BLAS refits + TLAS rebuild of that frame, then {rows} rows spread over the frame "
-                                      f"x {sc.width} px at {int(sc.ubo['numSamples'][0])} spp (trace + shade); the "
-                                      f"reference's Vulkan RT path needs a ray-tracing driver, unavailable on this box"},
+           "config": game_config(sc, world),
+           "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": nthreads, "kind": kind,
+                            "sample": f"{K} frames, {what}: BLAS refits + TLAS rebuild, raygen / closest-hit / miss "
+                                      f"over the frame, roughness + composite + FXAA passes; {note}; the reference's "
+                                      f"Vulkan RT path needs a ray-tracing driver, unavailable on this box"},
            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
+def launch_replicas(n):
+    """--gpus N without a launcher around us: start N ranks of this same command line, one per GPU
+    (RANK / LOCAL_RANK / WORLD_SIZE / MASTER_* in their environment, as torchrun sets them), and wait
+    for them; rank 0 prints the JSON line.  Returns the worst exit code."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__), *sys.argv[1:]], env=env))
+    return max(p.wait() for p in procs)
+
+
+def run_dist_check(args):
+    """The N > 1 plumbing without a GPU: each rank joins a gloo group and reports synthetic counts
+    (rank r: (r + 1) * 1e6 rays in 10 + r ms); rank 0 prints the aggregate line."""
+    import torch.distributed as dist
+    rank, world, _ = dist_env()
+    if world > 1:
+        dist.init_process_group("gloo")
+    value, ms = replica_throughput((rank + 1) * 1e6, 10.0 + rank, world, "cpu")
+    if rank == 0:
+        print(json.dumps({"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "ms_per_step": ms,
+                          "workload": "dist-check"}), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.gpus > 1 and "RANK" not in os.environ:
+        sys.exit(launch_replicas(args.gpus))
+    if args.workload == "dist-check":
+        run_dist_check(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)

@@ -46,8 +46,8 @@ typedef struct {
 #define RG_FLAG_HOST_LOOP 16u    /* rg_render_batch: host-polled round loop instead of the CUDA graph */
 #define RG_FLAG_TLAS_LBVH 32u    /* build the TLAS as an LBVH (Morton order) instead of by binned SAH; TLASes of more
                                     than 8192 instances are always LBVHs */
-#define RG_FLAG_BLAS_LBVH 64u    /* build BLASes as LBVHs instead of by binned SAH; BLASes of more than 2^18 triangles,
-                                    or whose SAH tree would be deeper than 28 levels, are always LBVHs */
+#define RG_FLAG_BLAS_LBVH 64u    /* build BLASes as LBVHs instead of by binned SAH; BLASes of more than 2^18 triangles
+                                    are always LBVHs */
 
 /* resources/shaders/vertex.def:3-7 (render/vertex.hpp:27-29): 32 B */
 typedef struct {
@@ -125,8 +125,11 @@ typedef struct {
     uint64_t masked;     /* mask-0 traces (closesthit.rchit:144): miss shader only, no traversal */
     uint64_t nodes;      /* BVH node visits (RG_FLAG_COUNT_VISITS) */
     uint64_t tris;       /* triangle tests (RG_FLAG_COUNT_VISITS) */
-    uint64_t stack_overflows;
+    uint64_t stack_overflows; /* rays whose short traversal stack overflowed; each was traced again with a deep
+                                 stack, so its hit is complete (a cost, not an error) */
     uint64_t iterations; /* trace/shade rounds of the wavefront loop (0 for the megakernel) */
+    uint64_t deep_overflows; /* rays that overflowed even the deep stack: 0 for every tree this library builds
+                                (at most 64 BVH2 levels); non-zero means hits may be missing */
 } rg_stats;
 
 /* Debug images of Raytracer::selectResultImage (raytracer.cpp:379-392). */
@@ -154,24 +157,42 @@ rg_status rg_upload_geometry(rg_ctx* ctx, const rg_vertex* vertices, uint32_t nv
                              const rg_material* materials, uint32_t nm);
 /* Replaces RenderSystem::updateModelBuffers (render/render_system.cpp:225-233) for a range:
  * changed vertices (the caller then refits) / materials (live material edit,
- * gpu/gpu_material.cpp:52-94). */
+ * gpu/gpu_material.cpp:52-94).  A vertex update whose new matIndex would take an instance of the
+ * current (host-built) TLAS past the material buffer is refused with RG_ERR_INVALID_ARG and changes
+ * nothing. */
 rg_status rg_update_vertices(rg_ctx* ctx, uint32_t first, const rg_vertex* vertices, uint32_t n);
 rg_status rg_update_materials(rg_ctx* ctx, uint32_t first, const rg_material* materials, uint32_t n);
-/* Same as rg_update_vertices from vertices already in device memory (device pointer). */
+/* Same as rg_update_vertices from vertices already in device memory (device pointer).  The host
+ * never sees these vertices: their matIndex values must stay as they were (or within the materials
+ * every instance of them reaches); positions may change freely. */
 rg_status rg_update_vertices_device(rg_ctx* ctx, uint32_t first, const rg_vertex* d_vertices, uint32_t n);
 
 /* Replaces BottomLevelAS::BottomLevelAS (render/acceleration_structure.cpp:140-194) as driven by
  * Raytracer::setupBottomLevelAS (render/raytracer.cpp:54-74): triangles
- * indices[indexOffset + 3k + 0..2] + vertexOffset, k < triCount.  *out_blas receives the handle. */
+ * indices[indexOffset + 3k + 0..2] + vertexOffset, k < triCount.  *out_blas receives the handle.
+ * Checked on the host first (the reference relied on Vulkan's robustBufferAccess,
+ * vulkan_context.cpp:256-257): a range past the index buffer, or vertexOffset + index past the
+ * vertex buffer, returns RG_ERR_INVALID_ARG before any kernel runs.  The build is queued on the
+ * context's stream; it can block the host while the scene's device buffers grow (cudaMalloc). */
 rg_status rg_build_blas(rg_ctx* ctx, uint32_t vertexOffset, uint32_t indexOffset, uint32_t triCount, uint32_t* out_blas);
 /* Refit of a BLAS after its vertices moved (same topology).  No reference counterpart: Raygun
  * never refits. */
 rg_status rg_refit_blas(rg_ctx* ctx, uint32_t blas);
 
 /* Replaces TopLevelAS::TopLevelAS + Raytracer::setupTopLevelAS (render/acceleration_structure.cpp:55-138,
- * render/raytracer.cpp:76-85): rebuilds the TLAS from scratch from host instances. */
+ * render/raytracer.cpp:76-85): rebuilds the TLAS from scratch from host instances.  Every instance
+ * that can be hit (known BLAS, non-zero mask) is checked on the host through its offset table entry
+ * (closesthit.rchit:98-109): indexBufferOffset + 3 * triCount within the index buffer,
+ * vertexBufferOffset + each index within the vertex buffer, materialBufferOffset + each referenced
+ * vertex's matIndex within the material buffer; a violation returns RG_ERR_INVALID_ARG ("instance k:
+ * ...") and builds nothing.  Instances with an unknown BLAS, a zero mask or a singular transform are
+ * never hit. */
 rg_status rg_build_tlas(rg_ctx* ctx, const rg_instance* instances, uint32_t n);
-/* Same, from instances already in device memory (device pointer). */
+/* Same, from instances already in device memory (device pointer).  The host cannot check these;
+ * the TLAS build does instead, and an instance is never hit unless its vertexBufferOffset and
+ * indexBufferOffset are its BLAS's own (those of rg_build_blas, as in the reference, where every
+ * instance's offsets are its model's, acceleration_structure.cpp:79-82) and materialBufferOffset
+ * keeps the BLAS's materials inside the material buffer. */
 rg_status rg_build_tlas_device(rg_ctx* ctx, const rg_instance* d_instances, uint32_t n);
 
 /* Replaces the resize path RenderSystem::reload -> Raytracer::setupRaytracingImages
@@ -238,7 +259,9 @@ typedef struct rg_job {
 enum { RG_SORT_NONE = 0, RG_SORT_OCTANT = 1, RG_SORT_MORTON = 2 };
 typedef struct rg_batch_tune {
     int32_t threads;      /* block size: 64, 128 or 256 */
-    int32_t stack_depth;  /* traversal stack entries per thread: 16, 24, 32 or 48 (48: up to 128 threads) */
+    int32_t stack_depth;  /* traversal stack words per thread: 16, 24, 32 or 48 (48: up to 128 threads); one word
+                             flags an overflow, the rest hold entries.  A ray that overflows them is traced
+                             again with a deep stack (rg_stats.stack_overflows counts them) */
     int32_t sort_key;     /* RG_SORT_*: rays sorted per round by direction octant or origin Morton code */
 } rg_batch_tune;
 
@@ -327,8 +350,17 @@ rg_status rg_bvh_records(rg_ctx* ctx, uint32_t blas, void* out, uint32_t capacit
 /* World-to-object transforms the TLAS build computed (12 floats per instance). */
 rg_status rg_instance_inverse(rg_ctx* ctx, float* out);
 /* Closest hit of n rays (8 floats: origin.xyz, tmin, dir.xyz, tmax) through the current TLAS:
- * hit_tuv n x 3 (t, u, v), hit_ids n x 2 (instance, primitive; 0xFFFFFFFF = miss). */
+ * hit_tuv n x 3 (t, u, v), hit_ids n x 2 (instance, primitive; 0xFFFFFFFF = miss).  The traversal
+ * stack has the batch launch shape's depth (rg_set_batch_tune; 48 by default).  Resets the per-frame
+ * statistics: rg_get_stats afterwards reports this call's stack_overflows / deep_overflows. */
 rg_status rg_trace_rays(rg_ctx* ctx, const float* rays, uint32_t n, float* hit_tuv, uint32_t* hit_ids);
+/* The same closest hits from and into device memory, asynchronous on the context's stream, traced by
+ * one launch of the frame loop's traversal kernel (the rays fill its ray queue; no shading follows).
+ * The hits equal rg_trace_rays'.  Like the reference's traceRayEXT of a batch of rays with no
+ * shading (closesthit.rchit:215,232,244 issue such rays), it is how incoherent secondary-ray
+ * throughput is measured.  Resets the per-frame statistics (stack_overflows; nodes / tris with
+ * RG_FLAG_COUNT_VISITS). */
+rg_status rg_trace_rays_device(rg_ctx* ctx, const float* d_rays, uint32_t n, float* d_hit_tuv, uint32_t* d_hit_ids);
 /* Post passes alone on host G-buffers (width*height*4 floats each, current resolution):
  * writes the framebuffer; used to check the post kernels on identical inputs. */
 rg_status rg_post_only(rg_ctx* ctx, const rg_ubo* ubo, const float* base, const float* normal, const float* rough,

@@ -52,7 +52,7 @@ def lib():
         L.orc_trace.restype = I
         L.orc_render.argtypes = [P, P, U32, U32, U32, U32, U32, P, P, P, P, I, I]
         L.orc_render.restype = I
-        L.orc_post.argtypes = [P, U32, U32, P, P, P, P, P, I]
+        L.orc_post.argtypes = [P, U32, U32, P, P, P, P, P, I, I]
         L.orc_post.restype = I
         L.orc_round_half.argtypes = [P, P, ctypes.c_uint64]
         _lib = L
@@ -75,17 +75,20 @@ def lbvh(boxes: np.ndarray):
     return out
 
 
-def sah(boxes: np.ndarray, max_levels: int = 0xFFFFFFFF):
-    """Binned-SAH BVH2 over boxes (n, 6) -> dict(order, left, right, nodeboxes, levels), or None when
-    the tree would have more than max_levels levels."""
+# level from which the binned-SAH builder halves ranges instead of binning (the CUDA library's
+# kSahMedianLevel): it bounds the depth of every SAH tree by this + ceil(log2 n)
+SAH_MEDIAN_LEVEL = 32
+
+
+def sah(boxes: np.ndarray, median_level: int = SAH_MEDIAN_LEVEL):
+    """Binned-SAH BVH2 over boxes (n, 6) -> dict(order, left, right, nodeboxes, levels); ranges are
+    halved without binning from level median_level on."""
     boxes = np.ascontiguousarray(boxes, np.float32)
     n = len(boxes)
     out = dict(order=np.zeros(n, np.uint32), left=np.zeros(max(n - 1, 0), np.uint32),
                right=np.zeros(max(n - 1, 0), np.uint32), nodeboxes=np.zeros((max(n - 1, 0), 6), np.float32))
-    levels = lib().orc_sah(_p(boxes), n, max_levels, _p(out["order"]), _p(out["left"]), _p(out["right"]),
+    levels = lib().orc_sah(_p(boxes), n, median_level, _p(out["order"]), _p(out["left"]), _p(out["right"]),
                            _p(out["nodeboxes"]))
-    if levels == 0xFFFFFFFF:
-        return None
     out["levels"] = int(levels)
     return out
 
@@ -180,7 +183,7 @@ class OracleScene:
         return imgs[0], imgs[1], imgs[2], {k: int(v) for k, v in zip(keys, st)}
 
 
-def post(ubo, base, normal, rough, fxaa=True, debug=False):
+def post(ubo, base, normal, rough, fxaa=True, debug=False, nthreads=1):
     """Post passes on G-buffers (H, W, 4).  Returns final (H, W, 4) [and the debug images:
     transitions, roughColorsA, roughColorsB, pre-FXAA final]."""
     H, W = base.shape[:2]
@@ -188,7 +191,7 @@ def post(ubo, base, normal, rough, fxaa=True, debug=False):
     fin = np.zeros((H, W, 4), np.float32)
     dbg = np.zeros((4, H, W, 4), np.float32) if debug else None
     u = np.ascontiguousarray(ubo)
-    lib().orc_post(_p(u), W, H, _p(b), _p(n), _p(r), _p(fin), _p(dbg) if debug else None, 1 if fxaa else 0)
+    lib().orc_post(_p(u), W, H, _p(b), _p(n), _p(r), _p(fin), _p(dbg) if debug else None, 1 if fxaa else 0, nthreads)
     return (fin, dbg) if debug else fin
 
 

@@ -37,6 +37,14 @@ def reference_present() -> bool:
     return os.path.isdir(SHADERS)
 
 
+def staged_present() -> bool:
+    """The rewritten shader copies of an earlier build (oracle/_ref/src) are there: the checker can be
+    rebuilt from them where the reference tree itself is absent (the git-ignored folder travels with
+    the working tree to the GPU host)."""
+    src = os.path.join(OUT, "src")
+    return os.path.isfile(os.path.join(src, "closesthit.rchit")) and os.path.isfile(os.path.join(src, "raygen.rgen"))
+
+
 def _rewrite(text: str) -> str:
     out = []
     for line in text.split("\n"):
@@ -51,9 +59,13 @@ def _rewrite(text: str) -> str:
 
 
 def build(force: bool = False) -> str:
-    if not reference_present():
-        raise RuntimeError(f"reference shaders not found under {SHADERS}")
     src = os.path.join(OUT, "src")
+    if not reference_present():
+        if not staged_present():
+            raise RuntimeError(f"reference shaders not found under {SHADERS}")
+        deps = [os.path.join(HERE, "ref_shaders.cpp"), os.path.join(HERE, "glsl_shim.hpp"), os.path.join(ORACLE, "rg_oracle.cpp")]
+        deps += [os.path.join(src, n) for n in os.listdir(src)]
+        return _compile(src, deps, force)
     os.makedirs(src, exist_ok=True)
     deps = [os.path.join(HERE, "ref_shaders.cpp"), os.path.join(HERE, "glsl_shim.hpp"), os.path.join(ORACLE, "rg_oracle.cpp")]
     for name in sorted(os.listdir(SHADERS)):
@@ -66,6 +78,10 @@ def build(force: bool = False) -> str:
                 with open(dst, "w", encoding="utf-8") as f:
                     f.write(text)
             deps.append(dst)
+    return _compile(src, deps, force)
+
+
+def _compile(src, deps, force):
     if force or not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
         cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fsingle-precision-constant",
                "-fno-strict-aliasing", "-w", "-fPIC", "-shared", "-I", src, "-I", HERE,
@@ -83,8 +99,10 @@ def lib():
         P, U32, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
         L.ref_render.argtypes = [P, U32, P, U32, P, U32, P, U32, P, U32, P, U32, U32, P, P, P, P, I]
         L.ref_render.restype = I
-        L.ref_post.argtypes = [P, U32, U32, P, P, P, P, P, I]
+        L.ref_post.argtypes = [P, U32, U32, P, P, P, P, P, I, I]
         L.ref_post.restype = I
+        L.ref_scene_render.argtypes = [P, P, U32, U32, P, P, P, P, I, U32, U32]
+        L.ref_scene_render.restype = I
         _lib = L
     return _lib
 
@@ -105,12 +123,24 @@ def render(scene, ubo=None, nthreads=None):
     return imgs[0], imgs[1], imgs[2], int(rays[0])
 
 
-def post(ubo, base, normal, rough, fxaa=True, debug=False):
+def render_scene(oscene, ubo, width, height, nthreads=None, rows=(0, 1)):
+    """The reference raygen over an oracle.OracleScene that persists across frames (refit and
+    instance updates through the OracleScene) -> (base, normal, rough, rays); rows = (first, step)
+    renders rows first, first + step, ... only."""
+    u = np.ascontiguousarray(ubo)
+    imgs = [np.zeros((height, width, 4), np.float32) for _ in range(3)]
+    rays = np.zeros(1, np.uint64)
+    lib().ref_scene_render(oscene.h, _p(u), width, height, _p(imgs[0]), _p(imgs[1]), _p(imgs[2]), _p(rays),
+                           nthreads or os.cpu_count(), rows[0], rows[1])
+    return imgs[0], imgs[1], imgs[2], int(rays[0])
+
+
+def post(ubo, base, normal, rough, fxaa=True, debug=False, nthreads=1):
     """The reference compute passes -> final image [, debug images as in oracle.post]."""
     H, W = base.shape[:2]
     b, n, r = (np.ascontiguousarray(x, np.float32) for x in (base, normal, rough))
     fin = np.zeros((H, W, 4), np.float32)
     dbg = np.zeros((4, H, W, 4), np.float32) if debug else None
     u = np.ascontiguousarray(ubo)
-    lib().ref_post(_p(u), W, H, _p(b), _p(n), _p(r), _p(fin), _p(dbg) if debug else None, 1 if fxaa else 0)
+    lib().ref_post(_p(u), W, H, _p(b), _p(n), _p(r), _p(fin), _p(dbg) if debug else None, 1 if fxaa else 0, nthreads)
     return (fin, dbg) if debug else fin

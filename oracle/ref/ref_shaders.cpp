@@ -217,16 +217,70 @@ struct Images {
     ns::roughColorsASampler.img = &ns::roughColorsA;    \
     ns::roughColorsBSampler.img = &ns::roughColorsB
 
+// one compute dispatch over W x H invocations, rows spread over nthreads threads (the invocations of
+// a dispatch write distinct pixels and read only the previous dispatch's images)
 template <class F>
-void dispatch(int W, int H, F main) {
-    rgsl::Invocation inv;
-    rgsl::g_inv = &inv;
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) {
-            inv.globalID = rgsl::uvec3((rgsl::uint)x, (rgsl::uint)y, 0u);
-            main();
+void dispatch(int W, int H, F main, int nthreads = 1) {
+    auto rows = [&](std::atomic<int>& next) {
+        rgsl::Invocation inv;
+        rgsl::g_inv = &inv;
+        for (;;) {
+            const int y = next.fetch_add(1);
+            if (y >= H) break;
+            for (int x = 0; x < W; ++x) {
+                inv.globalID = rgsl::uvec3((rgsl::uint)x, (rgsl::uint)y, 0u);
+                main();
+            }
         }
-    rgsl::g_inv = nullptr;
+        rgsl::g_inv = nullptr;
+    };
+    std::atomic<int> next{0};
+    if (nthreads <= 1) {
+        rows(next);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) th.emplace_back([&] { rows(next); });
+    for (auto& x : th) x.join();
+}
+
+// raygen over every pixel of an already bound scene
+void raygen_all(uint32_t W, uint32_t H, float* base, float* normal, float* rough, uint64_t* rays, int nthreads, uint32_t row0 = 0,
+                uint32_t rowStep = 1) {
+    Images I((int)W, (int)H);
+    sh_raygen::image = I.img[1];
+    sh_raygen::normalImage = I.img[2];
+    sh_raygen::roughImage = I.img[3];
+    if (nthreads < 1) nthreads = 1;
+    std::vector<uint64_t> counts(nthreads, 0);
+    std::atomic<uint32_t> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t)
+        th.emplace_back([&, t] {
+            bind_payload_this_thread();
+            g_rays = 0;
+            rgsl::Invocation inv;
+            inv.launchSize = rgsl::uvec3(W, H, 1u);
+            for (;;) {
+                const uint32_t y = row0 + next.fetch_add(1) * rowStep;
+                if (y >= H) break;
+                for (uint32_t x = 0; x < W; ++x) {
+                    inv.launchID = rgsl::uvec3(x, y, 0u);
+                    rgsl::g_inv = &inv;
+                    sh_raygen::main();
+                }
+            }
+            counts[t] = g_rays;
+        });
+    for (auto& x : th) x.join();
+    std::memcpy(base, I.base.data(), 16 * (size_t)W * H);
+    std::memcpy(normal, I.normal.data(), 16 * (size_t)W * H);
+    std::memcpy(rough, I.rough.data(), 16 * (size_t)W * H);
+    if (rays) {
+        uint64_t tot = 0;
+        for (auto c : counts) tot += c;
+        *rays = tot;
+    }
 }
 
 }  // namespace rgref
@@ -238,43 +292,19 @@ int ref_render(const void* vertices, uint32_t nv, const uint32_t* indices, uint3
                const uint32_t* meshes, uint32_t nmesh, const void* instances, uint32_t ninst, const void* ubo, uint32_t W,
                uint32_t H, float* base, float* normal, float* rough, uint64_t* rays, int nthreads) {
     orc_scene* sc = orc_scene_create(vertices, nv, indices, ni, materials, nm, meshes, nmesh, instances, ninst);
-    const Scene& s = *(const Scene*)sc;
-    rgref::bind_scene(s, *(const Ubo*)ubo);
-    rgref::Images I((int)W, (int)H);
-    sh_raygen::image = I.img[1];
-    sh_raygen::normalImage = I.img[2];
-    sh_raygen::roughImage = I.img[3];
-    if (nthreads < 1) nthreads = 1;
-    std::vector<uint64_t> counts(nthreads, 0);
-    std::atomic<uint32_t> next{0};
-    std::vector<std::thread> th;
-    for (int t = 0; t < nthreads; ++t)
-        th.emplace_back([&, t] {
-            rgref::bind_payload_this_thread();
-            rgref::g_rays = 0;
-            rgsl::Invocation inv;
-            inv.launchSize = rgsl::uvec3(W, H, 1u);
-            for (;;) {
-                uint32_t y = next.fetch_add(1);
-                if (y >= H) break;
-                for (uint32_t x = 0; x < W; ++x) {
-                    inv.launchID = rgsl::uvec3(x, y, 0u);
-                    rgsl::g_inv = &inv;
-                    sh_raygen::main();
-                }
-            }
-            counts[t] = rgref::g_rays;
-        });
-    for (auto& x : th) x.join();
-    std::memcpy(base, I.base.data(), 16 * (size_t)W * H);
-    std::memcpy(normal, I.normal.data(), 16 * (size_t)W * H);
-    std::memcpy(rough, I.rough.data(), 16 * (size_t)W * H);
-    if (rays) {
-        uint64_t tot = 0;
-        for (auto c : counts) tot += c;
-        *rays = tot;
-    }
+    rgref::bind_scene(*(const Scene*)sc, *(const Ubo*)ubo);
+    rgref::raygen_all(W, H, base, normal, rough, rays, nthreads);
     orc_scene_destroy(sc);
+    return 0;
+}
+
+// the same on an oracle scene that persists across frames (orc_scene_refit / orc_scene_set_instances
+// between calls move its instances and refit its BLASes, as a frame loop does);
+// rows row0, row0 + rowStep, ... only (the others stay zero)
+int ref_scene_render(orc_scene* sc, const void* ubo, uint32_t W, uint32_t H, float* base, float* normal, float* rough, uint64_t* rays,
+                     int nthreads, uint32_t row0, uint32_t rowStep) {
+    rgref::bind_scene(*(const Scene*)sc, *(const Ubo*)ubo);
+    rgref::raygen_all(W, H, base, normal, rough, rays, nthreads, row0, rowStep < 1 ? 1 : rowStep);
     return 0;
 }
 
@@ -282,7 +312,7 @@ int ref_render(const void* vertices, uint32_t nv, const uint32_t* indices, uint3
 // final_out = the image the reference presents (FXAA output after the swap, or finalImage);
 // debug (nullable): roughTransitions, roughColorsA, roughColorsB, finalImage before FXAA
 int ref_post(const void* ubo_, uint32_t W, uint32_t H, const float* base, const float* normal, const float* rough, float* final_out,
-             float* debug, int fxaa) {
+             float* debug, int fxaa, int nthreads) {
     const Ubo& u = *(const Ubo*)ubo_;
     rgref::Images I((int)W, (int)H);
     std::memcpy(I.base.data(), base, 16 * (size_t)W * H);
@@ -293,12 +323,12 @@ int ref_post(const void* ubo_, uint32_t W, uint32_t H, const float* base, const 
     RG_BIND_COMPUTE(sh_blur_v, I, u);
     RG_BIND_COMPUTE(sh_post, I, u);
     RG_BIND_COMPUTE(sh_fxaa, I, u);
-    rgref::dispatch((int)W, (int)H, sh_prepare::main);
+    rgref::dispatch((int)W, (int)H, sh_prepare::main, nthreads);
     for (int i = 0; i < 10; ++i) {  // raytracer.cpp:116-121
-        rgref::dispatch((int)W, (int)H, sh_blur_h::main);
-        rgref::dispatch((int)W, (int)H, sh_blur_v::main);
+        rgref::dispatch((int)W, (int)H, sh_blur_h::main, nthreads);
+        rgref::dispatch((int)W, (int)H, sh_blur_v::main, nthreads);
     }
-    rgref::dispatch((int)W, (int)H, sh_post::main);
+    rgref::dispatch((int)W, (int)H, sh_post::main, nthreads);
     size_t n = 4 * (size_t)W * H;
     if (debug) {
         std::memcpy(debug, I.trans.data(), 4 * n);
@@ -307,7 +337,7 @@ int ref_post(const void* ubo_, uint32_t W, uint32_t H, const float* base, const 
         std::memcpy(debug + 3 * n, I.fin.data(), 4 * n);
     }
     if (fxaa) {
-        rgref::dispatch((int)W, (int)H, sh_fxaa::main);  // writes baseImage, then swap (raytracer.cpp:137-140)
+        rgref::dispatch((int)W, (int)H, sh_fxaa::main, nthreads);  // writes baseImage, then swap (raytracer.cpp:137-140)
         std::memcpy(final_out, I.base.data(), 4 * n);
     } else {
         std::memcpy(final_out, I.fin.data(), 4 * n);

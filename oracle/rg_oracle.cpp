@@ -320,13 +320,15 @@ static void lbvh_build(Lbvh& b, const std::vector<Box>& prim) {
 // usable split (coincident centroids, or every cost infinite) is halved.  Children of one primitive
 // are leaf refs.  Internal nodes are numbered in level order, tasks of a level in order (the GPU
 // numbers a level's nodes in the order its warps emit them, so trees compare up to that numbering).
-// Returns the number of levels, or 0xFFFFFFFF when it would exceed maxLevels (tree unfinished).
+// From level medianLevel on (root = level 0) every range is halved without binning, so no tree is
+// deeper than medianLevel + ceil(log2 n) levels however the centroids are spread.  Returns the
+// number of levels.
 static float half_area3(const float* lo, const float* hi) {
     const float dx = std::fmax(hi[0] - lo[0], 0.0f), dy = std::fmax(hi[1] - lo[1], 0.0f), dz = std::fmax(hi[2] - lo[2], 0.0f);
     return dx * dy + dy * dz + dz * dx;
 }
 
-static uint32_t sah_build(Lbvh& l, const std::vector<Box>& prim, uint32_t maxLevels) {
+static uint32_t sah_build(Lbvh& l, const std::vector<Box>& prim, uint32_t medianLevel) {
     const int kBins = 16;
     const uint32_t n = (uint32_t)prim.size();
     l.n = n;
@@ -344,7 +346,7 @@ static uint32_t sah_build(Lbvh& l, const std::vector<Box>& prim, uint32_t maxLev
     std::vector<uint32_t> tmp(n);
     uint32_t baseCur = 0, baseNext = 1, levels = 0;
     while (!cur.empty()) {
-        if (levels >= maxLevels) return 0xFFFFFFFFu;
+        const bool median = levels >= medianLevel;
         nxt.clear();
         for (uint32_t t = 0; t < cur.size(); ++t) {
             const uint32_t b = cur[t].first, e = cur[t].second, node = baseCur + t;
@@ -395,7 +397,7 @@ static uint32_t sah_build(Lbvh& l, const std::vector<Box>& prim, uint32_t maxLev
             }
             float bestCost = INFINITY;
             int bestCand = -1;
-            for (int cand = 0; cand < 3 * (kBins - 1); ++cand) {
+            for (int cand = 0; !median && cand < 3 * (kBins - 1); ++cand) {
                 const int a = cand / (kBins - 1), sp = cand % (kBins - 1) + 1;
                 if (scale[a] <= 0.0f) continue;
                 float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -1114,10 +1116,14 @@ static float dist4(const float* a, const float* b) {
     return std::sqrt(((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3);
 }
 
-static void rough_passes(const Img& rough, const Img& normal, Img& trans, Img& A, Img& B) {
+template <class F>
+static void parallel_rows(uint32_t r0, uint32_t r1, int nthreads, F&& f);
+
+static void rough_passes(const Img& rough, const Img& normal, Img& trans, Img& A, Img& B, int nt = 1) {
     const int W = rough.W, H = rough.H;
     // rough_prepare.comp:28-54
-    for (int y = 0; y < H; ++y)
+    parallel_rows(0, (uint32_t)H, nt, [&](uint32_t yy, int) {
+        const int y = (int)yy;
         for (int x = 0; x < W; ++x) {
             float r[4], ru[4], rd[4], rl[4], rr[4], n[4], nu[4], nd[4], nl[4], nr[4];
             rough.load(x, y, r); rough.load(x, y + 1, ru); rough.load(x, y - 1, rd); rough.load(x + 1, y, rl); rough.load(x - 1, y, rr);
@@ -1133,13 +1139,15 @@ static void rough_passes(const Img& rough, const Img& normal, Img& trans, Img& A
             std::memcpy(A.at(x, y), r, 16);
             std::memcpy(B.at(x, y), r, 16);
         }
-    // rough_blur.h:23-40, 10 x (H: A->B, V: B->A)
+    });
+    // rough_blur.h:23-40, 10 x (H: A->B, V: B->A); a pass reads only the previous pass's image
     for (int it = 0; it < 10; ++it) {
         for (int pass = 0; pass < 2; ++pass) {
             const Img& in = pass == 0 ? A : B;
             Img& out = pass == 0 ? B : A;
             int ox = pass == 0 ? 1 : 0, oy = pass == 0 ? 0 : 1;
-            for (int y = 0; y < H; ++y)
+            parallel_rows(0, (uint32_t)H, nt, [&](uint32_t yy, int) {
+                const int y = (int)yy;
                 for (int x = 0; x < W; ++x) {
                     float t = trans.at(x, y)[0];
                     if (t < 0.001f) continue;
@@ -1152,6 +1160,7 @@ static void rough_passes(const Img& rough, const Img& normal, Img& trans, Img& A
                     for (int k = 0; k < 3; ++k) o[k] = rh((c[k] * w + a[k] * t) + b[k] * t);
                     o[3] = rh(c[3]);
                 }
+            });
         }
     }
 }
@@ -1360,14 +1369,13 @@ uint32_t orc_lbvh(const float* boxes, uint32_t n, uint32_t* morton, uint32_t* or
     return n;
 }
 
-// binned-SAH BVH2 over n boxes (sah_build above); returns the number of levels, or 0xFFFFFFFF when
-// the tree would have more than maxLevels
-uint32_t orc_sah(const float* boxes, uint32_t n, uint32_t maxLevels, uint32_t* order, uint32_t* left, uint32_t* right, float* nodeboxes) {
+// binned-SAH BVH2 over n boxes (sah_build above, ranges halved from level medianLevel on); returns
+// the number of levels
+uint32_t orc_sah(const float* boxes, uint32_t n, uint32_t medianLevel, uint32_t* order, uint32_t* left, uint32_t* right, float* nodeboxes) {
     std::vector<Box> b(n);
     for (uint32_t i = 0; i < n; ++i) std::memcpy(&b[i], boxes + 6 * (size_t)i, 24);
     Lbvh l;
-    const uint32_t levels = sah_build(l, b, maxLevels);
-    if (levels == 0xFFFFFFFFu) return levels;
+    const uint32_t levels = sah_build(l, b, medianLevel);
     if (order) std::memcpy(order, l.order.data(), 4 * (size_t)n);
     if (n > 1) {
         if (left) std::memcpy(left, l.left.data(), 4 * (size_t)(n - 1));
@@ -1523,13 +1531,13 @@ int orc_render(orc_scene* sc, const void* ubo, uint32_t W, uint32_t H, uint32_t 
 // roughColorsB, finalImage before FXAA.  When showAlpha is set, the images get .aaaa as in
 // postprocess.comp:41-49 (normal/rough/base are modified in place).
 int orc_post(const void* ubo, uint32_t W, uint32_t H, float* base, float* normal, float* rough, float* final_out, float* debug,
-             int fxaa) {
+             int fxaa, int nthreads) {
     const Ubo& u = *(const Ubo*)ubo;
     Img ib(W, H), in(W, H), ir(W, H), tr(W, H), A(W, H), B(W, H), fin(W, H);
     std::memcpy(ib.px.data(), base, 16 * (size_t)W * H);
     std::memcpy(in.px.data(), normal, 16 * (size_t)W * H);
     std::memcpy(ir.px.data(), rough, 16 * (size_t)W * H);
-    rough_passes(ir, in, tr, A, B);
+    rough_passes(ir, in, tr, A, B, nthreads);
     postprocess(ib, A, u, fin);
     if (u.showAlpha) {
         for (Img* im : {&fin, &in, &ir, &ib, &A, &B})
@@ -1554,13 +1562,14 @@ int orc_post(const void* ubo, uint32_t W, uint32_t H, float* base, float* normal
         return 0;
     }
     Fxaa f(fin);
-    for (uint32_t y = 0; y < H; ++y)
+    parallel_rows(0, H, nthreads, [&](uint32_t y, int) {
         for (uint32_t x = 0; x < W; ++x) {
             float o[4];
             f.pixel((int)x, (int)y, o);
             float* d = final_out + 4 * ((size_t)y * W + x);
             for (int k = 0; k < 4; ++k) d[k] = rh(o[k]);
         }
+    });
     return 0;
 }
 

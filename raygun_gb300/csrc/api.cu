@@ -8,7 +8,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "rg_internal.cuh"
@@ -29,7 +31,9 @@ struct BvhSet {  // buffers of one LBVH (BLAS or TLAS)
 };
 
 struct BlasRec {
-    uint32_t vOff = 0, iOff = 0;
+    uint32_t vOff = 0, iOff = 0, triCount = 0;
+    uint32_t maxMat = 0;  // largest matIndex its triangles' vertices carry, as of geometry generation gen
+    uint64_t gen = 0;
     BvhSet bvh;
     DevBuf tris;
 };
@@ -67,6 +71,16 @@ std::atomic<uint64_t> g_launches{0};
 struct SceneState {
     DevBuf vertices, indices, materials;
     uint32_t nv = 0, ni = 0, nm = 0;
+    // Host copies the range checks read (the reference relied on Vulkan's robustBufferAccess,
+    // vulkan_context.cpp:256-257; here every index, vertex and material reference is checked before
+    // a kernel reads through it): the index buffer, each vertex's matIndex, and per range the
+    // largest local index (iOff, triCount) and the largest matIndex of the vertices it references
+    // (vOff, iOff, triCount).
+    std::vector<uint32_t> hostIdx, hostMat;
+    uint64_t gen = 1;  // geometry generation: every rg_upload_geometry starts a new one
+    std::vector<rg_instance> hostInst;  // instances of the last host-built TLAS (empty after a device build)
+    std::map<std::pair<uint32_t, uint32_t>, uint32_t> maxIdx;
+    std::map<std::tuple<uint32_t, uint32_t, uint32_t>, uint32_t> maxMat;
     std::vector<BlasRec> blas;
     DevBuf blasTable;
     DevBuf instIn, instDev, tlasLeaves;
@@ -95,7 +109,7 @@ struct rg_ctx {
     DevBuf counters, tmpA, tmpB, tmpC, tmpD;  // counters: 8 per-frame + 8 cumulative
     DevBuf samples, workCounter;               // per-sample payload sums, persistent-kernel work counter
     // wavefront path state
-    DevBuf wfPayload, wfMeta, wfFrames, wfQO0, wfQO1, wfQD0, wfQD1, wfQP0, wfQP1, wfHitTUV, wfHitInst, wfCounts;
+    DevBuf wfPayload, wfMeta, wfFrames, wfQO0, wfQO1, wfQD0, wfQD1, wfQP0, wfQP1, wfHitTUV, wfHitInst, wfCounts, wfOverflow;
     uint32_t* hostCount = nullptr;             // pinned words for polling the queue length and work counter
     int lastIterations = 0;
     // batch rendering: job table, per-slot job / sample index, ray-sort scratch, per-job images
@@ -155,6 +169,64 @@ rg_status fail(rg_ctx* c, rg_status code, const std::string& msg) {
         rg_status s_ = (expr);       \
         if (s_ != RG_OK) return s_;  \
     } while (0)
+
+// largest mesh-local index of triangles [iOff/3, iOff/3 + n) of the index buffer (cached per range)
+uint32_t range_max_index(SceneState& st, uint32_t iOff, uint32_t n) {
+    const auto key = std::make_pair(iOff, n);
+    auto it = st.maxIdx.find(key);
+    if (it != st.maxIdx.end()) return it->second;
+    uint32_t m = 0;
+    for (size_t k = iOff, e = (size_t)iOff + 3ull * n; k < e; ++k) m = std::max(m, st.hostIdx[k]);
+    st.maxIdx.emplace(key, m);
+    return m;
+}
+
+// largest matIndex of the vertices vOff + index referenced by that range (the range's vertex
+// references must already be known to lie inside the vertex buffer)
+uint32_t range_max_material(SceneState& st, uint32_t vOff, uint32_t iOff, uint32_t n) {
+    const auto key = std::make_tuple(vOff, iOff, n);
+    auto it = st.maxMat.find(key);
+    if (it != st.maxMat.end()) return it->second;
+    uint32_t m = 0;
+    for (size_t k = iOff, e = (size_t)iOff + 3ull * n; k < e; ++k) m = std::max(m, st.hostMat[(size_t)vOff + st.hostIdx[k]]);
+    st.maxMat.emplace(key, m);
+    return m;
+}
+
+bool range_ok(SceneState& st, uint32_t vOff, uint32_t iOff, uint32_t n, uint32_t mOff, std::string* why);
+
+// an instance the TLAS traverses (known BLAS, non-zero mask) reaches only uploaded indices, vertices
+// and materials through its offset table entry (closesthit.rchit:98-109)
+bool instance_ok(SceneState& st, const rg_instance& in, std::string* why) {
+    if (in.blas >= st.blas.size() || !(in.mask & 0xFFu)) return true;  // never traversed
+    const BlasRec& r = st.blas[in.blas];
+    if (r.gen == st.gen && in.vertexBufferOffset == r.vOff && in.indexBufferOffset == r.iOff) {
+        // the BLAS's own ranges, checked when it was built: only the material offset is new
+        if (r.triCount == 0 || (uint64_t)in.materialBufferOffset + r.maxMat < st.nm) return true;
+        *why = "material offset + vertex matIndex outside the material buffer";
+        return false;
+    }
+    return range_ok(st, in.vertexBufferOffset, in.indexBufferOffset, r.triCount, in.materialBufferOffset, why);
+}
+
+// the triangle range [iOff/3, iOff/3 + n) with vertex offset vOff stays inside the index and vertex
+// buffers; with a material offset (mOff != ~0u) its vertices' materials stay inside the material buffer
+bool range_ok(SceneState& st, uint32_t vOff, uint32_t iOff, uint32_t n, uint32_t mOff, std::string* why) {
+    if (n == 0) return true;
+    if ((uint64_t)iOff + 3ull * n > st.ni) {
+        *why = "triangle range outside the index buffer";
+        return false;
+    }
+    if ((uint64_t)vOff + range_max_index(st, iOff, n) >= st.nv) {
+        *why = "vertex offset + index outside the vertex buffer";
+        return false;
+    }
+    if (mOff != ~0u && (uint64_t)mOff + range_max_material(st, vOff, iOff, n) >= st.nm) {
+        *why = "material offset + vertex matIndex outside the material buffer";
+        return false;
+    }
+    return true;
+}
 
 rg_status ensure(rg_ctx* c, DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 16;
@@ -259,6 +331,9 @@ rg_status upload_blas_entry(rg_ctx* c, uint32_t b) {
     e.wide = r.bvh.wide.as<WideNode>();
     e.tris = r.tris.as<float4>();
     e.n = r.bvh.n;
+    e.maxMat = r.maxMat;
+    e.vOff = r.vOff;
+    e.iOff = r.iOff;
     DevBlas* d = c->sc->blasTable.as<DevBlas>() + b;
     CK(cudaMemcpyAsync(d, &e, sizeof(DevBlas), cudaMemcpyHostToDevice, c->stream));
     if (r.bvh.n > 0) CK(cudaMemcpyAsync(d->root, root_box(r.bvh), 24, cudaMemcpyDeviceToDevice, c->stream));
@@ -309,7 +384,7 @@ DevScene scene_of(const SceneState& st) {
     return s;
 }
 
-rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
+rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n, bool checkOffsets) {
     c->sc->nInst = n;
     c->sc->tlasReady = false;
     TRY(ensure(c, c->sc->instDev, sizeof(DevInstance) * (size_t)(n ? n : 1)));
@@ -319,9 +394,9 @@ rg_status build_tlas_from_device_instances(rg_ctx* c, uint32_t n) {
     TRY(cur_events(c, &fe));
     CK(cudaEventRecord(fe->ev[EV_AS0], c->stream));
     CK(setup_instances(c->sc->instIn.as<rg_instance>(), n, c->sc->blasTable.as<DevBlas>(), (uint32_t)c->sc->blas.size(),
-                       c->sc->instDev.as<DevInstance>(), c->sc->tlas.primBoxes.as<float>(), c->stream));
+                       c->sc->instDev.as<DevInstance>(), c->sc->tlas.primBoxes.as<float>(), checkOffsets, c->sc->nm, c->stream));
     if (!(c->flags & RG_FLAG_TLAS_LBVH) && n > 1 && n <= kSahMaxPrims)
-        CK(sah_build(buffers(c, c->sc->tlas), false, 0xFFFFFFFFu, nullptr, c->stream));
+        CK(sah_build(buffers(c, c->sc->tlas), false, nullptr, c->stream));
     else CK(lbvh_build(buffers(c, c->sc->tlas), c->stream));
     CK(wide_records(buffers(c, c->sc->tlas), c->sc->tlas.wide.as<WideNode>(), c->stream));
     CK(inst_records(c->sc->tlas.order.as<uint32_t>(), n, c->sc->instDev.as<DevInstance>(), c->sc->blasTable.as<DevBlas>(),
@@ -374,7 +449,11 @@ rg_status ensure_wavefront(rg_ctx* c, size_t paths, WavefrontBuffers& w, size_t 
     TRY(ensure(c, c->wfQP1, 4 * Q));
     TRY(ensure(c, c->wfHitTUV, 16 * Q));
     TRY(ensure(c, c->wfHitInst, 4 * Q));
-    TRY(ensure(c, c->wfCounts, 16));
+    TRY(ensure(c, c->wfOverflow, 4 * Q));
+    if (!c->wfCounts.p) {  // the overflow list length and the finished-block count start at zero
+        TRY(ensure(c, c->wfCounts, 32));
+        CK(cudaMemsetAsync(c->wfCounts.p, 0, 32, c->stream));
+    }
     w.payload = c->wfPayload.as<float4>();
     w.meta = c->wfMeta.as<int2>();
     w.frames = c->wfFrames.p;
@@ -387,6 +466,7 @@ rg_status ensure_wavefront(rg_ctx* c, size_t paths, WavefrontBuffers& w, size_t 
     w.hitTUV = c->wfHitTUV.as<float4>();
     w.hitInst = c->wfHitInst.as<uint32_t>();
     w.counts = c->wfCounts.as<uint32_t>();
+    w.overflow = c->wfOverflow.as<uint32_t>();
     return RG_OK;
 }
 
@@ -449,7 +529,7 @@ rg_status rg_destroy(rg_ctx* c) {
     DevBuf* bufs[] = {&c->keysA, &c->keysB, &c->valsA, &c->valsB, &c->blockHist, &c->bounds, &c->base, &c->normal, &c->rough,
                       &c->finalImg, &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC,
                       &c->tmpD, &c->samples, &c->workCounter, &c->wfPayload, &c->wfMeta, &c->wfFrames, &c->wfQO0, &c->wfQO1,
-                      &c->wfQD0, &c->wfQD1, &c->wfQP0, &c->wfQP1, &c->wfHitTUV, &c->wfHitInst, &c->wfCounts, &c->jobTable,
+                      &c->wfQD0, &c->wfQD1, &c->wfQP0, &c->wfQP1, &c->wfHitTUV, &c->wfHitInst, &c->wfCounts, &c->wfOverflow, &c->jobTable,
                       &c->slotJob, &c->slotSample, &c->sortKeys, &c->sortPerm, &c->sortHist, &c->bBase, &c->bNormal, &c->bRough,
                       &c->bFinal, &c->bFxaa, &c->batchFb};
     for (DevBuf* b : bufs) release(c, *b);
@@ -498,12 +578,44 @@ rg_status rg_upload_geometry(rg_ctx* c, const rg_vertex* v, uint32_t nv, const u
     c->sc->nv = nv;
     c->sc->ni = ni;
     c->sc->nm = nm;
+    c->sc->hostIdx.assign(idx, idx + ni);
+    c->sc->hostMat.resize(nv);
+    for (uint32_t k = 0; k < nv; ++k) c->sc->hostMat[k] = v[k].matIndex;
+    c->sc->maxIdx.clear();
+    c->sc->maxMat.clear();
+    ++c->sc->gen;
     return RG_OK;
 }
 
 rg_status rg_update_vertices(rg_ctx* c, uint32_t first, const rg_vertex* v, uint32_t n) {
     if (!c || (n && !v) || (uint64_t)first + n > c->sc->nv) return fail(c, RG_ERR_INVALID_ARG, "vertex range outside the uploaded buffer");
     TRY(set_device(c));
+    std::vector<uint32_t> before(c->sc->hostMat.begin() + first, c->sc->hostMat.begin() + first + n);
+    bool matChanged = false;
+    for (uint32_t k = 0; k < n; ++k) {
+        matChanged |= before[k] != v[k].matIndex;
+        c->sc->hostMat[first + k] = v[k].matIndex;
+    }
+    if (matChanged) {  // the instances of the current TLAS must still reach only uploaded materials
+        SceneState& st = *c->sc;
+        st.maxMat.clear();
+        std::vector<uint32_t> oldMax(st.blas.size());
+        for (uint32_t b = 0; b < st.blas.size(); ++b) {  // the BLASes' material bounds
+            BlasRec& r = st.blas[b];
+            oldMax[b] = r.maxMat;
+            if (r.gen == st.gen && r.triCount) r.maxMat = range_max_material(st, r.vOff, r.iOff, r.triCount);
+        }
+        std::string why;
+        for (const rg_instance& in : st.hostInst)
+            if (!instance_ok(st, in, &why)) {  // refused: nothing was copied, nothing changes
+                std::copy(before.begin(), before.end(), st.hostMat.begin() + first);
+                for (uint32_t b = 0; b < st.blas.size(); ++b) st.blas[b].maxMat = oldMax[b];
+                st.maxMat.clear();
+                return fail(c, RG_ERR_INVALID_ARG, "vertex update: " + why);
+            }
+        for (uint32_t b = 0; b < st.blas.size(); ++b)
+            if (st.blas[b].maxMat != oldMax[b]) TRY(upload_blas_entry(c, b));
+    }
     if (n) CK(cudaMemcpyAsync(c->sc->vertices.as<rg_vertex>() + first, v, sizeof(rg_vertex) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     return RG_OK;
 }
@@ -526,32 +638,30 @@ rg_status rg_update_materials(rg_ctx* c, uint32_t first, const rg_material* m, u
 
 rg_status rg_build_blas(rg_ctx* c, uint32_t vOff, uint32_t iOff, uint32_t triCount, uint32_t* out) {
     if (!c || !out) return RG_ERR_INVALID_ARG;
-    if ((uint64_t)iOff + 3ull * triCount > c->sc->ni) return fail(c, RG_ERR_INVALID_ARG, "triangle range outside the index buffer");
     if (triCount >= 0x7FFFFFFFu) return fail(c, RG_ERR_INVALID_ARG, "too many triangles");
+    std::string why;
+    if (!range_ok(*c->sc, vOff, iOff, triCount, ~0u, &why)) return fail(c, RG_ERR_INVALID_ARG, why);
     TRY(set_device(c));
-    // vertex references of this range must stay inside the vertex buffer (checked on the host copy
-    // the caller passed at upload time would be cheaper, but the index buffer lives on the device)
     uint32_t b = (uint32_t)c->sc->blas.size();
     c->sc->blas.emplace_back();
     BlasRec& r = c->sc->blas.back();
     r.vOff = vOff;
     r.iOff = iOff;
+    r.triCount = triCount;
+    r.maxMat = triCount ? range_max_material(*c->sc, vOff, iOff, triCount) : 0u;
+    r.gen = c->sc->gen;
     TRY(ensure_bvh(c, r.bvh, triCount));
     TRY(ensure(c, r.tris, 48ull * (triCount ? triCount : 1)));
     if (triCount) {
         CK(tri_boxes(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), vOff, iOff, triCount, r.bvh.primBoxes.as<float>(), c->stream));
         // binned SAH where it fits (once per scene load; refits keep its topology), else the LBVH
-        bool sah = !(c->flags & RG_FLAG_BLAS_LBVH) && triCount > 1 && triCount <= kSahBlasMaxPrims;
+        const bool sah = !(c->flags & RG_FLAG_BLAS_LBVH) && triCount > 1 && triCount <= kSahBlasMaxPrims;
         if (sah) {
-            TRY(ensure(c, c->tmpD, 4));
-            uint32_t levels = 0;
-            CK(sah_build(buffers(c, r.bvh), true, kSahMaxLevels, c->tmpD.as<uint32_t>(), c->stream));
-            CK(cudaMemcpyAsync(&levels, c->tmpD.p, 4, cudaMemcpyDeviceToHost, c->stream));
-            CK(cudaStreamSynchronize(c->stream));
-            sah = levels <= kSahMaxLevels;
-            if (sah) CK(cudaMemsetAsync(r.bvh.morton.p, 0, 4ull * triCount, c->stream));  // no Morton order in an SAH tree
+            CK(sah_build(buffers(c, r.bvh), true, nullptr, c->stream));
+            CK(cudaMemsetAsync(r.bvh.morton.p, 0, 4ull * triCount, c->stream));  // no Morton order in an SAH tree
+        } else {
+            CK(lbvh_build(buffers(c, r.bvh), c->stream));
         }
-        if (!sah) CK(lbvh_build(buffers(c, r.bvh), c->stream));
         CK(wide_records(buffers(c, r.bvh), r.bvh.wide.as<WideNode>(), c->stream));
         CK(tri_records(c->sc->vertices.as<rg_vertex>(), c->sc->indices.as<uint32_t>(), vOff, iOff, r.bvh.order.as<uint32_t>(), triCount,
                        r.tris.as<float4>(), c->stream));
@@ -577,6 +687,8 @@ rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
     BlasRec& r = c->sc->blas[b];
     uint32_t n = r.bvh.n;
     if (!n) return RG_OK;
+    std::string why;  // geometry uploaded since the build must still hold the BLAS's triangles
+    if (!range_ok(*c->sc, r.vOff, r.iOff, n, ~0u, &why)) return fail(c, RG_ERR_INVALID_ARG, "refit: " + why);
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
     if (!fe->hasRefit) CK(cudaEventRecord(fe->ev[EV_REFIT0], c->stream));
@@ -596,10 +708,14 @@ rg_status rg_refit_blas(rg_ctx* c, uint32_t b) {
 
 rg_status rg_build_tlas(rg_ctx* c, const rg_instance* inst, uint32_t n) {
     if (!c || (n && !inst)) return RG_ERR_INVALID_ARG;
+    std::string why;
+    for (uint32_t i = 0; i < n; ++i)
+        if (!instance_ok(*c->sc, inst[i], &why)) return fail(c, RG_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": " + why);
     TRY(set_device(c));
     TRY(ensure(c, c->sc->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
     if (n) CK(cudaMemcpyAsync(c->sc->instIn.p, inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-    return build_tlas_from_device_instances(c, n);
+    c->sc->hostInst.assign(inst, inst + n);
+    return build_tlas_from_device_instances(c, n, false);
 }
 
 rg_status rg_build_tlas_device(rg_ctx* c, const rg_instance* d_inst, uint32_t n) {
@@ -607,7 +723,8 @@ rg_status rg_build_tlas_device(rg_ctx* c, const rg_instance* d_inst, uint32_t n)
     TRY(set_device(c));
     TRY(ensure(c, c->sc->instIn, sizeof(rg_instance) * (size_t)(n ? n : 1)));
     if (n) CK(cudaMemcpyAsync(c->sc->instIn.p, d_inst, sizeof(rg_instance) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
-    return build_tlas_from_device_instances(c, n);
+    c->sc->hostInst.clear();
+    return build_tlas_from_device_instances(c, n, true);
 }
 
 rg_status rg_set_resolution(rg_ctx* c, uint32_t w, uint32_t h) {
@@ -875,6 +992,7 @@ static rg_status read_stats(rg_ctx* c, rg_stats* s, int base) {
     s->tris = v[base + 5];
     s->stack_overflows = v[base + 6];
     s->iterations = base == 0 ? (uint64_t)c->lastIterations : 0;
+    s->deep_overflows = v[base + 7];
     return RG_OK;
 }
 
@@ -984,10 +1102,48 @@ rg_status rg_trace_rays(rg_ctx* c, const float* rays, uint32_t n, float* tuv, ui
     TRY(ensure(c, c->tmpC, 12ull * n));
     TRY(ensure(c, c->tmpD, 8ull * n));
     CK(cudaMemcpyAsync(c->tmpA.p, rays, 32ull * n, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_trace_rays(scene_of(*c->sc), c->tmpA.as<float>(), n, c->tmpC.as<float>(), c->tmpD.as<uint32_t>(), c->stream));
+    CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));  // rg_get_stats then reports this call's overflows
+    CK(launch_trace_rays(scene_of(*c->sc), c->tmpA.as<float>(), n, c->tmpC.as<float>(), c->tmpD.as<uint32_t>(),
+                         c->counters.as<unsigned long long>(), c->tune.depth, c->stream));
     CK(cudaMemcpyAsync(tuv, c->tmpC.p, 12ull * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(ids, c->tmpD.p, 8ull * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return RG_OK;
+}
+
+rg_status rg_trace_rays_device(rg_ctx* c, const float* d_rays, uint32_t n, float* d_tuv, uint32_t* d_ids) {
+    if (!c || (n && (!d_rays || !d_tuv || !d_ids))) return RG_ERR_INVALID_ARG;
+    if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
+    if (!n) return RG_OK;
+    TRY(set_device(c));
+    // the queue, hit records and overflow list of the frame loop, sized for n rays (no path state)
+    const size_t Q = n;
+    TRY(ensure(c, c->wfQO0, 16 * Q));
+    TRY(ensure(c, c->wfQO1, 16));
+    TRY(ensure(c, c->wfQD0, 16 * Q));
+    TRY(ensure(c, c->wfQD1, 16));
+    TRY(ensure(c, c->wfHitTUV, 16 * Q));
+    TRY(ensure(c, c->wfHitInst, 4 * Q));
+    TRY(ensure(c, c->wfOverflow, 4 * Q));
+    if (!c->wfCounts.p) {
+        TRY(ensure(c, c->wfCounts, 32));
+        CK(cudaMemsetAsync(c->wfCounts.p, 0, 32, c->stream));
+    }
+    TraceParams tp;
+    std::memset(&tp, 0, sizeof(tp));
+    tp.scene = scene_of(*c->sc);
+    tp.counters = c->counters.as<unsigned long long>();
+    tp.countVisits = (c->flags & RG_FLAG_COUNT_VISITS) ? 1 : 0;
+    tp.wf.qO[0] = c->wfQO0.as<float4>();
+    tp.wf.qO[1] = c->wfQO1.as<float4>();
+    tp.wf.qD[0] = c->wfQD0.as<float4>();
+    tp.wf.qD[1] = c->wfQD1.as<float4>();
+    tp.wf.hitTUV = c->wfHitTUV.as<float4>();
+    tp.wf.hitInst = c->wfHitInst.as<uint32_t>();
+    tp.wf.counts = c->wfCounts.as<uint32_t>();
+    tp.wf.overflow = c->wfOverflow.as<uint32_t>();
+    CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
+    CK(launch_trace_queue(tp, d_rays, n, d_tuv, d_ids, c->stream));
     return RG_OK;
 }
 

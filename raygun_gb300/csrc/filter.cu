@@ -460,12 +460,18 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_filter_conv(const __grid_co
                     };
                     if (a.y) put(a.y, v, nullptr);
                     if (a.add) {
+                        // forward skip (a.ya): the sum of the stored BF16 activations, x5 = bf16(bf16(y4) + y1);
+                        // backward (the skip gradient into layer 1's): FP32 sum, rounded once on the way out
+                        const bool storedSum = a.ya != nullptr;
 #pragma unroll
                         for (int c = 0; c < NC; ++c) {
                             const uint4 av = kPre ? addPre[kPre ? r : 0][c] : aux_load(a.add, y, c);
                             const bf16* hv = reinterpret_cast<const bf16*>(&av);
 #pragma unroll
-                            for (int e = 0; e < 8; ++e) v[8 * c + e] += __bfloat162float(hv[e]);
+                            for (int e = 0; e < 8; ++e) {
+                                const float own = storedSum ? __bfloat162float(__float2bfloat16(v[8 * c + e])) : v[8 * c + e];
+                                v[8 * c + e] = own + __bfloat162float(hv[e]);
+                            }
                         }
                     }
                     if (a.ya) put(a.ya, v, nullptr);

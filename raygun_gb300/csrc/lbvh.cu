@@ -348,7 +348,9 @@ __global__ void k_wide_records(const float* __restrict__ primBoxes, const uint32
 // 16 bins per axis (shared-memory atomics on order-preserving integer images of the bounds), evaluates
 // the 45 surface-area-heuristic splits, partitions the range stably with ballots, and emits its
 // children (single primitives become leaf refs, the rest next-level tasks).  Every split leaves both
-// sides non-empty, so each level shortens every range and the build ends after at most n - 1 levels.
+// sides non-empty, so each level shortens every range.  From level medianLevel on, ranges are halved
+// without binning, so no tree is deeper than medianLevel + ceil(log2 n) levels, whatever the centroid
+// distribution (a surface-area split can peel one primitive off a range per level).
 // Internal nodes are numbered in level order (a level's tasks follow the previous levels' nodes), so
 // a task is just its range.  The result has the LBVH's layout (order, left, right, nodeBoxes), so
 // records, refits and traversal are shared.
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
                                                                  uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
                                                                  uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
                                                                  uint2* __restrict__ tasksA, uint2* __restrict__ tasksB,
-                                                                 uint32_t maxLevels, uint32_t* __restrict__ levelsOut) {
+                                                                 uint32_t medianLevel, uint32_t* __restrict__ levelsOut) {
     __shared__ int bLo[kSahWarps][3][kSahBins][3], bHi[kSahWarps][3][kSahBins][3];
     __shared__ int bCnt[kSahWarps][3][kSahBins];
     __shared__ uint32_t nCur, nNext, baseCur, baseNext, levels;
@@ -389,10 +391,7 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
     for (;;) {
         const uint32_t count = nCur;
         if (count == 0) break;
-        if (levels >= maxLevels) {  // deeper than the caller accepts: report and stop (the tree is unfinished)
-            if (threadIdx.x == 0 && levelsOut) *levelsOut = 0xFFFFFFFFu;
-            return;
-        }
+        const bool median = levels >= medianLevel;  // from here on ranges are halved: the depth stays bounded
         for (uint32_t t = warp; t < count; t += kSahWarps) {
             const uint2 tk = cur[t];
             const uint32_t b = tk.x, e = tk.y, node = baseCur + t;
@@ -430,6 +429,13 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
                 const float ext = chi[a] - clo[a];
                 scale[a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
             }
+            auto bin_of = [&](const float* bx, int a) {
+                const float c = 0.5f * (bx[a] + bx[3 + a]);
+                return max(0, min((int)((c - clo[a]) * scale[a]), kSahBins - 1));
+            };
+            float bestCost = INFINITY;
+            int bestCand = -1;
+            if (!median) {
             for (int k = lane; k < 3 * kSahBins; k += 32) {
                 const int a = k / kSahBins, bn = k % kSahBins;
                 bCnt[warp][a][bn] = 0;
@@ -440,10 +446,6 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
                 }
             }
             __syncwarp();
-            auto bin_of = [&](const float* bx, int a) {
-                const float c = 0.5f * (bx[a] + bx[3 + a]);
-                return max(0, min((int)((c - clo[a]) * scale[a]), kSahBins - 1));
-            };
             for (uint32_t i = b + lane; i < e; i += 32) {
                 const float* bx = boxes + 6 * (size_t)order[i];
 #pragma unroll
@@ -459,8 +461,6 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
                 }
             }
             __syncwarp();
-            float bestCost = INFINITY;
-            int bestCand = -1;
             for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
                 const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
                 if (scale[a] <= 0.0f) continue;
@@ -496,6 +496,7 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
                     bestCand = oi;
                 }
             }
+            }  // !median
             uint32_t mid = b + (e - b) / 2;  // no usable split (coincident centroids): halve the range
             if (bestCand >= 0) {
                 const int a = bestCand / (kSahBins - 1), sp = bestCand % (kSahBins - 1) + 1;
@@ -563,14 +564,16 @@ __global__ void k_parents(const uint32_t* __restrict__ left, const uint32_t* __r
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i + 1 >= n) return;
     const uint32_t L = left[i], R = right[i];
-    parents[(L & kLeaf) ? (n - 1) + (L & ~kLeaf) : L] = i;
-    parents[(R & kLeaf) ? (n - 1) + (R & ~kLeaf) : R] = i;
+    for (const uint32_t c : {L, R}) {  // child refs of a finished tree are in range; anything else is skipped
+        const uint32_t slot = (c & kLeaf) ? (n - 1) + (c & ~kLeaf) : c;
+        if (((c & kLeaf) && (c & ~kLeaf) < n) || (!(c & kLeaf) && c > 0 && c + 1 < n)) parents[slot] = i;
+    }
     if (i == 0) parents[0] = 0xFFFFFFFFu;
 }
 
 // ---- instances ----------------------------------------------------------------------------------
 __global__ void k_instances(const rg_instance* __restrict__ in, uint32_t n, const DevBlas* __restrict__ blas, uint32_t nblas,
-                            DevInstance* __restrict__ out, float* __restrict__ boxes) {
+                            DevInstance* __restrict__ out, float* __restrict__ boxes, bool checkOffsets, uint32_t nm) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     rg_instance I = in[i];
@@ -583,6 +586,10 @@ __global__ void k_instances(const rg_instance* __restrict__ in, uint32_t n, cons
     float c20 = a10 * a21 - a11 * a20, c21 = a01 * a20 - a00 * a21, c22 = a00 * a11 - a01 * a10;
     float det = (a00 * c00 + a01 * c10) + a02 * c20;
     bool ok = (det != 0.0f) && isfinite(det) && I.blas < nblas && (I.mask & 0xFFu) != 0u;
+    if (ok && checkOffsets && blas[I.blas].n > 0) {
+        const DevBlas& B = blas[I.blas];
+        ok = I.vertexBufferOffset == B.vOff && I.indexBufferOffset == B.iOff && (uint64_t)I.materialBufferOffset + B.maxMat < nm;
+    }
     float id = ok ? 1.0f / det : 0.0f;
     float r[9] = {c00 * id, c01 * id, c02 * id, c10 * id, c11 * id, c12 * id, c20 * id, c21 * id, c22 * id};
     DevInstance d;
@@ -648,9 +655,9 @@ cudaError_t inst_records(const uint32_t* order, uint32_t n, const DevInstance* i
 }
 
 cudaError_t setup_instances(const rg_instance* in, uint32_t n, const DevBlas* blas, uint32_t nblas, DevInstance* out, float* boxes,
-                            cudaStream_t s) {
+                            bool checkOffsets, uint32_t nm, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_instances<<<blocks(n, 128), 128, 0, s>>>(in, n, blas, nblas, out, boxes);
+    k_instances<<<blocks(n, 128), 128, 0, s>>>(in, n, blas, nblas, out, boxes, checkOffsets, nm);
     count_launch();
     return cudaGetLastError();
 }
@@ -664,11 +671,11 @@ cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t maxLevels, uint32_t* levels, cudaStream_t s) {
+cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t* levels, cudaStream_t s) {
     if (b.n <= 1) return cudaSuccess;
     // scratch: the sort buffers (n words each); at most n / 2 tasks per level, 2 words each
     k_sah_build<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes,
-                                              reinterpret_cast<uint2*>(b.valsA), reinterpret_cast<uint2*>(b.valsB), maxLevels,
+                                              reinterpret_cast<uint2*>(b.valsA), reinterpret_cast<uint2*>(b.valsB), kSahMedianLevel,
                                               levels);
     count_launch();
     if (parents) {

@@ -45,9 +45,12 @@ struct DevBlas {
     const WideNode* wide;
     const float4* tris;  // 3 float4 per sorted leaf: v0 (w = primitive id bits), v1, v2
     uint32_t n;          // triangle count
-    uint32_t pad;
+    uint32_t maxMat;     // largest matIndex of the vertices its triangles reference
     float root[6];       // root box (lo xyz, hi xyz)
+    uint32_t vOff, iOff; // vertex and index offsets it was built from (range-checked on the host)
+    uint32_t pad0, pad1;
 };
+static_assert(sizeof(DevBlas) == 64, "BLAS table entry");
 
 // per-instance record read by the traversal and shading code
 struct __align__(16) DevInstance {
@@ -140,21 +143,24 @@ cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s);  // topology kept, primBoxes changed
 cudaError_t wide_records(const LbvhBuffers& b, WideNode* out, cudaStream_t s);  // after build / refit
 // binned-SAH BVH2 over b.primBoxes in the LBVH's layout (order, left, right, nodeBoxes), one CTA;
-// parents (for refits) on request.  *levels (device word, nullable) receives the number of levels, or
-// 0xFFFFFFFF when the tree would have more than maxLevels (the build then stops unfinished).  The
-// TLAS uses it up to kSahMaxPrims instances (it is rebuilt every frame), BLASes up to
-// kSahBlasMaxPrims triangles (built once per scene load) when the tree has at most kSahMaxLevels
-// levels (within the traversal stack's reach), the LBVH otherwise.
+// parents (for refits) on request.  *levels (device word, nullable) receives the number of levels.
+// From level kSahMedianLevel on, ranges are halved without binning, so a tree has at most
+// kSahMedianLevel + ceil(log2 n) levels.  The TLAS uses it up to kSahMaxPrims instances (it is
+// rebuilt every frame), BLASes up to kSahBlasMaxPrims triangles (built once per scene load), the
+// LBVH otherwise.
 constexpr uint32_t kSahMaxPrims = 8192;
 constexpr uint32_t kSahBlasMaxPrims = 1u << 18;
-constexpr uint32_t kSahMaxLevels = 28;
-cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t maxLevels, uint32_t* levels, cudaStream_t s);
+constexpr uint32_t kSahMedianLevel = 32;
+cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t* levels, cudaStream_t s);
 cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes,
                       cudaStream_t s);
 cudaError_t tri_records(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, const uint32_t* order, uint32_t n,
                         float4* tris, cudaStream_t s);
+// world boxes and shading records of n instances.  checkOffsets (instances from device memory, which
+// the host never saw): an instance is also invalid -- never hit -- unless its vertex and index offsets
+// are its BLAS's own and its material offset keeps the BLAS's materials below nm.
 cudaError_t setup_instances(const rg_instance* in, uint32_t n, const DevBlas* blas, uint32_t nblas, DevInstance* out,
-                            float* boxes, cudaStream_t s);
+                            float* boxes, bool checkOffsets, uint32_t nm, cudaStream_t s);
 // the TLAS leaf records (after the TLAS build; again after a BLAS refit, which moves root boxes)
 cudaError_t inst_records(const uint32_t* order, uint32_t n, const DevInstance* inst, const DevBlas* blas, InstRec* out,
                          cudaStream_t s);
@@ -169,7 +175,9 @@ struct WavefrontBuffers {
     uint32_t* qPath[2];
     float4* hitTUV;    // per queue slot: t, u, v, primitive bits
     uint32_t* hitInst; // per queue slot: instance or 0xFFFFFFFF (miss)
-    uint32_t* counts;  // [0], [1] queue lengths, [2] trace work counter
+    uint32_t* counts;  // [0], [1] queue lengths, [2] trace work counter, [3] overflow list length,
+                       // [4] trace blocks finished (both zero between launches)
+    uint32_t* overflow; // per queue slot: slots of rays whose short traversal stack overflowed
 };
 
 // one render job of a batch: a scene, its UBO and its image size.  Work items of the batch are
@@ -252,7 +260,12 @@ int batch_graph_kernels(const TraceTune& tune, int* perBody);
 // raygen.rgen:36-38 for one job of a batch: average its samples into RGBA16F G-buffers
 cudaError_t launch_resolve_job(const float4* samples, const JobDesc& hostJob, uint2* base, uint2* normal, uint2* rough,
                                cudaStream_t s);
-cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
+// closest hits of n rays (8 floats each, device memory) by one round of the frame loop's traversal
+// kernel (k_wf_trace): rays into queue 0 of p.wf, one launch, hit records out in rg_trace_rays' layout
+cudaError_t launch_trace_queue(const TraceParams& p, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
+// closest hits of n rays with a traversal stack of `depth` (16, 24, 32 or 48) entries
+cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids,
+                              unsigned long long* counters, int depth, cudaStream_t s);
 
 // ---- learned roughness filter (filter.cu) ----
 // one 3x3 convolution of NHWC BF16 activations (x 16-byte aligned): v = conv(x, w) + bias, then

@@ -191,13 +191,16 @@ constexpr int kTraceThreads = 128;
 // Beside it, six floats per thread keep the world-space ray's origin and clamped inverse direction
 // while the ray is inside a BLAS (the world direction itself stays in registers), so leaving the BLAS
 // restores them instead of dividing again.
+// The last of the DEPTH words flags an overflow (a push that found the other DEPTH - 1 entries
+// full), so the flag costs the traversal loop neither a register nor shared memory beyond the stack.
 template <int THREADS, int DEPTH>
 struct SmemStackT {
-    static constexpr int kDepth = DEPTH;
+    static constexpr int kDepth = DEPTH - 1;
     uint32_t* base;  // &stack[0][threadIdx.x]
     float* saved;    // &world[0][threadIdx.x]
     __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i * THREADS]; }
     __device__ __forceinline__ float& w(int i) const { return saved[i * THREADS]; }
+    __device__ __forceinline__ uint32_t& over() const { return base[(DEPTH - 1) * THREADS]; }
 };
 // the same stack in (L1-cached) local memory
 #ifndef RG_STACK_SMEM
@@ -205,11 +208,12 @@ struct SmemStackT {
 #endif
 template <int DEPTH>
 struct LocalStackT {
-    static constexpr int kDepth = DEPTH;
+    static constexpr int kDepth = DEPTH - 1;
     uint32_t* base;
     float* saved;
     __device__ __forceinline__ uint32_t& operator[](int i) const { return base[i]; }
     __device__ __forceinline__ float& w(int i) const { return saved[i]; }
+    __device__ __forceinline__ uint32_t& over() const { return base[DEPTH - 1]; }
 };
 #define RG_DECLARE_SMEM_STACK(name, THREADS, DEPTH)      \
     __shared__ uint32_t name##_mem[DEPTH][THREADS];      \
@@ -251,8 +255,10 @@ struct Trav {
     bool inBlas, active;
 };
 
+template <class STACK>
 __device__ __forceinline__ void trav_begin(Trav& T, const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz,
-                                           float tmin, float tmax) {
+                                           float tmin, float tmax, const STACK& stack) {
+    stack.over() = 0u;
     T.h.hit = false;
     T.h.t = tmax;
     T.h.u = T.h.v = 0.0f;
@@ -305,7 +311,7 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
             for (int j = 3; j >= 1; --j)
                 if (t[j] != INFINITY) {
                     if (T.sp < STACK::kDepth) stack[T.sp++] = r[j];
-                    else vc.overflow++;
+                    else stack.over() = 1u;
                 }
             T.ref = r[0];
             return;
@@ -346,7 +352,7 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
                         T.ref = bn == 1 ? kLeaf : 0u;
                         return;
                     }
-                    vc.overflow++;
+                    stack.over() = 1u;
                 }
             }
         }
@@ -372,12 +378,42 @@ __device__ __forceinline__ void trav_step(Trav& T, const DevScene& sc, const STA
         }
 }
 
+// Deep re-trace.  The short stack of the kernels (kTraversalStack entries in shared memory, or the
+// batch tuner's depth) holds the far children of the records on the ray's current path: up to 3 per
+// 4-wide record level, plus one marker while the ray is inside a BLAS.  Deep trees whose boxes the
+// ray hits many at a time can need more.  A push that finds the short stack full sets Trav::over
+// instead, and when that ray's traversal ends it is traced again from the start with this stack of
+// kDeepStack entries in local memory, so its result is complete.  Every tree this library builds has
+// at most 64 BVH2 levels (LBVH: 30 code bits plus at most 32 index bits of tie-break, one level per
+// bit; binned SAH: kSahMedianLevel + 18), i.e. at most 32 record levels, so a TLAS path, a marker and
+// a BLAS path take at most 3 * 32 + 1 + 3 * 32 = 193 entries.  Should a push still find it full, the
+// ray is counted in counters[7] (rg_stats.deep_overflows), never silently.
+constexpr int kDeepStack = 196;  // 195 entries and the overflow flag
+__device__ __noinline__ void retrace_deep(const DevScene* sc, float4 o, float4 d, Hit* out, unsigned long long* counters) {
+    uint32_t mem[kDeepStack];
+    float world[6];
+    const LocalStackT<kDeepStack> st{mem, world};
+    VisitCounts vc = {0, 0, 0};
+    Trav T;
+    trav_begin(T, *sc, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, st);
+    while (T.active) trav_step<false>(T, *sc, st, vc);
+    if (st.over() && counters) {
+        atomicAdd(counters + 7, 1ull);
+        atomicAdd(counters + 15, 1ull);
+    }
+    *out = T.h;
+}
+
 template <bool COUNT, class STACK>
 __device__ Hit closest_hit(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
-                           const STACK& stack, VisitCounts& vc) {
+                           const STACK& stack, VisitCounts& vc, unsigned long long* counters) {
     Trav T;
-    trav_begin(T, sc, ox, oy, oz, dx, dy, dz, tmin, tmax);
+    trav_begin(T, sc, ox, oy, oz, dx, dy, dz, tmin, tmax, stack);
     while (T.active) trav_step<COUNT>(T, sc, stack, vc);
+    if (stack.over()) {
+        vc.overflow++;
+        retrace_deep(&sc, make_float4(ox, oy, oz, tmin), make_float4(dx, dy, dz, tmax), &T.h, counters);
+    }
     return T.h;
 }
 
@@ -836,13 +872,15 @@ __device__ __forceinline__ void start_sample(const rg_ubo& U, const V3 camO, uin
 enum : int { kIdle = 0, kTraverse = 1, kResult = 2 };
 
 // starts the traversal of the pending trace; mask-0 traces and zero directions need none
-__device__ __forceinline__ int begin_ray(Trav& T, const DevScene& sc, const RayReq& ray) {
+template <class STACK>
+__device__ __forceinline__ int begin_ray(Trav& T, const DevScene& sc, const RayReq& ray, const STACK& stack) {
     if (ray.masked) {
         T.h.hit = false;
         T.active = false;
+        stack.over() = 0u;
         return kResult;
     }
-    trav_begin(T, sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax);
+    trav_begin(T, sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, stack);
     return T.active ? kTraverse : kResult;
 }
 
@@ -856,7 +894,7 @@ __device__ __forceinline__ int begin_ray(Trav& T, const DevScene& sc, const RayR
 // enumerate 8x4 pixel tiles, then pixels, then samples, so consecutive items are coherent.
 // Each sample's payload sums go to `samples` (12 floats); k_resolve averages them in sample order.
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(const TraceParams P) {
+__global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(const __grid_constant__ TraceParams P) {
     RG_DECLARE_STACK(stk);
     const DevScene& sc = P.scene;
     const rg_ubo& U = P.ubo;
@@ -896,7 +934,7 @@ __global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(co
             if (state == kResult) {
                 // closest-hit / miss shading of the finished trace, up to the next trace
                 if (shade_step(sc, L, maxRec, T.h, p, ray, frames, fsp, cur, cnt)) {
-                    state = begin_ray(T, sc, ray);
+                    state = begin_ray(T, sc, ray, stk);
                 } else {
                     float4* o = P.samples + 3 * ((size_t)(py * P.W + px) * S + sample);
                     o[0] = make_float4(p.hitValue.x, p.hitValue.y, p.hitValue.z, p.reflectContribution);
@@ -925,7 +963,7 @@ __global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(co
                             start_sample(U, camO, px, py, P.W, P.H, (int)sample, aaRow, p, ray, P.glossySeed);
                             cnt.primary++;
                             fsp = 0;
-                            state = begin_ray(T, sc, ray);
+                            state = begin_ray(T, sc, ray, stk);
                         }
                     }
                 }
@@ -937,6 +975,11 @@ __global__ void __launch_bounds__(kTraceThreads, RG_TRACE_MIN_BLOCKS) k_trace(co
             for (int k = 0; k < RG_TRACE_STEPS; ++k) {
                 trav_step<COUNT>(T, sc, stk, vc);
                 if (!T.active) {
+                    if (stk.over()) {
+                        vc.overflow++;
+                        retrace_deep(&sc, make_float4(ray.o.x, ray.o.y, ray.o.z, ray.tmin), make_float4(ray.d.x, ray.d.y, ray.d.z, ray.tmax),
+                                     &T.h, P.counters);
+                    }
                     state = kResult;
                     break;
                 }
@@ -1162,8 +1205,12 @@ __global__ void __launch_bounds__(256) k_wfb_raygen(const TraceParams P) {
 #ifndef RG_INNER_ROUNDS
 #define RG_INNER_ROUNDS 3
 #endif
+// Shared memory: the stack (DEPTH words) and the parked world ray (6 words) per thread, nothing else:
+// at 128 threads x 48 words that is 27,648 B, and 7 blocks (plus the 1 KB the driver reserves per
+// block) fill the 196 KB shared-memory carve-out exactly.  One more byte per block moves the SM to
+// the 228 KB carve-out and halves the L1 left for BVH records (measured: trace stage +5 %).
 template <bool COUNT, bool BATCH, int THREADS, int DEPTH>
-__global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k_wf_trace(const TraceParams P, int q) {
+__global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k_wf_trace(const __grid_constant__ TraceParams P, int q) {
     RG_DECLARE_SMEM_STACK(stk, THREADS, DEPTH);
     const WavefrontBuffers& wf = P.wf;
     const bool first = !BATCH && P.firstRound;
@@ -1177,6 +1224,17 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
     uint32_t slot = 0;
     const DevScene* scp = nullptr;  // BATCH: scene of the lane's ray
 #define RG_SC (BATCH ? *scp : P.scene)
+    // a finished ray's hit record; a ray whose short stack overflowed also joins the overflow list,
+    // whose rays the kernel's last block traces again with the deep stack (below)
+#define RG_WF_HIT_OUT()                                                                      \
+    do {                                                                                     \
+        if (stk.over()) {                                                                    \
+            vc.overflow++;                                                                   \
+            wf.overflow[atomicAdd(wf.counts + 3, 1u)] = slot;                                \
+        }                                                                                    \
+        wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));       \
+        wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;                                 \
+    } while (0)
     bool exhausted = false;
     for (;;) {
         const unsigned idle = __ballot_sync(0xFFFFFFFFu, !T.active);
@@ -1198,7 +1256,7 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
                         Payload p0;
                         RayReq r0;
                         if (frame_work_item(P, k, path, p0, r0)) {
-                            trav_begin(T, P.scene, r0.o.x, r0.o.y, r0.o.z, r0.d.x, r0.d.y, r0.d.z, r0.tmin, r0.tmax);
+                            trav_begin(T, P.scene, r0.o.x, r0.o.y, r0.o.z, r0.d.x, r0.d.y, r0.d.z, r0.tmin, r0.tmax, stk);
                             if (!T.active) {
                                 wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
                                 wf.hitInst[slot] = 0xFFFFFFFFu;
@@ -1208,7 +1266,7 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
                         slot = P.perm ? P.perm[k] : k;
                         if (BATCH) scp = &P.jobs[P.slotJob[wf.qPath[q][slot]]].scene;
                         const float4 o = wf.qO[q][slot], d = wf.qD[q][slot];
-                        trav_begin(T, RG_SC, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w);
+                        trav_begin(T, RG_SC, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, stk);
                         if (!T.active) {  // zero direction or the scene box missed
                             wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
                             wf.hitInst[slot] = 0xFFFFFFFFu;
@@ -1229,18 +1287,12 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
                 if (!__any_sync(0xFFFFFFFFu, inner)) break;
                 if (inner) {
                     trav_step<COUNT>(T, RG_SC, stk, vc);
-                    if (!T.active) {
-                        wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
-                        wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;
-                    }
+                    if (!T.active) RG_WF_HIT_OUT();
                 }
             }
             if (T.active && (T.ref & kLeaf)) {
                 trav_step<COUNT>(T, RG_SC, stk, vc);
-                if (!T.active) {
-                    wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
-                    wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;
-                }
+                if (!T.active) RG_WF_HIT_OUT();
             }
         }
 #else
@@ -1249,14 +1301,14 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
             for (int k = 0; k < RG_WF_STEPS; ++k) {
                 trav_step<COUNT>(T, RG_SC, stk, vc);
                 if (!T.active) {
-                    wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
-                    wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;
+                    RG_WF_HIT_OUT();
                     break;
                 }
             }
         }
 #endif
     }
+#undef RG_WF_HIT_OUT
 #undef RG_SC
     unsigned long long c[3] = {vc.nodes, vc.tris, vc.overflow};
     for (int k = 0; k < 3; ++k) {
@@ -1266,6 +1318,46 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
             atomicAdd(P.counters + 4 + k, v);
             atomicAdd(P.counters + 12 + k, v);
         }
+    }
+    // Rays whose short stack overflowed: the last block to finish (every other block has appended its
+    // rays to the list and fenced) traces them again from the start with the deep stack and rewrites
+    // their hit records, then clears the list for the next launch.  No block waits for another.
+    // (thread 0's stack word carries the verdict: every stack is idle once the block is here; no
+    // shared memory is added, which would cost the kernel L1 at 7 blocks per SM)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        stk.over() = atomicAdd(wf.counts + 4, 1u) == gridDim.x - 1 ? 1u : 0u;
+    }
+    __syncthreads();
+    const uint32_t lastBlock = *reinterpret_cast<volatile uint32_t*>(&stk_mem[DEPTH - 1][0]);
+    if (!lastBlock) return;
+    __threadfence();
+    const uint32_t nOver = __ldcg(wf.counts + 3);
+    for (uint32_t i = threadIdx.x; i < nOver; i += blockDim.x) {
+        const uint32_t s = __ldcg(wf.overflow + i);
+        float4 o, d;
+        const DevScene* sc = &P.scene;
+        if (first) {  // work item s's camera ray, as the first round computed it
+            uint32_t path;
+            Payload p0;
+            RayReq r0;
+            frame_work_item(P, s, path, p0, r0);
+            o = make_float4(r0.o.x, r0.o.y, r0.o.z, r0.tmin);
+            d = make_float4(r0.d.x, r0.d.y, r0.d.z, r0.tmax);
+        } else {
+            o = __ldcg(&wf.qO[q][s]);
+            d = __ldcg(&wf.qD[q][s]);
+            if (BATCH) sc = &P.jobs[P.slotJob[__ldcg(&wf.qPath[q][s])]].scene;
+        }
+        Hit h;
+        retrace_deep(sc, o, d, &h, P.counters);
+        wf.hitTUV[s] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+        wf.hitInst[s] = h.hit ? h.inst : 0xFFFFFFFFu;
+    }
+    if (threadIdx.x == 0) {
+        wf.counts[3] = 0;
+        wf.counts[4] = 0;
     }
 }
 
@@ -1392,12 +1484,13 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : RG_SHADE_MIN_BLOCKS) k_wf_sha
 // the rest of one path, traced and shaded back to back
 template <bool GLOSSY, class STACK>
 __device__ __forceinline__ void finish_path(const DevScene& sc, const V3 L, const int maxRec, RayReq& ray, Payload& p, Frame* frames,
-                                            int& fsp, const STACK& stk, VisitCounts& vc, RayCounts& cnt) {
+                                            int& fsp, const STACK& stk, VisitCounts& vc, RayCounts& cnt, unsigned long long* counters) {
     Frame cur;
     for (;;) {
         Hit h;
         h.hit = false;
-        if (!ray.masked) h = closest_hit<false>(sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, stk, vc);
+        if (!ray.masked)
+            h = closest_hit<false>(sc, ray.o.x, ray.o.y, ray.o.z, ray.d.x, ray.d.y, ray.d.z, ray.tmin, ray.tmax, stk, vc, counters);
         if (!shade_step<GLOSSY>(sc, L, maxRec, h, p, ray, frames, fsp, cur, cnt)) break;
     }
 }
@@ -1406,7 +1499,7 @@ __device__ __forceinline__ void finish_path(const DevScene& sc, const V3 L, cons
 // each thread traces and shades its path's remaining sequence back to back -- instead of one
 // (trace, shade) launch pair per remaining round.  BATCH: only after the last work item was taken.
 template <bool BATCH, bool GLOSSY = false>
-__global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, int q) {
+__global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const __grid_constant__ TraceParams P, int q) {
     RG_DECLARE_STACK(stk);
     const WavefrontBuffers& wf = P.wf;
     const V3 L0 = v3(P.ubo.lightDir[0], P.ubo.lightDir[1], P.ubo.lightDir[2]);
@@ -1433,9 +1526,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_wf_tail(const TraceParams P, 
         if constexpr (BATCH) {
             const JobDesc& J = P.jobs[P.slotJob[path]];
             finish_path<GLOSSY>(J.scene, v3(J.ubo.lightDir[0], J.ubo.lightDir[1], J.ubo.lightDir[2]), J.ubo.maxRecursions, ray, p, frames, fsp,
-                        stk, vc, cnt);
+                        stk, vc, cnt, P.counters);
         } else {
-            finish_path<GLOSSY>(P.scene, L0, maxRec0, ray, p, frames, fsp, stk, vc, cnt);
+            finish_path<GLOSSY>(P.scene, L0, maxRec0, ray, p, frames, fsp, stk, vc, cnt, P.counters);
         }
         store_sample(P.samples + 3 * (size_t)(BATCH ? P.slotSample[path] : path), p);
     }
@@ -1548,14 +1641,20 @@ __global__ void __launch_bounds__(256) k_sort_scatter(const TraceParams P, int q
     }
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_trace_rays(const DevScene sc, const float* __restrict__ rays, uint32_t n,
-                                                               float* __restrict__ tuv, uint32_t* __restrict__ ids) {
-    RG_DECLARE_STACK(stk);
+template <int DEPTH>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_rays(const __grid_constant__ DevScene sc, const float* __restrict__ rays,
+                                                               uint32_t n, float* __restrict__ tuv, uint32_t* __restrict__ ids,
+                                                               unsigned long long* counters) {
+    RG_DECLARE_SMEM_STACK(stk, kTraceThreads, DEPTH);
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const float* r = rays + 8 * (size_t)k;
     VisitCounts vc = {0, 0, 0};
-    Hit h = closest_hit<false>(sc, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], stk, vc);
+    Hit h = closest_hit<false>(sc, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], stk, vc, counters);
+    if (vc.overflow) {  // rays re-traced deep, counted like the frame's
+        atomicAdd(counters + 6, vc.overflow);
+        atomicAdd(counters + 14, vc.overflow);
+    }
     if (h.hit) {
         tuv[3 * k] = h.t; tuv[3 * k + 1] = h.u; tuv[3 * k + 2] = h.v;
         ids[2 * k] = h.inst; ids[2 * k + 1] = h.prim;
@@ -1563,6 +1662,33 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(const DevScene sc,
         tuv[3 * k] = tuv[3 * k + 1] = tuv[3 * k + 2] = 0.0f;
         ids[2 * k] = ids[2 * k + 1] = 0xFFFFFFFFu;
     }
+}
+
+// rays (origin + tmin, direction + tmax: two float4 each) into queue 0 for one traversal round
+__global__ void k_rays_to_queue(const float4* __restrict__ rays, uint32_t n, const WavefrontBuffers wf) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        wf.counts[0] = n;
+        wf.counts[2] = 0;  // the trace kernel's fetch counter
+    }
+    if (i >= n) return;
+    wf.qO[0][i] = rays[2 * (size_t)i];
+    wf.qD[0][i] = rays[2 * (size_t)i + 1];
+}
+
+// hit records of that round in rg_trace_rays' layout: t, u, v and (instance, primitive), zeros and
+// 0xFFFFFFFF for a miss
+__global__ void k_queue_hits(uint32_t n, const WavefrontBuffers wf, float* __restrict__ tuv, uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 h = wf.hitTUV[i];
+    const uint32_t inst = wf.hitInst[i];
+    const bool hit = inst != 0xFFFFFFFFu;
+    tuv[3 * (size_t)i] = hit ? h.x : 0.0f;
+    tuv[3 * (size_t)i + 1] = hit ? h.y : 0.0f;
+    tuv[3 * (size_t)i + 2] = hit ? h.z : 0.0f;
+    ids[2 * (size_t)i] = inst;
+    ids[2 * (size_t)i + 1] = hit ? __float_as_uint(h.w) : 0xFFFFFFFFu;
 }
 
 }  // namespace
@@ -1638,6 +1764,21 @@ static TraceKernel trace_kernel(bool batch, bool count, int threads, int depth) 
 
 bool tune_supported(const TraceTune& t) {
     return trace_kernel(true, false, t.threads, t.depth) != nullptr && t.sortKey >= RG_SORT_NONE && t.sortKey <= RG_SORT_MORTON;
+}
+
+cudaError_t launch_trace_queue(const TraceParams& p, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const TraceKernel trace = trace_kernel(false, p.countVisits ? 1 : 0, kTraceThreads, kTraversalStack);
+    const int g = grid_of((const void*)trace, kTraceThreads);
+    if (!g) return cudaErrorUnknown;
+    TraceParams q = p;
+    q.firstRound = 0;
+    q.perm = nullptr;
+    k_rays_to_queue<<<(n + 255) / 256, 256, 0, s>>>(reinterpret_cast<const float4*>(rays), n, q.wf);
+    trace<<<g, kTraceThreads, 0, s>>>(q, 0);
+    k_queue_hits<<<(n + 255) / 256, 256, 0, s>>>(n, q.wf, tuv, ids);
+    count_launch(3);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_trace_wavefront(const TraceParams& p, cudaStream_t s, uint32_t* hostCount, int* iterations,
@@ -1844,9 +1985,17 @@ cudaError_t launch_resolve_job(const float4* samples, const JobDesc& j, uint2* b
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s) {
+cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids,
+                              unsigned long long* counters, int depth, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_trace_rays<<<(n + 127) / 128, 128, 0, s>>>(sc, rays, n, tuv, ids);
+    const uint32_t g = (n + kTraceThreads - 1) / kTraceThreads;
+    switch (depth) {
+        case 16: k_trace_rays<16><<<g, kTraceThreads, 0, s>>>(sc, rays, n, tuv, ids, counters); break;
+        case 24: k_trace_rays<24><<<g, kTraceThreads, 0, s>>>(sc, rays, n, tuv, ids, counters); break;
+        case 32: k_trace_rays<32><<<g, kTraceThreads, 0, s>>>(sc, rays, n, tuv, ids, counters); break;
+        case 48: k_trace_rays<48><<<g, kTraceThreads, 0, s>>>(sc, rays, n, tuv, ids, counters); break;
+        default: return cudaErrorInvalidValue;
+    }
     count_launch();
     return cudaGetLastError();
 }

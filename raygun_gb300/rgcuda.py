@@ -40,7 +40,7 @@ EXPORTS = [
     "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory", "rg_filter_create", "rg_filter_destroy",
     "rg_filter_last_error", "rg_filter_get_params", "rg_filter_set_params", "rg_filter_get_grads", "rg_filter_forward",
     "rg_filter_train_step", "rg_filter_input", "rg_filter_target", "rg_set_filter", "rg_set_glossy",
-    "rg_bvh_records", "rg_download_async",
+    "rg_bvh_records", "rg_download_async", "rg_trace_rays_device",
 ]
 FILTER_PARAMS = 78243
 # layer shapes of the learned filter: (out, in) real channel counts
@@ -75,7 +75,7 @@ class Timings(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("primary", "shadow", "secondary", "masked", "nodes", "tris",
-                                               "stack_overflows", "iterations")]
+                                               "stack_overflows", "iterations", "deep_overflows")]
 
 
 class BatchTune(ctypes.Structure):
@@ -125,6 +125,7 @@ def load(path: str = LIB_PATH):
         "rg_bvh_records": ([P, U32, P, U32, ctypes.POINTER(U32)], I32),
         "rg_download_async": ([P, P], I32),
         "rg_trace_rays": ([P, P, U32, P, P], I32),
+        "rg_trace_rays_device": ([P, P, U32, P, P], I32),
         "rg_post_only": ([P, P, P, P, P, I32], I32),
         "rg_lbvh_build_host": ([P, P, U32, P, P, P, P, P], I32),
         "rg_update_vertices_device": ([P, U32, P, U32], I32),
@@ -418,6 +419,11 @@ class Context:
         ids = np.zeros((n, 2), np.uint32)
         self._ck(self.L.rg_trace_rays(self.h, _p(rays), n, _p(tuv), _p(ids)))
         return tuv, ids
+
+    def trace_rays_device(self, d_rays: int, n: int, d_tuv: int, d_ids: int):
+        """rg_trace_rays_device: device pointers (n x 8 floats in, n x 3 floats and n x 2 uint32 out),
+        asynchronous on the context's stream."""
+        self._ck(self.L.rg_trace_rays_device(self.h, ctypes.c_void_p(d_rays), n, ctypes.c_void_p(d_tuv), ctypes.c_void_p(d_ids)))
 
     def post_only(self, ubo, base, normal, rough, fxaa=True):
         u = np.ascontiguousarray(ubo, dtype=scenes.UBO)

@@ -31,7 +31,7 @@ def test_layouts():
     assert S.UBO.fields["numSamples"][1] == 140 and S.UBO.fields["maxRecursions"][1] == 156
     assert S.UBO.fields["fadeColor"][1] == 176
     assert S.MATERIAL.fields["effectId"][1] == 40 and S.MATERIAL.fields["emission"][1] == 48
-    assert ctypes.sizeof(__import__("raygun_gb300.rgcuda", fromlist=["Stats"]).Stats) == 64
+    assert ctypes.sizeof(__import__("raygun_gb300.rgcuda", fromlist=["Stats"]).Stats) == 72
 
 
 def test_no_device_is_an_error_not_a_fallback(rg):

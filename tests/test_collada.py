@@ -23,7 +23,7 @@ from raygun_gb300 import scenes as S
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "raygun_gb300")
 FIX = os.path.join(ROOT, "tests", "fixtures")
-REFERENCE = os.environ.get("RAYGUN_REFERENCE", "/root/reference")
+from oracle.ref import REFERENCE  # noqa: E402  (where the reference tree is, if anywhere)
 
 
 @pytest.fixture(scope="module")

@@ -46,3 +46,21 @@ def test_single_rank_needs_no_group():
     import bench
     v, ms = bench.replica_throughput(1e7, 20.0, 1)
     assert v == pytest.approx(500.0) and ms == 20.0
+
+
+def test_bench_launches_n_replicas():
+    """`bench.py --gpus 2` starts two ranks itself (no torchrun), they join one gloo group, and rank 0
+    alone prints the aggregate: n_gpus = 2, rays summed over ranks / the slowest rank's time."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--workload", "dist-check"],
+                       capture_output=True, text=True, timeout=180, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    assert lines[0]["n_gpus"] == 2
+    assert lines[0]["value"] == pytest.approx(3.0e6 / 0.011 / 1e6)
+    assert lines[0]["ms_per_step"] == pytest.approx(11.0)

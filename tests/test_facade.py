@@ -77,6 +77,32 @@ def test_camera_matrices(demo, tmp_path):
     assert u["numSamples"] == 2 and u["maxRecursions"] == 4 and np.allclose(u["clearColor"], 0.2)
 
 
+def test_camera_matches_glm():
+    """The facade's Camera (viewInverse = T * R * S of its transform, projInverse = the inverse of
+    glm's depth-[0,1] perspective with the Y flip, lookAt / axis rotations as quaternions) against the
+    reference's own glm on 40 seeded cases (tests/golden/camera_glm.npz, made by
+    tests/golden/make_camera_golden.py from the glm the reference vendors).  The facade inverts in
+    double and rounds once, glm in float, so the bar is 1e-6 of each matrix's largest entry (measured:
+    2e-7); the rotation quaternions agree to 5e-7 (up to sign, q and -q being one rotation)."""
+    from raygun_gb300 import build
+    build.build()
+    exe = os.path.join(PKG, "_build", "camera_dump")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-o", exe,
+                    os.path.join(ROOT, "tests", "cpp", "camera_dump.cpp"), "-L", PKG, "-lrgfacade", "-lrgcuda",
+                    f"-Wl,-rpath,{PKG}"], check=True)
+    g = np.load(os.path.join(ROOT, "tests", "golden", "camera_glm.npz"))
+    r = subprocess.run([exe], input=g["cases"].astype(np.float32).tobytes(), capture_output=True, check=True)
+    out = np.frombuffer(r.stdout, np.float32).reshape(len(g["cases"]), 36)
+    for name, got, want in (("viewInverse", out[:, :16], g["view_inverse"]), ("projInverse", out[:, 16:32], g["proj_inverse"])):
+        scale = np.abs(want).max(1, keepdims=True)
+        err = np.abs(got - want) / scale
+        assert err.max() <= 1e-6, (name, float(err.max()), int(err.max(1).argmax()))
+    q, qw = out[:, 32:], g["rotation"]
+    sign = np.where((q * qw).sum(1, keepdims=True) < 0, -1.0, 1.0)
+    assert np.abs(q * sign - qw).max() <= 5e-7
+
+
 @pytest.mark.gpu
 def test_facade_frames_match_oracle(demo, tmp_path, orc):
     from test_gpu_parity import assert_image_close

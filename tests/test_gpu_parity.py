@@ -238,6 +238,80 @@ def test_errors_are_status_codes(rg):
         ctx.render(u)
 
 
+def test_malformed_scene_rejected_on_host(rg, orc):
+    """Index, vertex and material references that leave the uploaded buffers are rejected on the host
+    with RG_ERR_INVALID_ARG before any kernel reads through them (the reference relied on Vulkan's
+    robustBufferAccess instead, vulkan_context.cpp:256-257).  Indices are local to their mesh, so the
+    checks are made per range: vertexOffset + index, and materialBufferOffset + vertex.matIndex."""
+    sc = S.spheres_scene(n_spheres=2, width=16, height=16, slices=8, stacks=4)
+    ctx = rg.Context()
+    ctx.upload_geometry(sc.vertices, sc.indices, sc.materials)
+    ctx.set_resolution(16, 16)
+    nv, nt, nm = len(sc.vertices), len(sc.indices) // 3, len(sc.materials)
+    maxi = int(sc.indices.max())
+    for voff, ioff, n in ((nv - maxi, 0, nt),  # vertexOffset + index reaches nv
+                          (0, 3, nt),  # one triangle past the index buffer
+                          (1 << 31, 0, 1)):
+        with pytest.raises(rg.RgError) as e:
+            ctx.build_blas(voff, ioff, n)
+        assert e.value.code == -1, (voff, ioff, n)
+    b = ctx.build_blas(nv - maxi - 1, 0, nt)  # the last vertex is still inside
+    b = ctx.build_blas(0, 0, nt)
+    good = S.identity_instance(b)
+    good["vertexBufferOffset"], good["indexBufferOffset"] = 0, 0
+    ctx.build_tlas(good)
+    maxm = int(sc.vertices["matIndex"].max())
+    for field, value in (("indexBufferOffset", 3), ("vertexBufferOffset", nv - maxi),
+                         ("materialBufferOffset", nm - maxm)):
+        inst = np.concatenate([good, good])
+        inst[1][field] = value
+        with pytest.raises(rg.RgError) as e:
+            ctx.build_tlas(inst)
+        assert e.value.code == -1 and "instance 1" in str(e.value), field
+    # instances that are never traversed (unknown BLAS, mask 0) are not checked
+    skip = np.concatenate([good, good, good])
+    skip[1]["blas"], skip[1]["indexBufferOffset"] = 99, 10 ** 6
+    skip[2]["mask"], skip[2]["materialBufferOffset"] = 0, 10 ** 6
+    ctx.build_tlas(skip)
+    ctx.build_tlas(good)
+    # a vertex update that points a referenced vertex past the materials is refused, and nothing changes
+    v = sc.vertices[:1].copy()
+    v["matIndex"] = nm
+    with pytest.raises(rg.RgError) as e:
+        ctx.update_vertices(0, v)
+    assert e.value.code == -1
+    ctx.render(sc.ubo)
+    img = ctx.download()
+    o = orc.OracleScene(sc)
+    assert_image_close(img, orc.post(sc.ubo, *o.render()[:3]), "after refused updates")
+    ctx.close()
+
+
+def test_device_instances_with_foreign_offsets_are_skipped(rg, orc):
+    """rg_build_tlas_device cannot check instances on the host: the TLAS build skips (never hits) an
+    instance whose vertex/index offsets are not its BLAS's own or whose material offset takes the
+    BLAS's materials past the buffer; the others trace as the oracle traces them."""
+    import torch
+    sc = S.spheres_scene(n_spheres=4, width=32, height=18, slices=8, stacks=4)
+    ctx = rg.Context()
+    ctx.upload_geometry(sc.vertices, sc.indices, sc.materials)
+    b = ctx.build_blas(0, 0, len(sc.indices) // 3)
+    inst = np.concatenate([S.identity_instance(b)] * 3)
+    inst["transform"][1, :, 3] += (0, 50, 0)
+    inst["transform"][2, :, 3] += (0, 100, 0)
+    inst[1]["vertexBufferOffset"] = 1
+    inst[2]["materialBufferOffset"] = len(sc.materials)
+    d = torch.from_numpy(inst.view(np.uint8)).cuda()
+    ctx.build_tlas_device(d.data_ptr(), len(inst))
+    rays = np.zeros((3, 8), np.float32)
+    rays[:, 0:3] = [(0, 5, -20), (0, 55, -20), (0, 105, -20)]
+    rays[:, 3], rays[:, 7] = 1e-3, 1e4
+    rays[:, 4:7] = (0, -0.25, 1)
+    tuv, ids = ctx.trace_rays(rays)
+    assert ids[0, 0] == 0 and ids[1, 0] == 0xFFFFFFFF and ids[2, 0] == 0xFFFFFFFF
+    ctx.close()
+
+
 def test_hbm_budget_rejects(rg):
     ctx = rg.Context(hbm_budget_bytes=1 << 20)
     with pytest.raises(rg.RgError) as e:
@@ -346,23 +420,97 @@ def test_large_blas_is_lbvh(rg, orc):
     ctx.close()
 
 
-def test_deep_sah_blas_falls_back_to_lbvh(rg, orc):
-    """Small triangles at x = 17^k: every surface-area split takes one triangle off the far end, so
-    the binned-SAH tree would have 29 levels. Past 28 the build stops and the BLAS is the LBVH
-    instead, bit for bit the oracle's."""
-    n = 30
-    verts = np.zeros(3 * n, S.VERTEX)
-    for k in range(n):
-        x = np.float32(17.0 ** k)
-        verts["position"][3 * k:3 * k + 3] = [(x, 0, 0), (x, 0, 0.5), (x, 0.5, 0)]
-        verts["normal"][3 * k:3 * k + 3] = (1, 0, 0)
-    assert np.isfinite(verts["position"]).all()
-    idx = np.arange(3 * n, dtype=np.uint32)
-    sc = S.spheres_scene(n_spheres=1, width=8, height=8)
-    ctx = rg.Context()
-    ctx.upload_geometry(verts, idx, sc.materials)
-    b = ctx.build_blas(0, 0, n)
-    p = verts["position"].reshape(n, 3, 3)
+def deep_chain_scene(n_side=30, width=48, height=32):
+    """Small triangles in the planes x = +-17^k (k < n_side), facing along x.  Every binned-SAH split
+    peels the outermost triangles off, so the tree runs past the level from which the builder halves
+    ranges (34 levels for 30 a side).  The camera at the origin looks down the +x chain: its rays
+    descend the whole chain, pushing the far siblings of every record on the way."""
+    xs = 17.0 ** np.arange(n_side)
+    pos, nrm, idx = [], [], []
+    for sign in (1.0, -1.0):
+        for x in xs:
+            b = len(pos)
+            pos += [(sign * x, 0.0, 0.0), (sign * x, 0.0, 0.5), (sign * x, 0.5, 0.0)]
+            nrm += [(-sign, 0.0, 0.0)] * 3
+            idx.append((b, b + 1, b + 2))
+    mesh = S.Mesh(np.array(pos), np.array(nrm), np.array(idx, np.uint32))
+    assert np.isfinite(mesh.positions.astype(np.float32)).all()
+    mats = S.random_materials(S.Rng(5), 1)
+    ubo = S.make_ubo((0.0, 0.2, 0.2), (1.0, 0.2, 0.2), 60.0, width, height, (-0.4, -1.0, 0.3), 1, 3)
+    return S._finish("deep-chain", [(mesh, np.zeros(len(pos), np.uint32))], mats, S.identity_instance(), ubo, width, height)
+
+
+def test_deep_sah_blas_bounded_and_traced(rg, orc):
+    """A BLAS whose surface-area splits peel one triangle at a time: the GPU builds the oracle's tree,
+    whose ranges are halved from level 32 on (so no SAH tree is deeper than 32 + ceil(log2 n)
+    levels), and rays through it hit what the oracle's rays hit."""
+    sc = deep_chain_scene()
+    n = int(sc.meshes["triCount"][0])
+    p = sc.vertices["position"][sc.indices.astype(np.int64)].reshape(n, 3, 3)
     boxes = np.ascontiguousarray(np.concatenate([p.min(1), p.max(1)], 1), np.float32)
-    lbvh_equal(ctx.bvh(b), orc.lbvh(boxes))
-    ctx.close()
+    ref = orc.sah(boxes)
+    assert ref["levels"] == 34 and orc.sah(boxes, 1 << 20)["levels"] == 35  # the halving took over
+    rt = rg.Raytracer(sc).prepare()
+    assert orc.same_tree(rt.ctx.bvh(0), ref)
+    o = orc.OracleScene(sc)
+    rng = np.random.RandomState(3)
+    k = 4000
+    rays = np.zeros((k, 8), np.float32)
+    rays[:, 0] = 0.0
+    rays[:, 1:3] = rng.uniform(0.01, 0.2, (k, 2))
+    rays[:, 3], rays[:, 7] = 1e-3, 3e38
+    rays[:, 4] = np.where(np.arange(k) < k // 2, 1.0, -1.0)  # exactly along the chains: down the whole tree
+    rays = np.concatenate([rays, camera_rays(sc)])
+    to, io = o.trace(rays)
+    assert (io[:, 0] != 0xFFFFFFFF).mean() > 0.3
+    tg, ig = rt.ctx.trace_rays(rays)
+    assert np.array_equal(ig, io) and np.array_equal(tg, to)
+    assert rt.ctx.stats()["deep_overflows"] == 0
+    rt.ctx.close()
+
+
+def stacked_scene(n=1 << 14, width=48, height=32):
+    """n coincident triangles facing the camera.  Their centroids coincide, so the builder halves
+    every range: a balanced tree of 14 levels whose boxes every camera ray enters, all at the same
+    distance.  A ray then visits every record with all four children hit and pushes three of them at
+    each of its 7 record levels: 21 entries plus the marker, beyond a 16-word stack (15 entries),
+    within the default 48."""
+    tri = np.array([(4.0, -3.0, -3.0), (4.0, 9.0, -3.0), (4.0, -3.0, 9.0)])
+    pos = np.tile(tri, (n, 1))
+    nrm = np.tile((-1.0, 0.0, 0.0), (3 * n, 1))
+    idx = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+    mesh = S.Mesh(pos, nrm, idx)
+    mats = S.random_materials(S.Rng(6), 1)
+    ubo = S.make_ubo((0.0, 0.0, 0.0), (1.0, 0.0, 0.0), 60.0, width, height, (-0.4, -1.0, 0.3), 1, 2)
+    return S._finish("stacked", [(mesh, np.zeros(len(pos), np.uint32))], mats, S.identity_instance(), ubo, width, height)
+
+
+def test_stack_overflow_is_retraced(rg, orc):
+    """With a 16-word traversal stack (rg_set_batch_tune) every ray through the stacked scene
+    overflows it; each is traced again with the deep stack, so the hits still equal the oracle's,
+    and the batch frame (the wavefront trace kernel, re-traced by its last block) equals rg_render's
+    48-word frame, which does not overflow, bit for bit."""
+    sc = stacked_scene()
+    rt = rg.Raytracer(sc).prepare()
+    ref = rt.render()
+    assert rt.ctx.stats()["stack_overflows"] == 0
+    o = orc.OracleScene(sc)
+    rays = camera_rays(sc)
+    to, io = o.trace(rays)
+    assert (io[:, 0] != 0xFFFFFFFF).mean() > 0.9
+    for depth in (48, 16):
+        rt.ctx.set_batch_tune(128, depth, "none")
+        tg, ig = rt.ctx.trace_rays(rays)
+        st = rt.ctx.stats()
+        assert np.array_equal(ig, io) and np.array_equal(tg, to), depth
+        assert st["deep_overflows"] == 0
+        assert (st["stack_overflows"] > 0) == (depth == 16), (depth, st)
+    rt.ctx.close()
+    for flags in (0, rg.RG_FLAG_HOST_LOOP):
+        br = rg.BatchRenderer([sc], flags=flags)
+        br.ctx.set_batch_tune(128, 16, "none")
+        img = br.render()[0]
+        st = br.ctx.stats()
+        assert st["stack_overflows"] > 0 and st["deep_overflows"] == 0, st
+        assert np.array_equal(img, ref), flags
+        br.ctx.close()

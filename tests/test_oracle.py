@@ -239,7 +239,7 @@ def _check_bvh2(t, boxes):
 def test_oracle_sah_tree(orc):
     """The oracle's binned-SAH builder (the CUDA library's default BLAS/TLAS builder restated): valid
     BVH2s with exact node boxes, a lower surface-area cost than the LBVH over the same boxes, and the
-    level limit the library falls back to the LBVH at."""
+    depth bound of halving ranges from a fixed level on."""
     def half(b):
         d = np.maximum(b[..., 3:] - b[..., :3], 0).astype(np.float64)
         return d[..., 0] * d[..., 1] + d[..., 1] * d[..., 2] + d[..., 2] * d[..., 0]
@@ -252,11 +252,17 @@ def test_oracle_sah_tree(orc):
             lb = orc.lbvh(boxes)
             cost = lambda b: half(b["nodeboxes"]).sum() / half(b["nodeboxes"][0])
             assert cost(t) < cost(lb), (n, cost(t), cost(lb))
-    # small triangles at x = 17^k: every split takes one off the far end -> n - 1 levels
+    # small triangles at x = 17^k: every split takes one off the far end -> n - 1 levels, unless ranges
+    # are halved from a lower level on: then at most that level + ceil(log2(what remains)) levels
     n = 30
     x = (17.0 ** np.arange(n)).astype(np.float32)
     boxes = np.zeros((n, 6), np.float32)
     boxes[:, 0], boxes[:, 3] = x, x
     boxes[:, 4], boxes[:, 5] = 0.5, 0.5
     assert orc.sah(boxes)["levels"] == n - 1
-    assert orc.sah(boxes, 28) is None
+    for m in (0, 5, 10, 20):
+        t = orc.sah(boxes, m)
+        _check_bvh2(t, boxes)
+        assert t["levels"] <= m + int(np.ceil(np.log2(n - m))), (m, t["levels"])
+        assert orc.same_tree(t, orc.sah(boxes, m))
+    assert orc.sah(boxes, 28)["levels"] == 29  # one more split peels the last two apart
