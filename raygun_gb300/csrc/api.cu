@@ -228,6 +228,9 @@ bool range_ok(SceneState& st, uint32_t vOff, uint32_t iOff, uint32_t n, uint32_t
     return true;
 }
 
+// the roughness pass's status word (1 when one of its staged copies never landed)
+int* post_status(rg_ctx* c) { return reinterpret_cast<int*>(c->counters.as<unsigned long long>() + 16); }
+
 rg_status ensure(rg_ctx* c, DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.cap >= bytes) return RG_OK;
@@ -495,11 +498,12 @@ rg_status rg_create(rg_ctx** out, const rg_device_opts* opts) {
     }
     c->scenes.push_back(new SceneState());
     c->sc = c->scenes[0];
-    if (ensure(c, c->counters, 16 * sizeof(unsigned long long)) != RG_OK) {
+    // counters: 8 per frame, 8 cumulative, then one status word of the roughness pass
+    if (ensure(c, c->counters, 18 * sizeof(unsigned long long)) != RG_OK) {
         delete c;
         return RG_ERR_OUT_OF_MEMORY;
     }
-    cudaMemsetAsync(c->counters.p, 0, 128, c->stream);
+    cudaMemsetAsync(c->counters.p, 0, 18 * sizeof(unsigned long long), c->stream);
     if (cudaHostAlloc(&c->hostCount, 8 * sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -751,6 +755,7 @@ rg_status rg_set_resolution(rg_ctx* c, uint32_t w, uint32_t h) {
 static rg_status run_post(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     PostParams pp;
     std::memset(&pp, 0, sizeof(pp));
+    pp.status = post_status(c);
     pp.W = c->W;
     pp.H = c->H;
     pp.base = c->base.as<uint2>();
@@ -859,8 +864,10 @@ rg_status rg_download(rg_ctx* c, float* host) {
     if (!c->haveFrame) return fail(c, RG_ERR_NOT_READY, "no frame rendered");
     TRY(set_device(c));
     CK(cudaMemcpyAsync(host, c->fb.p, 16ull * c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&c->hostCount[7], post_status(c), 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     TRY(settle_graph(c));
+    if (c->hostCount[7]) return fail(c, RG_ERR_CUDA, "roughness pass: a staged tile copy did not complete");
     return RG_OK;
 }
 
@@ -928,9 +935,11 @@ rg_status rg_download_image(rg_ctx* c, int32_t which, float* host) {
 rg_status rg_synchronize(rg_ctx* c) {
     if (!c) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
+    CK(cudaMemcpyAsync(&c->hostCount[7], post_status(c), 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaStreamSynchronize(c->copyStream));
     TRY(settle_graph(c));
+    if (c->hostCount[7]) return fail(c, RG_ERR_CUDA, "roughness pass: a staged tile copy did not complete");
     return RG_OK;
 }
 
@@ -1180,6 +1189,7 @@ cudaError_t enqueue_batch_posts(rg_ctx* c, const JobDesc* jd, const rg_job* jobs
         if (e != cudaSuccess) return e;
         PostParams pp;
         std::memset(&pp, 0, sizeof(pp));
+        pp.status = post_status(c);
         pp.W = d.W;
         pp.H = d.H;
         pp.base = c->bBase.as<uint2>();

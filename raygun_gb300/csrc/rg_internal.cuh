@@ -318,6 +318,7 @@ struct PostParams {
     float fade[4];
     int showAlpha;
     int fxaa;
+    int* status;           // nullable: set to 1 when a staged copy of the roughness pass never landed
 };
 cudaError_t launch_rough_post(const PostParams& p, cudaStream_t s);
 cudaError_t launch_fxaa(const PostParams& p, cudaStream_t s);
