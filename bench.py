@@ -154,29 +154,6 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def measure_l2_peak(dev, reps=40, trials=5):
-    """Copy bandwidth of a working set that stays in L2: two 24 MiB buffers (48 MiB, well inside the
-    126 MB L2), b.copy_(a) repeated back to back and timed with CUDA events, best of `trials`;
-    read + write bytes.  The same kind of copy as the measured HBM peak, only L2-resident."""
-    import torch
-    n = (24 << 20) // 4
-    a = torch.rand(n, device=dev)
-    b = torch.empty_like(a)
-    for _ in range(10):
-        b.copy_(a)
-    best = 0.0
-    for _ in range(trials):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize(dev)
-        e0.record()
-        for _ in range(reps):
-            b.copy_(a)
-        e1.record()
-        torch.cuda.synchronize(dev)
-        best = max(best, 2 * a.numel() * 4 * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9)
-    return best
-
-
 def camera_rays_device(ubo, width, height, dev):
     """Pixel-centre camera rays of raygen.h:84-90 (origin, tmin 0.001, direction, tmax 1e4) for a
     width x height image, on the device: n x 8 float32."""
@@ -440,9 +417,11 @@ def run_ours(args):
 
     # the L2 bound: the scene's records, triangles and vertices (~64 MB) stay in the 126 MB L2 through
     # a frame, so the traversal's roofline is the L2's copy bandwidth, measured here
-    l2 = measure_l2_peak(dev)
-    roofline["l2"] = {"peak": l2, "frac": achieved / l2, "unit": "GB/s",
-                      "source": "measured in this run: torch copy of a 48 MiB L2-resident working set, best of 5 x 40 copies"}
+    l2_read, l2_copy = rgcuda.measure_l2(local, 64 << 20, 64)
+    roofline["l2"] = {"peak": l2_read, "frac": achieved / l2_read, "unit": "GB/s", "copy_gbs": l2_copy,
+                      "source": "measured in this run by rg_measure_l2: 64 MiB working set (inside the 126 MB L2) read "
+                                "with 16-byte loads, 64 passes per launch, best of 4 launches; the traversal's bytes are "
+                                "reads of L2-resident records and triangles"}
 
     # ---------------- incoherent secondary closest-hit throughput ----------------
     # the frame's first-bounce reflection / refraction rays (closesthit.rchit:215,232,244), traced by one

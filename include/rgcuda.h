@@ -370,6 +370,13 @@ rg_status rg_post_only(rg_ctx* ctx, const rg_ubo* ubo, const float* base, const 
 rg_status rg_lbvh_build_host(rg_ctx* ctx, const float* boxes, uint32_t n, uint32_t* morton, uint32_t* order,
                              uint32_t* left, uint32_t* right, float* nodeboxes);
 
+/* L2 bandwidth of device `device` (no counterpart in the reference; the measure the traversal's
+ * roofline is quoted against, since a frame's BVH records and triangles stay in L2): a working set
+ * of working_set_bytes (1 MiB .. 1 GiB; well under the L2 size to measure L2) read with 16-byte
+ * loads, and copied half into half, `reps` passes per launch, best of four launches timed with CUDA
+ * events, in GB/s (copy counts read + write bytes).  Allocates and frees its own buffers. */
+rg_status rg_measure_l2(int32_t device, uint64_t working_set_bytes, int32_t reps, double* read_gbs, double* copy_gbs);
+
 /* LBVH build that allocates nothing (no counterpart in the reference).  For callers that must not
  * allocate device memory after start-up -- an engine that owns a fixed memory arena, or a frame
  * loop that cannot afford the device synchronisation a cudaMalloc may cause.  Same results as

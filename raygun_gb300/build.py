@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librgcuda.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["api.cu", "lbvh.cu", "trace.cu", "post.cu", "noalloc.cu", "filter.cu", "filter_api.cu"]
+SOURCES = ["api.cu", "lbvh.cu", "trace.cu", "post.cu", "noalloc.cu", "filter.cu", "filter_api.cu", "measure.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE]
 

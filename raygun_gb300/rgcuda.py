@@ -40,7 +40,7 @@ EXPORTS = [
     "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory", "rg_filter_create", "rg_filter_destroy",
     "rg_filter_last_error", "rg_filter_get_params", "rg_filter_set_params", "rg_filter_get_grads", "rg_filter_forward",
     "rg_filter_train_step", "rg_filter_input", "rg_filter_target", "rg_set_filter", "rg_set_glossy",
-    "rg_bvh_records", "rg_download_async", "rg_trace_rays_device",
+    "rg_bvh_records", "rg_download_async", "rg_trace_rays_device", "rg_measure_l2",
 ]
 FILTER_PARAMS = 78243
 # layer shapes of the learned filter: (out, in) real channel counts
@@ -126,6 +126,7 @@ def load(path: str = LIB_PATH):
         "rg_download_async": ([P, P], I32),
         "rg_trace_rays": ([P, P, U32, P, P], I32),
         "rg_trace_rays_device": ([P, P, U32, P, P], I32),
+        "rg_measure_l2": ([I32, ctypes.c_uint64, I32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)], I32),
         "rg_post_only": ([P, P, P, P, P, I32], I32),
         "rg_lbvh_build_host": ([P, P, U32, P, P, P, P, P], I32),
         "rg_update_vertices_device": ([P, U32, P, U32], I32),
@@ -567,6 +568,16 @@ class Filter:
         self._ck(self.L.rg_filter_train_step(self.h, ctypes.c_void_p(d_in), ctypes.c_void_p(d_target), batch, height, width,
                                              ctypes.c_float(lr), ctypes.byref(loss)))
         return loss.value
+
+
+def measure_l2(device=0, working_set_bytes=64 << 20, reps=64):
+    """rg_measure_l2: (read GB/s, copy GB/s) of an L2-resident working set on `device`."""
+    L = load()
+    r, c = ctypes.c_double(), ctypes.c_double()
+    rc = L.rg_measure_l2(device, working_set_bytes, reps, ctypes.byref(r), ctypes.byref(c))
+    if rc != RG_OK:
+        raise RgError(rc, "rg_measure_l2 failed")
+    return r.value, c.value
 
 
 def filter_layers(params: np.ndarray):
