@@ -367,6 +367,221 @@ __device__ __forceinline__ float half_area3(const float* lo, const float* hi) {
     return dx * dy + dy * dz + dz * dx;
 }
 
+// One level with fewer tasks than warps: G warps share a task (G * count <= 32), each taking a
+// contiguous chunk of the task's range.  The same computation as one warp per task -- bounds and bin
+// contents are order-independent minima, maxima and counts, the split is chosen by the same rule, and
+// the partition stays stable (each warp writes its chunk at the offsets of the chunks before it) --
+// so the tree is the same; the top levels just run on the whole CTA instead of a few warps.
+__device__ __forceinline__ void sah_level_grouped(const float* __restrict__ boxes, uint32_t* __restrict__ order, uint32_t* __restrict__ tmp,
+                                                  uint32_t* __restrict__ left, uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
+                                                  const uint2* cur, uint2* nxt, uint32_t count, bool median, uint32_t baseCur,
+                                                  uint32_t baseNext, uint32_t& nNext, int (*bLo)[3][kSahBins][3],
+                                                  int (*bHi)[3][kSahBins][3], int (*bCnt)[3][kSahBins], float (*gPart)[12],
+                                                  float (*tClo)[3], float (*tScale)[3], int* tBest, uint32_t* wLeft) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t G = kSahWarps;
+    while (G * count > (uint32_t)kSahWarps) G >>= 1;
+    const uint32_t t = (uint32_t)warp / G, m = (uint32_t)warp % G;
+    const bool has = t < count;  // warp-uniform
+    const int lw = (int)(t * G);  // the task's leader warp (owner of its bins)
+    uint32_t b = 0, e = 0, cb = 0, ce = 0, node = 0;
+    if (has) {
+        const uint2 tk = cur[t];
+        b = tk.x;
+        e = tk.y;
+        node = baseCur + t;
+        const uint32_t chunk = (e - b + G - 1) / G;
+        cb = min(e, b + m * chunk);
+        ce = min(e, cb + chunk);
+    }
+    // bounds and centroid bounds of the chunk, then of the task
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = cb + lane; i < ce; i += 32) {
+        const float* bx = boxes + 6 * (size_t)order[i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], bx[a]);
+            hi[a] = fmaxf(hi[a], bx[3 + a]);
+            const float c = 0.5f * (bx[a] + bx[3 + a]);
+            clo[a] = fminf(clo[a], c);
+            chi[a] = fmaxf(chi[a], c);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], off));
+            clo[a] = fminf(clo[a], __shfl_xor_sync(0xFFFFFFFFu, clo[a], off));
+            chi[a] = fmaxf(chi[a], __shfl_xor_sync(0xFFFFFFFFu, chi[a], off));
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            gPart[warp][a] = lo[a];
+            gPart[warp][3 + a] = hi[a];
+            gPart[warp][6 + a] = clo[a];
+            gPart[warp][9 + a] = chi[a];
+        }
+    __syncthreads();
+    if (has && m == 0) {
+        if (lane == 0) {
+            for (uint32_t g = 1; g < G; ++g)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = fminf(lo[a], gPart[lw + g][a]);
+                    hi[a] = fmaxf(hi[a], gPart[lw + g][3 + a]);
+                    clo[a] = fminf(clo[a], gPart[lw + g][6 + a]);
+                    chi[a] = fmaxf(chi[a], gPart[lw + g][9 + a]);
+                }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                nodeBoxes[6 * (size_t)node + a] = lo[a];
+                nodeBoxes[6 * (size_t)node + 3 + a] = hi[a];
+                const float ext = chi[a] - clo[a];
+                tClo[t][a] = clo[a];
+                tScale[t][a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
+            }
+        }
+        if (!median)
+            for (int k = lane; k < 3 * kSahBins; k += 32) {
+                const int a = k / kSahBins, bn = k % kSahBins;
+                bCnt[lw][a][bn] = 0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    bLo[lw][a][bn][c] = ord_float(INFINITY);
+                    bHi[lw][a][bn][c] = ord_float(-INFINITY);
+                }
+            }
+    }
+    __syncthreads();
+    float tc[3] = {0.0f, 0.0f, 0.0f}, ts[3] = {0.0f, 0.0f, 0.0f};
+    if (has)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            tc[a] = tClo[t][a];
+            ts[a] = tScale[t][a];
+        }
+    auto bin_of = [&](const float* bx, int a) {
+        const float c = 0.5f * (bx[a] + bx[3 + a]);
+        return max(0, min((int)((c - tc[a]) * ts[a]), kSahBins - 1));
+    };
+    if (has && !median)  // every warp bins its chunk into the leader's bins
+        for (uint32_t i = cb + lane; i < ce; i += 32) {
+            const float* bx = boxes + 6 * (size_t)order[i];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (ts[a] <= 0.0f) continue;
+                const int k = bin_of(bx, a);
+                atomicAdd(&bCnt[lw][a][k], 1);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    atomicMin(&bLo[lw][a][k][c], ord_float(bx[c]));
+                    atomicMax(&bHi[lw][a][k][c], ord_float(bx[3 + c]));
+                }
+            }
+        }
+    __syncthreads();
+    if (has && m == 0) {  // the leader picks the split: cheapest surface-area cost, ties to the lowest candidate
+        float bestCost = INFINITY;
+        int bestCand = -1;
+        if (!median) {
+            for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
+                const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
+                if (ts[a] <= 0.0f) continue;
+                float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                int nl = 0, nr = 0;
+                for (int k = 0; k < kSahBins; ++k) {
+                    const int cnt = bCnt[lw][a][k];
+                    if (!cnt) continue;
+                    float* X0 = k < sp ? L0 : R0;
+                    float* X1 = k < sp ? L1 : R1;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        X0[c] = fminf(X0[c], unord_float(bLo[lw][a][k][c]));
+                        X1[c] = fmaxf(X1[c], unord_float(bHi[lw][a][k][c]));
+                    }
+                    if (k < sp) nl += cnt;
+                    else nr += cnt;
+                }
+                if (!nl || !nr) continue;
+                const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
+                if (cost < bestCost) {
+                    bestCost = cost;
+                    bestCand = cand;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
+                const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
+                if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
+                    bestCost = oc;
+                    bestCand = oi;
+                }
+            }
+        }
+        if (lane == 0) tBest[t] = bestCand;
+    }
+    __syncthreads();
+    const int best = has ? tBest[t] : -1;
+    const int sa = best >= 0 ? best / (kSahBins - 1) : 0, sp = best >= 0 ? best % (kSahBins - 1) + 1 : 0;
+    if (best >= 0) {  // left count of the chunk
+        uint32_t nl = 0;
+        for (uint32_t i0 = cb; i0 < ce; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool isL = i < ce && bin_of(boxes + 6 * (size_t)order[i], sa) < sp;
+            nl += __popc(__ballot_sync(0xFFFFFFFFu, isL));
+        }
+        if (lane == 0) wLeft[warp] = nl;
+    }
+    __syncthreads();
+    uint32_t nlTotal = 0;
+    if (best >= 0) {  // stable partition: this chunk's lefts after the lefts of the chunks before it, rights likewise
+        uint32_t before = 0;
+        for (uint32_t g = 0; g < G; ++g) {
+            const uint32_t c = wLeft[lw + g];
+            if (g < m) before += c;
+            nlTotal += c;
+        }
+        uint32_t lb = b + before, rb = b + nlTotal + ((cb - b) - before);
+        for (uint32_t i0 = cb; i0 < ce; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool valid = i < ce;
+            const uint32_t prim = valid ? order[i] : 0u;
+            const bool isL = valid && bin_of(boxes + 6 * (size_t)prim, sa) < sp;
+            const unsigned lm = __ballot_sync(0xFFFFFFFFu, isL), rm = __ballot_sync(0xFFFFFFFFu, valid && !isL);
+            const unsigned below = (1u << lane) - 1u;
+            if (isL) tmp[lb + __popc(lm & below)] = prim;
+            else if (valid) tmp[rb + __popc(rm & below)] = prim;
+            lb += __popc(lm);
+            rb += __popc(rm);
+        }
+    }
+    __syncthreads();
+    if (best >= 0)
+        for (uint32_t i = cb + lane; i < ce; i += 32) order[i] = tmp[i];
+    if (has && m == 0 && lane == 0) {  // children: single primitives become leaf refs, the rest next-level tasks
+        const uint32_t mid = best >= 0 ? b + nlTotal : b + (e - b) / 2;
+        const uint32_t rb0[2] = {b, mid}, re0[2] = {mid, e};
+        uint32_t ref[2];
+        for (int c = 0; c < 2; ++c) {
+            if (re0[c] - rb0[c] == 1) {
+                ref[c] = kLeaf | rb0[c];
+            } else {
+                const uint32_t idx = atomicAdd(&nNext, 1u);
+                nxt[idx] = make_uint2(rb0[c], re0[c]);
+                ref[c] = baseNext + idx;
+            }
+        }
+        left[node] = ref[0];
+        right[node] = ref[1];
+    }
+}
+
 __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __restrict__ boxes, uint32_t n, uint32_t* __restrict__ order,
                                                                  uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
                                                                  uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
@@ -375,6 +590,12 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
     __shared__ int bLo[kSahWarps][3][kSahBins][3], bHi[kSahWarps][3][kSahBins][3];
     __shared__ int bCnt[kSahWarps][3][kSahBins];
     __shared__ uint32_t nCur, nNext, baseCur, baseNext, levels;
+    // levels with fewer tasks than warps: per-warp partial bounds, per-task centroid frame and split,
+    // per-warp left counts
+    __shared__ float gPart[kSahWarps][12];
+    __shared__ float tClo[kSahWarps][3], tScale[kSahWarps][3];
+    __shared__ int tBest[kSahWarps];
+    __shared__ uint32_t wLeft[kSahWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) order[i] = i;
     if (threadIdx.x == 0) {
@@ -392,6 +613,10 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
         const uint32_t count = nCur;
         if (count == 0) break;
         const bool median = levels >= medianLevel;  // from here on ranges are halved: the depth stays bounded
+        if (count < (uint32_t)kSahWarps) {
+            sah_level_grouped(boxes, order, tmp, left, right, nodeBoxes, cur, nxt, count, median, baseCur, baseNext, nNext, bLo, bHi,
+                              bCnt, gPart, tClo, tScale, tBest, wLeft);
+        } else
         for (uint32_t t = warp; t < count; t += kSahWarps) {
             const uint2 tk = cur[t];
             const uint32_t b = tk.x, e = tk.y, node = baseCur + t;
