@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--serve-large", type=int, default=12, help="large terrain scenes in the catalog")
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
     ap.add_argument("--serve-graph", action="store_true", help="serve: CUDA-graph batches instead of the host loop")
+    ap.add_argument("--serve-filter-fraction", type=float, default=0.25,
+                    help="serve: share of requests that ask for the learned filter (committed trained weights)")
     ap.add_argument("--filter-scenes", type=int, default=200, help="filter: training scenes")
     ap.add_argument("--filter-crops", type=int, default=20000, help="filter: 128x128 training crops")
     ap.add_argument("--filter-epochs", type=int, default=30)
@@ -610,8 +612,9 @@ def run_batch(args):
 
 SERVE_WORKLOAD = "serving loop: Poisson arrivals at {rate:g} req/s, {n} requests; scenes of the batched-rendering " \
                  "distribution ({small} scenes) or, with probability 0.05, large terrain scenes ({large} scenes of " \
-                 "10-60 tessellated 1M-triangle heightfields) at 320x180..3840x2160 and 1-8 spp; LRU scene residency " \
-                 "under a {budget:g} GB HBM budget; waiting requests batched per step; every image read back"
+                 "10-60 tessellated 1M-triangle heightfields) at 320x180..3840x2160 and 1-8 spp; the learned roughness " \
+                 "filter on a share of the requests; LRU scene residency under a {budget:g} GB HBM budget; waiting " \
+                 "requests batched per step; every image read back"
 
 
 def run_serve(args):
@@ -633,13 +636,19 @@ def run_serve(args):
     budget = int(args.serve_budget_gb * 1e9)
     ctx = rgcuda.Context(device=local, hbm_budget_bytes=budget,
                          flags=0 if args.serve_graph else rgcuda.RG_FLAG_HOST_LOOP)
-    srv = V.RenderServer(ctx, catalog, budget)
+    flt = None
+    if args.serve_filter_fraction > 0:
+        from raygun_gb300 import filter_train
+        flt = rgcuda.Filter(ctx, seed=0)
+        filter_train.load_weights(flt)
+    srv = V.RenderServer(ctx, catalog, budget, learned_filter=flt)
     reqs = V.poisson_requests(args.serve_requests, args.serve_rate, 4, [(k, catalog[k]) for k in catalog if k[0] == "b"],
-                              [(k, catalog[k]) for k in large_keys])
+                              [(k, catalog[k]) for k in large_keys], filter_fraction=args.serve_filter_fraction)
     # a server that has been running: the working buffers of a large batch exist and the catalog is
     # resident as far as the budget allows (catalog order)
     warm = V.poisson_requests(96, args.serve_rate, 40, [(k, catalog[k]) for k in catalog if k[0] == "b"],
-                              [(k, catalog[k]) for k in large_keys], large_fraction=0.2)
+                              [(k, catalog[k]) for k in large_keys], large_fraction=0.2,
+                              filter_fraction=args.serve_filter_fraction)
     for r in warm:
         r.arrival = 0.0
     t0 = time.perf_counter()
@@ -672,6 +681,7 @@ def run_serve(args):
                    "catalog_instanced_tris": int(sum(sc.instanced_tri_count for sc in catalog.values())),
                    "catalog_unique_tris": int(sum(int(sc.meshes["triCount"].astype(np.int64).sum()) for sc in catalog.values())),
                    "batch_mode": "graph" if args.serve_graph else "host loop",
+                   "filter_fraction": args.serve_filter_fraction,
                    "l2": "inputs larger than L2", "parallelism": "single GPU"},
         "serving": {**summary, "batches": srv.batches, "mean_batch": float(np.mean(srv.batch_sizes)) if srv.batch_sizes else 0.0,
                     "evictions": srv.res.evictions - ev0, "uploads": srv.res.uploads - up0,

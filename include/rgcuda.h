@@ -247,11 +247,16 @@ rg_status rg_scene_destroy(rg_ctx* ctx, uint32_t scene);
 rg_status rg_scene_bytes(rg_ctx* ctx, uint32_t scene, uint64_t* out_bytes);
 
 /* One render of a batch: RenderSystem::render (render/render_system.cpp:88-162) of the scene in
- * slot `scene` at width x height with this UBO; fxaa as for rg_render. */
+ * slot `scene` at width x height with this UBO.  options: RG_JOB_FXAA as rg_render's fxaa;
+ * RG_JOB_FILTER: the learned roughness filter set with rg_set_filter stands in for the roughness
+ * passes of this job (an error when the context has none); a batch with such a job runs its round
+ * loop from the host (no graph capture). */
+#define RG_JOB_FXAA 1
+#define RG_JOB_FILTER 2
 typedef struct rg_job {
     uint32_t scene;
     uint32_t width, height;
-    int32_t fxaa;
+    int32_t options;
     rg_ubo ubo;
 } rg_job;
 
@@ -311,7 +316,8 @@ rg_status rg_filter_train_step(rg_filter* f, const void* d_input, const float* d
 rg_status rg_filter_input(rg_ctx* ctx, void* d_out);
 /* the rough RGB of the context's last frame, d_out [H][W][4] FP32 (training target of a glossy frame) */
 rg_status rg_filter_target(rg_ctx* ctx, float* d_out);
-/* frames of this context use the filter in place of the roughness passes (NULL: the plain passes) */
+/* frames of this context (rg_render) use the filter in place of the roughness passes (NULL: the plain
+ * passes); batch jobs use it when they ask for it (RG_JOB_FILTER) */
 rg_status rg_set_filter(rg_ctx* ctx, rg_filter* f);
 /* glossy reference shading (training targets; 0 = off, the default): at each sample's primary hit
  * the reflection and refraction directions are drawn around their mirror directions from a GGX lobe

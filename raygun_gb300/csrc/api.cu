@@ -1200,8 +1200,13 @@ cudaError_t enqueue_batch_posts(rg_ctx* c, const JobDesc* jd, const rg_job* jobs
         pp.framebuffer = c->batchFb.as<float4>() + c->batchOffset[j];
         for (int k = 0; k < 4; ++k) pp.fade[k] = d.ubo.fadeColor[k];
         pp.showAlpha = d.ubo.showAlpha ? 1 : 0;
-        pp.fxaa = jobs[j].fxaa ? 1 : 0;
-        if ((e = launch_rough_post(pp, c->stream)) != cudaSuccess) return e;
+        pp.fxaa = (jobs[j].options & RG_JOB_FXAA) ? 1 : 0;
+        if (jobs[j].options & RG_JOB_FILTER)  // the learned filter in place of the roughness passes
+            e = filter_frame(c->filter, pp.base, pp.normal, pp.rough, d.W, d.H, (float)d.S, pp.fade, pp.showAlpha, pp.finalImg,
+                             c->stream);
+        else
+            e = launch_rough_post(pp, c->stream);
+        if (e != cudaSuccess) return e;
         if ((e = launch_fxaa(pp, c->stream)) != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -1230,7 +1235,7 @@ std::vector<uint8_t> batch_graph_key(rg_ctx* c, const TraceParams& tp, const Sor
         key_put(k, jd[j].sampleBase);
         key_put(k, jd[j].ubo.fadeColor);
         key_put(k, jd[j].ubo.showAlpha);
-        key_put(k, jobs[j].fxaa);
+        key_put(k, jobs[j].options);
         key_put(k, c->batchOffset[j]);
     }
     return k;
@@ -1362,6 +1367,9 @@ rg_status rg_set_batch_slots(rg_ctx* c, uint32_t slots) {
 rg_status rg_render_batch(rg_ctx* c, const rg_job* jobs, uint32_t n) {
     if (!c) return RG_ERR_INVALID_ARG;
     if (!jobs || n == 0) return fail(c, RG_ERR_INVALID_ARG, "empty batch");
+    for (uint32_t j = 0; j < n; ++j)
+        if ((jobs[j].options & RG_JOB_FILTER) && !c->filter)
+            return fail(c, RG_ERR_INVALID_ARG, "job " + std::to_string(j) + ": learned filter asked for, none set (rg_set_filter)");
     std::vector<JobDesc> jd(n);
     uint64_t work = 0, samples = 0, pixels = 0, maxPixels = 0;
     for (uint32_t j = 0; j < n; ++j) {
@@ -1445,7 +1453,9 @@ rg_status rg_render_batch(rg_ctx* c, const rg_job* jobs, uint32_t n) {
     FrameEvents* fe;
     TRY(cur_events(c, &fe));
     CK(cudaEventRecord(fe->ev[EV_RT0], c->stream));
-    const bool hostLoop = (c->flags & (RG_FLAG_HOST_LOOP | RG_FLAG_KERNEL_TIMING | RG_FLAG_COUNT_VISITS)) != 0;
+    bool filtered = false;
+    for (uint32_t j = 0; j < n; ++j) filtered |= (jobs[j].options & RG_JOB_FILTER) != 0;
+    const bool hostLoop = filtered || (c->flags & (RG_FLAG_HOST_LOOP | RG_FLAG_KERNEL_TIMING | RG_FLAG_COUNT_VISITS)) != 0;
     if (hostLoop) {
         if (c->flags & RG_FLAG_KERNEL_TIMING)
             CK(launch_trace_batch(tp, c->tune, sort, c->stream, c->hostCount, &c->lastIterations, next_kernel_events, fe));

@@ -51,7 +51,8 @@ WIDE_RECORD = np.dtype([("planes", "<f4", (6, 4)), ("ref", "<u4", 4)])
 assert WIDE_RECORD.itemsize == 112
 
 # rg_job (include/rgcuda.h): one render of a batch
-JOB = np.dtype([("scene", "<u4"), ("width", "<u4"), ("height", "<u4"), ("fxaa", "<i4"), ("ubo", scenes.UBO)])
+JOB = np.dtype([("scene", "<u4"), ("width", "<u4"), ("height", "<u4"), ("options", "<i4"), ("ubo", scenes.UBO)])
+RG_JOB_FXAA, RG_JOB_FILTER = 1, 2
 SORT_KEYS = {"none": 0, "octant": 1, "morton": 2}
 AUTOTUNE_CONFIGS = 36
 
@@ -511,7 +512,7 @@ class BatchRenderer:
         for k, sc in enumerate(self.scenes):
             j[k]["scene"] = self.slots[k]
             j[k]["width"], j[k]["height"] = sc.width, sc.height
-            j[k]["fxaa"] = 1 if fxaa else 0
+            j[k]["options"] = RG_JOB_FXAA if fxaa else 0
             j[k]["ubo"] = sc.ubo[0] if sc.ubo.shape else sc.ubo
         return j
 

@@ -27,6 +27,8 @@ PATH_SLOT_BYTES = 64 + 8 + 144 * 10 + 2 * 36 + 20
 # per sample (payload sums), per output pixel (batch framebuffer), per pixel of the largest job
 # (G-buffers, post scratch)
 SAMPLE_BYTES, PIXEL_BYTES, SCRATCH_PIXEL_BYTES = 48, 16, 40
+# per pixel of the largest filtered job: the learned filter's input, activations and prediction
+FILTER_PIXEL_BYTES = 512
 # device bytes per triangle of a resident BLAS (BVH2 nodes, 4-wide records, build scratch kept for
 # refits, leaf-ordered triangles) and per instance of a TLAS; geometry buffers are counted as uploaded
 BLAS_TRI_BYTES, TLAS_INSTANCE_BYTES = 236, 496
@@ -42,6 +44,7 @@ class Request:
     depth: int
     arrival: float  # seconds from the start of the run
     fxaa: bool = True
+    filter: bool = False  # the learned roughness filter in place of the roughness passes
 
     @property
     def samples(self) -> int:
@@ -77,8 +80,9 @@ def working_bytes(reqs, path_slots: int) -> int:
         return 0
     samples = sum(r.samples for r in reqs)
     pixels = sum(r.width * r.height for r in reqs)
+    filtered = [r.width * r.height for r in reqs if r.filter]
     return (min(samples, path_slots) * PATH_SLOT_BYTES + samples * SAMPLE_BYTES + pixels * PIXEL_BYTES
-            + max(r.width * r.height for r in reqs) * SCRATCH_PIXEL_BYTES)
+            + max(r.width * r.height for r in reqs) * SCRATCH_PIXEL_BYTES + max(filtered, default=0) * FILTER_PIXEL_BYTES)
 
 
 class Residency:
@@ -132,8 +136,13 @@ class Residency:
 
 class RenderServer:
     def __init__(self, ctx, catalog: dict, budget_bytes: int, max_batch: int = 64, path_slots: int = 1 << 23,
-                 read_back: bool = True, keep_images: bool = False):
+                 read_back: bool = True, keep_images: bool = False, learned_filter=None):
+        """learned_filter: an rgcuda.Filter that requests asking for it (Request.filter) use in place
+        of the roughness passes; without one such requests are turned away."""
         self.ctx = ctx
+        self.filter = learned_filter
+        if learned_filter is not None:
+            ctx.set_filter(learned_filter)
         self.catalog = catalog
         self.budget = budget_bytes
         self.max_batch = max_batch
@@ -162,6 +171,9 @@ class RenderServer:
         for req in list(self.queue):
             if len(batch) >= self.max_batch:
                 break
+            if req.filter and self.filter is None:
+                rejected.append(req)
+                continue
             trial_keys = keys if req.scene in keys else keys + [req.scene]
             trial = batch + [req]
             need = sum(self.res.footprint(k) for k in trial_keys) + max(held, working_bytes(trial, self.path_slots))
@@ -179,7 +191,8 @@ class RenderServer:
         """Render the next batch; returns the results of every request it finished or rejected."""
         batch, rejected, keys = self.admit()
         now = clock()
-        out = [Result(r.id, r.arrival, now, now, False, "does not fit the HBM budget") for r in rejected]
+        out = [Result(r.id, r.arrival, now, now, False, "learned filter asked for, none loaded" if r.filter and self.filter is None
+                      else "does not fit the HBM budget") for r in rejected]
         for r in rejected:
             self.queue.remove(r)
         if not batch:
@@ -187,7 +200,7 @@ class RenderServer:
         for r in batch:
             self.queue.remove(r)
         start = clock()
-        from .rgcuda import JOB, RgError
+        from .rgcuda import JOB, RG_JOB_FILTER, RG_JOB_FXAA, RgError
         room = self.budget - max(self._working_held(), working_bytes(batch, self.path_slots))
         while self.res.resident_bytes() + sum(self.res.footprint(k) for k in keys if k not in self.res.slots) > room:
             if not self.res.evict_lru(set(keys)):
@@ -199,7 +212,8 @@ class RenderServer:
                 for j, r in enumerate(batch):
                     sc = self.catalog[r.scene]
                     jobs[j]["scene"] = slots[r.scene]
-                    jobs[j]["width"], jobs[j]["height"], jobs[j]["fxaa"] = r.width, r.height, 1 if r.fxaa else 0
+                    jobs[j]["width"], jobs[j]["height"] = r.width, r.height
+                    jobs[j]["options"] = (RG_JOB_FXAA if r.fxaa else 0) | (RG_JOB_FILTER if r.filter else 0)
                     jobs[j]["ubo"] = scenes.reframe(sc, r.width, r.height, r.spp, r.depth)[0]
                 self.ctx.render_batch(jobs)
                 break
@@ -235,13 +249,16 @@ class RenderServer:
         return out
 
 
-def poisson_requests(n: int, rate: float, seed: int, pool_small, pool_large, large_fraction: float = 0.05):
+def poisson_requests(n: int, rate: float, seed: int, pool_small, pool_large, large_fraction: float = 0.05,
+                     filter_fraction: float = 0.0):
     """n requests with exponential inter-arrival gaps (mean 1/rate).  A request takes a scene of the
     batched-rendering distribution (its own size, samples and depth) or, with probability
     ``large_fraction``, a large terrain scene at a size drawn from 320x180 ... 3840x2160 with 1-8
     samples and depth 1-6.  Draw order per request: gap, large?, scene index, then for a large scene
-    size index, samples, depth."""
+    size index, samples, depth.  With probability ``filter_fraction`` a request asks for the learned
+    filter (drawn from a stream of its own, seed ^ 0x5EED, so the other draws do not move)."""
     rng = scenes.Rng(seed)
+    frng = scenes.Rng(seed ^ 0x5EED)
     t, out = 0.0, []
     for i in range(n):
         t += -math.log(1.0 - rng.uniform(1)[0]) / rate
@@ -255,7 +272,8 @@ def poisson_requests(n: int, rate: float, seed: int, pool_small, pool_large, lar
         else:
             w, h = sc.width, sc.height
             spp, depth = int(sc.ubo["numSamples"][0]), int(sc.ubo["maxRecursions"][0])
-        out.append(Request(i, key, w, h, spp, depth, t))
+        filt = bool(frng.uniform(1)[0] < filter_fraction)
+        out.append(Request(i, key, w, h, spp, depth, t, filter=filt))
     return out
 
 

@@ -3,7 +3,9 @@
 CPU: LRU residency and HBM-budget admission against a fake context that records what the server
 asks of the C ABI; the Poisson arrival generator; the latency summary.
 GPU: a small open-loop run whose budget forces evictions; every image it returns equals the single
-render of the same scene, size and UBO.
+render of the same scene, size and UBO.  Served images against the oracle's render of the same
+request; requests that ask for the learned filter against rg_render with that filter, in a batch
+that mixes them with plain requests.
 """
 import math
 
@@ -170,3 +172,55 @@ def test_gpu_open_loop_with_evictions(rg):
         assert np.array_equal(byid[q.id].image, ref), q
     s = V.summarize(results, wall, srv.rays)
     assert s["completed"] == len(reqs) and s["mrays_per_s"] > 0
+
+
+def test_filter_requests_need_a_filter():
+    cat = small_catalog()
+    srv = V.RenderServer(FakeContext(), cat, 1 << 40, path_slots=1 << 10)
+    srv.submit(V.Request(0, "s0", 32, 18, 1, 1, 0.0, filter=True))
+    res = srv.step(lambda: 0.0)
+    assert [(r.id, r.ok) for r in res] == [(0, False)] and "filter" in res[0].error
+    reqs = V.poisson_requests(2000, 400.0, 4, list(cat.items()), [], filter_fraction=0.25)
+    assert 0.2 < np.mean([r.filter for r in reqs]) < 0.3
+    plain = V.poisson_requests(2000, 400.0, 4, list(cat.items()), [])
+    assert [(r.scene, r.arrival) for r in reqs] == [(r.scene, r.arrival) for r in plain]
+
+
+@pytest.mark.gpu
+def test_gpu_served_images_vs_oracle_and_learned_filter(rg, orc):
+    from raygun_gb300 import filter_train
+    from test_gpu_parity import assert_image_close
+    cat = small_catalog()
+    ctx = rg.Context()
+    flt = rg.Filter(ctx, seed=0)
+    filter_train.load_weights(flt)  # the committed trained weights
+    srv = V.RenderServer(ctx, cat, 1 << 40, max_batch=8, path_slots=1 << 16, keep_images=True, learned_filter=flt)
+    reqs = [V.Request(0, "s0", 48, 27, 2, 3, 0.0), V.Request(1, "s1", 40, 24, 1, 4, 0.0),
+            V.Request(2, "s0", 48, 27, 2, 3, 0.0, filter=True), V.Request(3, "s2", 64, 36, 2, 2, 0.0, filter=True)]
+    results, _ = V.run_open_loop(srv, reqs)
+    assert all(r.ok for r in results), [r.error for r in results]
+    assert len({r.batch for r in results}) == 1  # one batch mixes plain and filtered jobs
+    byid = {r.id: r for r in results}
+    for q in reqs:
+        sc = cat[q.scene]
+        framed = S.Scene(sc.name, sc.vertices, sc.indices, sc.materials, sc.meshes, sc.instances,
+                         S.reframe(sc, q.width, q.height, q.spp, q.depth), q.width, q.height)
+        if not q.filter:  # the oracle's frame of the request
+            o = orc.OracleScene(framed)
+            b, n, r, _ = o.render()
+            assert_image_close(byid[q.id].image, orc.post(framed.ubo, b, n, r), f"served request {q.id}")
+        else:  # rg_render with the same filter weights, in a context of its own
+            rt = rg.Raytracer(framed).prepare()
+            f2 = rg.Filter(rt.ctx, seed=0)
+            filter_train.load_weights(f2)
+            rt.ctx.set_filter(f2)
+            ref = rt.render()
+            plain = None
+            rt.ctx.set_filter(None)
+            plain = rt.render()
+            f2.close()
+            rt.ctx.close()
+            assert np.array_equal(byid[q.id].image, ref), q
+            assert not np.array_equal(ref, plain)  # the filter changed the frame
+    flt.close()
+    ctx.close()
