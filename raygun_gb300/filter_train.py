@@ -213,14 +213,18 @@ def load_weights(flt, path: str = WEIGHTS):
 
 def main():
     """python -m raygun_gb300.filter_train --infer W H [--repeat N]: the committed weights on a
-    seeded random 16-channel input of W x H (inference only; used for kernel profiles)."""
+    seeded random 16-channel input of W x H (inference only); --train W H [--repeat N]: N Adam steps
+    on a seeded random input and target of W x H (forward, backward, weight gradients).  Both are the
+    workloads of the filter kernels' profiles."""
     import argparse
     import torch
     ap = argparse.ArgumentParser()
-    ap.add_argument("--infer", nargs=2, type=int, required=True, metavar=("W", "H"))
+    mode = ap.add_mutually_exclusive_group(required=True)
+    mode.add_argument("--infer", nargs=2, type=int, metavar=("W", "H"))
+    mode.add_argument("--train", nargs=2, type=int, metavar=("W", "H"))
     ap.add_argument("--repeat", type=int, default=3)
     args = ap.parse_args()
-    W, H = args.infer
+    W, H = args.infer or args.train
     ctx = rg.Context()
     flt = rg.Filter(ctx)
     load_weights(flt)
@@ -230,9 +234,19 @@ def main():
     d_in = x.to(torch.bfloat16).cuda()
     d_out = torch.empty(H, W, 4, device="cuda")
     torch.cuda.synchronize()
+    if args.infer:
+        for _ in range(args.repeat):
+            flt.forward(d_in.data_ptr(), 1, H, W, d_out.data_ptr())
+        print(f"filter forward {W}x{H} x{args.repeat}: mean prediction {float(d_out[..., :3].mean()):.5f}")
+        return
+    tgt = torch.zeros(H, W, 4)
+    tgt[..., :3] = torch.rand(H, W, 3, generator=g)
+    d_tgt = tgt.cuda()
+    torch.cuda.synchronize()
+    loss = 0.0
     for _ in range(args.repeat):
-        flt.forward(d_in.data_ptr(), 1, H, W, d_out.data_ptr())
-    print(f"filter forward {W}x{H} x{args.repeat}: mean prediction {float(d_out[..., :3].mean()):.5f}")
+        loss = flt.train_step(d_in.data_ptr(), d_tgt.data_ptr(), 1, H, W, 1e-3)
+    print(f"filter train {W}x{H} x{args.repeat}: last loss {loss:.5f}")
 
 
 if __name__ == "__main__":

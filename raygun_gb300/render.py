@@ -1,6 +1,8 @@
 """Headless render of the game-frame scene (1024 instances of the eight procedural meshes).
 
-    python -m raygun_gb300.render [--res WxH] [--spp S] [--frames N] [--out frame.npy]
+    python -m raygun_gb300.render [--res WxH] [--spp S] [--frames N] [--blas-lbvh] [--tlas-lbvh]
+                                  [--learned-filter] [--out frame.npy]
+    python -m raygun_gb300.render --lbvh-boxes N [--frames K]   (K LBVH builds over N seeded boxes)
 
 Builds the scene, renders N frames through the library (RenderSystem::render without a window),
 prints the rays of the last frame and optionally saves its RGBA32F framebuffer.  No timing: this is
@@ -22,11 +24,33 @@ def main(argv=None):
     ap.add_argument("--res", default="1920x1080")
     ap.add_argument("--spp", type=int, default=4)
     ap.add_argument("--frames", type=int, default=1)
+    ap.add_argument("--blas-lbvh", action="store_true", help="BLASes as LBVHs (Morton sort, Karras) instead of binned SAH")
+    ap.add_argument("--tlas-lbvh", action="store_true", help="the TLAS as an LBVH instead of binned SAH")
+    ap.add_argument("--learned-filter", action="store_true", help="the learned roughness filter (committed weights)")
+    ap.add_argument("--lbvh-boxes", type=int, default=0, help="instead of frames: LBVH builds over this many seeded boxes")
     ap.add_argument("--out", default=None)
     args = ap.parse_args(argv)
+    if args.lbvh_boxes:
+        rng = np.random.RandomState(7)
+        c = rng.uniform(-100, 100, (args.lbvh_boxes, 3)).astype(np.float32)
+        e = rng.uniform(0.01, 0.5, (args.lbvh_boxes, 3)).astype(np.float32)
+        boxes = np.concatenate([c - e, c + e], 1)
+        ctx = rgcuda.Context()
+        for _ in range(args.frames):
+            out = ctx.lbvh_build_host(boxes)
+        print(json.dumps({"lbvh_boxes": args.lbvh_boxes, "builds": args.frames, "root_box": out["nodeboxes"][0].tolist()}))
+        ctx.close()
+        return
     w, h = (int(x) for x in args.res.split("x"))
     sc = S.instanced_scene(width=w, height=h, num_samples=args.spp)
-    rt = rgcuda.Raytracer(sc).prepare()
+    flags = (rgcuda.RG_FLAG_BLAS_LBVH if args.blas_lbvh else 0) | (rgcuda.RG_FLAG_TLAS_LBVH if args.tlas_lbvh else 0)
+    rt = rgcuda.Raytracer(sc, flags=flags).prepare()
+    flt = None
+    if args.learned_filter:
+        from . import filter_train
+        flt = rgcuda.Filter(rt.ctx, seed=0)
+        filter_train.load_weights(flt)
+        rt.ctx.set_filter(flt)
     fb = None
     for _ in range(args.frames):
         fb = rt.render()
@@ -36,6 +60,9 @@ def main(argv=None):
                       "finite": bool(np.isfinite(fb).all())}))
     if args.out:
         np.save(args.out, fb)
+    if flt is not None:
+        rt.ctx.set_filter(None)
+        flt.close()
     rt.ctx.close()
 
 
