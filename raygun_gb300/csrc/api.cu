@@ -100,7 +100,7 @@ struct rg_ctx {
     SceneState* sc = nullptr;
     uint32_t scId = 0;
     // shared sort scratch
-    DevBuf keysA, keysB, valsA, valsB, blockHist, bounds;
+    DevBuf keysA, keysB, valsA, valsB, sortState, bounds;
     // images (raytracer.cpp:173-195)
     uint32_t W = 0, H = 0;
     DevBuf base, normal, rough, finalImg, fxaaOut, fb, dbgT, dbgA, dbgB;
@@ -284,7 +284,7 @@ rg_status ensure_sort_scratch(rg_ctx* c, uint32_t n) {
     TRY(ensure(c, c->keysB, 4ull * n));
     TRY(ensure(c, c->valsA, 4ull * n));
     TRY(ensure(c, c->valsB, 4ull * n));
-    TRY(ensure(c, c->blockHist, 4ull * 256 * sort_block_count(n)));
+    TRY(ensure(c, c->sortState, 4ull * sort_state_words(n)));
     TRY(ensure(c, c->bounds, 64));
     return RG_OK;
 }
@@ -317,7 +317,7 @@ LbvhBuffers buffers(rg_ctx* c, const BvhSet& s) {
     b.keysB = c->keysB.as<uint32_t>();
     b.valsA = c->valsA.as<uint32_t>();
     b.valsB = c->valsB.as<uint32_t>();
-    b.blockHist = c->blockHist.as<uint32_t>();
+    b.sortState = c->sortState.as<uint32_t>();
     b.parents = s.parents.as<uint32_t>();
     b.flags = s.flags.as<uint32_t>();
     b.bounds = c->bounds.as<uint32_t>();
@@ -530,7 +530,7 @@ rg_status rg_destroy(rg_ctx* c) {
         if (c->copied[k]) cudaEventDestroy(c->copied[k]);
     }
     if (c->copyStream) cudaStreamDestroy(c->copyStream);
-    DevBuf* bufs[] = {&c->keysA, &c->keysB, &c->valsA, &c->valsB, &c->blockHist, &c->bounds, &c->base, &c->normal, &c->rough,
+    DevBuf* bufs[] = {&c->keysA, &c->keysB, &c->valsA, &c->valsB, &c->sortState, &c->bounds, &c->base, &c->normal, &c->rough,
                       &c->finalImg, &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC,
                       &c->tmpD, &c->samples, &c->workCounter, &c->wfPayload, &c->wfMeta, &c->wfFrames, &c->wfQO0, &c->wfQO1,
                       &c->wfQD0, &c->wfQD1, &c->wfQP0, &c->wfQP1, &c->wfHitTUV, &c->wfHitInst, &c->wfCounts, &c->wfOverflow, &c->jobTable,

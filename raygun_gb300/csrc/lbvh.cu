@@ -5,10 +5,12 @@
 //   1. primitive boxes (triangles: min/max of the three vertices)
 //   2. centroid bounds (order-preserving uint atomics: exact, order independent)
 //   3. 30-bit Morton codes of the centroids, normalised to the cube of the largest centroid extent
-//   4. stable LSD radix sort of (code, primitive) in four 8-bit passes
+//   4. stable LSD radix sort of (code, primitive) in four 8-bit passes, one onesweep kernel each
 //   5. Karras 2012 hierarchy (n-1 internal nodes; equal codes split on the index)
 //   6. bottom-up boxes: one thread per leaf climbs; the second arrival at a node writes its box
 // Refit (topology kept, boxes recomputed) reruns step 6 only.
+#include <cstdlib>
+
 #include "rg_internal.cuh"
 
 namespace rg {
@@ -18,7 +20,8 @@ namespace {
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortRounds = 8;
-constexpr int kSortTile = kSortWarps * kSortRounds * 32;  // 2048 keys per block
+static_assert(kSortWarps * kSortRounds * 32 == kSortTileKeys, "one onesweep tile per block");
+constexpr uint32_t kMortonMaxBlocks = 608;  // grid-stride: bounds the global histogram atomics
 
 __global__ void k_tri_boxes(const rg_vertex* __restrict__ v, const uint32_t* __restrict__ idx, uint32_t vOff, uint32_t iOff,
                             uint32_t n, float* __restrict__ boxes) {
@@ -64,7 +67,8 @@ __global__ void k_bounds_init(uint32_t* bounds) {
     else if (threadIdx.x < 6) bounds[threadIdx.x] = 0u;
 }
 
-__global__ void k_centroid_bounds(const float* __restrict__ boxes, uint32_t n, uint32_t* bounds) {
+__global__ void __launch_bounds__(256) k_centroid_bounds(const float* __restrict__ boxes, uint32_t n, uint32_t* bounds) {
+    __shared__ float red[6][8];
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         float c[3];
@@ -79,19 +83,36 @@ __global__ void k_centroid_bounds(const float* __restrict__ boxes, uint32_t n, u
             mn[a] = fminf(mn[a], __shfl_xor_sync(0xFFFFFFFFu, mn[a], off));
             mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xFFFFFFFFu, mx[a], off));
         }
-    if ((threadIdx.x & 31) == 0)
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
         for (int a = 0; a < 3; ++a) {
-            if (mn[a] <= mx[a]) {
-                atomicMin(&bounds[a], f2ord(mn[a]));
-                atomicMax(&bounds[3 + a], f2ord(mx[a]));
-            }
+            red[a][w] = mn[a];
+            red[3 + a][w] = mx[a];
         }
+    __syncthreads();
+    // one atomic per block and bound (same-address atomics from every warp serialise in L2)
+    if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        float lo = red[a][0], hi = red[3 + a][0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            lo = fminf(lo, red[a][k]);
+            hi = fmaxf(hi, red[3 + a][k]);
+        }
+        if (lo <= hi) {  // the block saw a centroid
+            atomicMin(&bounds[a], f2ord(lo));
+            atomicMax(&bounds[3 + a], f2ord(hi));
+        }
+    }
 }
 
-__global__ void k_morton(const float* __restrict__ boxes, uint32_t n, const uint32_t* __restrict__ bounds,
-                         uint32_t* __restrict__ morton, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
+// codes, the sort's input (keys, and values = primitive ids in BOTH value buffers, so that every
+// word of either is a valid primitive id whatever a pass writes), and the four digit histograms of
+// the sort (grid-stride; one shared-memory histogram per block, flushed with global atomics)
+__global__ void __launch_bounds__(256) k_morton(const float* __restrict__ boxes, uint32_t n, const uint32_t* __restrict__ bounds,
+                                                uint32_t* __restrict__ morton, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                uint32_t* __restrict__ valsAlt, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[4 * 256];
+    for (int i = threadIdx.x; i < 4 * 256; i += 256) h[i] = 0;
     // every axis is scaled by the LARGEST centroid extent (a cube), so a thin axis spends few of its
     // 10 bits and the hierarchy splits mostly along the long axes
     float lo[3], inv[3];
@@ -101,63 +122,81 @@ __global__ void k_morton(const float* __restrict__ boxes, uint32_t n, const uint
         emax = fmaxf(emax, __fsub_rn(ord2f(bounds[3 + a]), lo[a]));
     }
     for (int a = 0; a < 3; ++a) inv[a] = emax > 0.0f ? __fdiv_rn(1.0f, emax) : 0.0f;
-    float c[3];
-    centroid(boxes + 6 * (size_t)p, c);
-    uint32_t x = quant10(c[0], lo[0], inv[0]), y = quant10(c[1], lo[1], inv[1]), z = quant10(c[2], lo[2], inv[2]);
-    uint32_t m = (expand10(x) << 2) | (expand10(y) << 1) | expand10(z);
-    morton[p] = m;
-    keys[p] = m;
-    vals[p] = p;
-}
-
-// ---- stable LSD radix sort ----------------------------------------------------------------------
-__global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
-                                                             uint32_t* __restrict__ blockHist, uint32_t nb) {
-    __shared__ uint32_t cnt[256];
-    cnt[threadIdx.x] = 0;
     __syncthreads();
-    uint32_t base = blockIdx.x * kSortTile;
-    for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
-        uint32_t k = base + i;
-        if (k < n) atomicAdd(&cnt[(keys[k] >> shift) & 0xFFu], 1u);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        float c[3];
+        centroid(boxes + 6 * (size_t)p, c);
+        uint32_t x = quant10(c[0], lo[0], inv[0]), y = quant10(c[1], lo[1], inv[1]), z = quant10(c[2], lo[2], inv[2]);
+        uint32_t m = (expand10(x) << 2) | (expand10(y) << 1) | expand10(z);
+        morton[p] = m;
+        keys[p] = m;
+        vals[p] = p;
+        valsAlt[p] = p;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) atomicAdd(&h[256 * d + ((m >> (8 * d)) & 0xFFu)], 1u);
     }
     __syncthreads();
-    blockHist[(size_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
+    for (int i = threadIdx.x; i < 4 * 256; i += 256)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
-// exclusive scan of blockHist in digit-major order (one block)
-__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* data, uint32_t total) {
-    __shared__ uint32_t part[1024];
-    uint32_t chunk = (total + 1023) / 1024;
-    uint32_t b = threadIdx.x * chunk, e = min(total, b + chunk);
-    uint32_t s = 0;
-    for (uint32_t i = b; i < e; ++i) s += data[i];
-    part[threadIdx.x] = s;
+// ---- onesweep LSD radix sort (Adinets & Merrill 2022) --------------------------------------------
+// k_morton counts the four 8-bit digit histograms of the codes as it writes them.  Each of the four
+// passes is then ONE kernel: a block takes the next tile in launch order (an atomic counter, so every
+// earlier tile belongs to a block that is already running), ranks its kSortTileKeys keys by digit
+// (stable: warp chunks in key order, lanes in key order), publishes its per-digit counts, and finds
+// how many keys of each digit precede it by decoupled look-back over the earlier tiles' published
+// words, then scatters.  A status word is flag (bits 31:30) | count (bits 29:0): 0 = not yet
+// published, kStatAgg = this tile's own count, kStatIncl = count over this and all earlier tiles.
+// A look-back that finds a predecessor unpublished polls it a bounded number of times and then
+// counts that tile's keys of the digit directly from the input, so no wait is unbounded and the
+// result does not depend on the bound.
+constexpr uint32_t kStatAgg = 1u << 30;
+constexpr uint32_t kStatIncl = 2u << 30;
+constexpr uint32_t kStatCount = (1u << 30) - 1u;
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// exclusive prefix sum over the block's 256 threads (one value each); `warpSums` holds 8 words
+__device__ __forceinline__ uint32_t block_exclusive_256(uint32_t v, uint32_t* warpSums) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warpSums[w] = x;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[threadIdx.x] - s;
-    for (uint32_t i = b; i < e; ++i) {
-        uint32_t x = data[i];
-        data[i] = run;
-        run += x;
-    }
+    uint32_t before = 0;
+    for (int k = 0; k < w; ++k) before += warpSums[k];
+    return before + x - v;
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
-                                                                uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
-                                                                uint32_t n, int shift, const uint32_t* __restrict__ offsets,
-                                                                uint32_t nb) {
+__global__ void __launch_bounds__(kSortThreads) k_sort_onesweep(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+                                                                 uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
+                                                                 uint32_t n, int pass, uint32_t* __restrict__ state, uint32_t nTiles,
+                                                                 uint32_t spinLimit) {
     __shared__ uint32_t wc[kSortWarps][256];
+    __shared__ uint32_t digitBase[256];
+    __shared__ uint32_t warpSums[kSortWarps];
+    __shared__ uint32_t tileShared;
+    const int shift = 8 * pass;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) tileShared = atomicAdd(state + kSortTileCounters + pass, 1u);
     for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&wc[0][0])[i] = 0;
     __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tile = tileShared;
     const uint32_t ltmask = (1u << lane) - 1u;
-    uint32_t base = blockIdx.x * kSortTile + w * (kSortRounds * 32);
+    const uint32_t base = tile * kSortTileKeys + w * (kSortRounds * 32);
     uint32_t key[kSortRounds], val[kSortRounds], pos[kSortRounds];
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
@@ -174,23 +213,49 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
         __syncwarp();
     }
     __syncthreads();
-    {  // per digit: prefix over warps, seeded with this block's global offset
-        uint32_t d = threadIdx.x;
-        uint32_t run = offsets[(size_t)d * nb + blockIdx.x];
-        for (int ww = 0; ww < kSortWarps; ++ww) {
-            uint32_t t = wc[ww][d];
-            wc[ww][d] = run;
-            run += t;
-        }
+    // thread d: this tile's count of digit d, and each warp's exclusive offset within the tile
+    const uint32_t d = threadIdx.x;
+    uint32_t cnt = 0;
+    for (int ww = 0; ww < kSortWarps; ++ww) {
+        uint32_t t = wc[ww][d];
+        wc[ww][d] = cnt;
+        cnt += t;
     }
+    uint32_t* status = state + kSortStatusOffset + (size_t)pass * nTiles * 256;
+    st_relaxed(status + (size_t)tile * 256 + d, (tile == 0 ? kStatIncl : kStatAgg) | cnt);
+    // keys of smaller digits in the whole input (this pass's histogram)
+    const uint32_t globalBefore = block_exclusive_256(state[256 * pass + d], warpSums);
+    // keys of digit d in earlier tiles
+    uint32_t earlier = 0;
+    for (int64_t t = (int64_t)tile - 1; t >= 0; --t) {
+        const uint32_t* sp = status + (size_t)t * 256 + d;
+        uint32_t v = ld_relaxed(sp);
+        for (uint32_t spins = 0; (v >> 30) == 0 && spins < spinLimit; ++spins) {
+            __nanosleep(100);
+            v = ld_relaxed(sp);
+        }
+        if ((v >> 30) == 0) {  // still unpublished: count tile t's keys of digit d from the input
+            uint32_t c = 0;
+            const uint32_t b0 = (uint32_t)t * kSortTileKeys, b1 = min(n, b0 + kSortTileKeys);
+            for (uint32_t i = b0; i < b1; ++i) c += ((keysIn[i] >> shift) & 0xFFu) == d;
+            v = kStatAgg | c;
+        }
+        earlier += v & kStatCount;
+        if ((v >> 30) == 2) break;
+    }
+    if (tile > 0) st_relaxed(status + (size_t)tile * 256 + d, kStatIncl | (earlier + cnt));
+    digitBase[d] = globalBefore + earlier;
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r) {
         uint32_t i = base + r * 32 + lane;
         if (i < n) {
-            uint32_t dst = wc[w][(key[r] >> shift) & 0xFFu] + pos[r];
-            keysOut[dst] = key[r];
-            valsOut[dst] = val[r];
+            uint32_t dg = (key[r] >> shift) & 0xFFu;
+            uint32_t dst = digitBase[dg] + wc[w][dg] + pos[r];
+            if (dst < n) {  // always true: the counts are exact
+                keysOut[dst] = key[r];
+                valsOut[dst] = val[r];
+            }
         }
     }
 }
@@ -264,28 +329,45 @@ __device__ inline void load_box_cg(const float* p, float* b) {
     for (int a = 0; a < 6; ++a) b[a] = __ldcg(p + a);
 }
 
+__device__ __forceinline__ uint32_t arrive(uint32_t* flag) {  // release my box, acquire my sibling's
+    uint32_t old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(flag) : "memory");
+    return old;
+}
+
+// one thread per leaf climbs towards the root; at each node the first arrival stops and the second,
+// which then sees the first's box (release / acquire on the node's arrival counter), writes the
+// union.  The climbing thread keeps the box of the child it comes from in registers and loads only
+// its sibling's.
 __global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t* __restrict__ order, uint32_t n,
                             const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
                             const uint32_t* __restrict__ parents, uint32_t* flags, float* nodeBoxes) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     uint32_t node = parents[(n - 1) + k];
+    uint32_t from = kLeaf | k;
+    float cur[6];
+    load_box_cg(primBoxes + 6 * (size_t)order[k], cur);
     while (node != 0xFFFFFFFFu) {
-        __threadfence();
-        uint32_t old = atomicAdd(&flags[node], 1u);
-        if (old == 0) return;
-        __threadfence();
-        uint32_t L = left[node], R = right[node];
-        float bl[6], br[6];
-        if (L & kLeaf) load_box_cg(primBoxes + 6 * (size_t)order[L & ~kLeaf], bl);
-        else load_box_cg(nodeBoxes + 6 * (size_t)L, bl);
-        if (R & kLeaf) load_box_cg(primBoxes + 6 * (size_t)order[R & ~kLeaf], br);
-        else load_box_cg(nodeBoxes + 6 * (size_t)R, br);
-        float* o = nodeBoxes + 6 * (size_t)node;
+        if (arrive(&flags[node]) == 0) return;
+        const uint32_t L = left[node], R = right[node];
+        const uint32_t other = L == from ? R : L;
+        float ob[6];
+        if (other & kLeaf) load_box_cg(primBoxes + 6 * (size_t)order[other & ~kLeaf], ob);
+        else load_box_cg(nodeBoxes + 6 * (size_t)other, ob);
+        const float* bl = L == from ? cur : ob;
+        const float* br = L == from ? ob : cur;
+        float nb[6];
         for (int a = 0; a < 3; ++a) {
-            __stcg(o + a, fminf(bl[a], br[a]));
-            __stcg(o + 3 + a, fmaxf(bl[3 + a], br[3 + a]));
+            nb[a] = fminf(bl[a], br[a]);
+            nb[3 + a] = fmaxf(bl[3 + a], br[3 + a]);
         }
+        float* o = nodeBoxes + 6 * (size_t)node;
+        for (int a = 0; a < 6; ++a) {
+            __stcg(o + a, nb[a]);
+            cur[a] = nb[a];
+        }
+        from = node;
         node = parents[node];
     }
 }
@@ -854,8 +936,6 @@ inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-size_t sort_block_count(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
-
 cudaError_t tri_boxes(const rg_vertex* v, const uint32_t* idx, uint32_t vOff, uint32_t iOff, uint32_t n, float* boxes, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_tri_boxes<<<blocks(n, 256), 256, 0, s>>>(v, idx, vOff, iOff, n, boxes);
@@ -920,24 +1000,29 @@ cudaError_t wide_records(const LbvhBuffers& b, WideNode* out, cudaStream_t s) {
 cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s) {
     const uint32_t n = b.n;
     if (n == 0) return cudaSuccess;
+    if (n > kStatCount) return cudaErrorInvalidValue;  // the sort's status words count in 30 bits
+    const uint32_t nTiles = (uint32_t)sort_tiles(n);
+    cudaError_t e = cudaMemsetAsync(b.sortState, 0, 4 * sort_state_words(n), s);
+    if (e != cudaSuccess) return e;
     k_bounds_init<<<1, 32, 0, s>>>(b.bounds);
     uint32_t gb = min(blocks(n, 256), 1024u);
     k_centroid_bounds<<<gb, 256, 0, s>>>(b.primBoxes, n, b.bounds);
-    k_morton<<<blocks(n, 256), 256, 0, s>>>(b.primBoxes, n, b.bounds, b.morton, b.keysA, b.valsA);
+    k_morton<<<min(blocks(n, 256), kMortonMaxBlocks), 256, 0, s>>>(b.primBoxes, n, b.bounds, b.morton, b.keysA, b.valsA, b.valsB,
+                                                                   b.sortState);
     count_launch(3);
-    const uint32_t nb = (uint32_t)sort_block_count(n);
+    // polls of an unpublished predecessor tile before a look-back counts that tile itself
+    // (RG_SORT_SPIN_LIMIT overrides; 0 makes every such look-back count, which tests use)
+    uint32_t spinLimit = 1u << 16;
+    if (const char* env = getenv("RG_SORT_SPIN_LIMIT")) spinLimit = (uint32_t)strtoul(env, nullptr, 10);
     uint32_t *kin = b.keysA, *vin = b.valsA, *kout = b.keysB, *vout = b.valsB;
     for (int pass = 0; pass < 4; ++pass) {
-        int shift = 8 * pass;
-        k_sort_hist<<<nb, kSortThreads, 0, s>>>(kin, n, shift, b.blockHist, nb);
-        k_sort_scan<<<1, 1024, 0, s>>>(b.blockHist, 256u * nb);
-        k_sort_scatter<<<nb, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, b.blockHist, nb);
-        count_launch(3);
+        k_sort_onesweep<<<nTiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, pass, b.sortState, nTiles, spinLimit);
+        count_launch();
         uint32_t* t = kin; kin = kout; kout = t;
         t = vin; vin = vout; vout = t;
     }
     // after 4 passes the sorted data is back in keysA / valsA
-    cudaError_t e = cudaMemcpyAsync(b.order, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+    e = cudaMemcpyAsync(b.order, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
     if (n == 1) return cudaGetLastError();
     k_karras<<<blocks(n - 1, 256), 256, 0, s>>>(kin, n, b.left, b.right, b.parents);

@@ -29,11 +29,11 @@ constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign;
 
 // scratch layout for kMaxPrims primitives
 constexpr size_t kKeysBytes = align_up(4ull * kMaxPrims);
-constexpr size_t kHistBytes = align_up(4ull * 256 * ((kMaxPrims + 2047) / 2048));
+constexpr size_t kSortStateBytes = align_up(4ull * sort_state_words(kMaxPrims));
 constexpr size_t kParentsBytes = align_up(8ull * kMaxPrims);
 constexpr size_t kFlagsBytes = align_up(4ull * kMaxPrims);
 constexpr size_t kBoundsBytes = align_up(64);
-constexpr size_t kScratchBytes = 4 * kKeysBytes + kHistBytes + kParentsBytes + kFlagsBytes + kBoundsBytes;
+constexpr size_t kScratchBytes = 4 * kKeysBytes + kSortStateBytes + kParentsBytes + kFlagsBytes + kBoundsBytes;
 
 static __device__ __align__(256) unsigned char g_lbvh_scratch[kScratchBytes];
 
@@ -83,7 +83,7 @@ extern "C" rg_status rg_lbvh_build_device_noalloc(const float* d_boxes, uint32_t
     b.keysB = reinterpret_cast<uint32_t*>(p); p += kKeysBytes;
     b.valsA = reinterpret_cast<uint32_t*>(p); p += kKeysBytes;
     b.valsB = reinterpret_cast<uint32_t*>(p); p += kKeysBytes;
-    b.blockHist = reinterpret_cast<uint32_t*>(p); p += kHistBytes;
+    b.sortState = reinterpret_cast<uint32_t*>(p); p += kSortStateBytes;  // zeroed by the build
     b.parents = reinterpret_cast<uint32_t*>(p); p += kParentsBytes;
     b.flags = reinterpret_cast<uint32_t*>(p); p += kFlagsBytes;  // zeroed inside lbvh_build (refit step)
     b.bounds = reinterpret_cast<uint32_t*>(p);                    // reset by the build's first kernel

@@ -132,13 +132,20 @@ struct LbvhBuffers {  // scratch + outputs of one LBVH build, sized by the calle
     float* nodeBoxes;      // (n-1) x 6
     // scratch
     uint32_t* keysA; uint32_t* keysB; uint32_t* valsA; uint32_t* valsB;
-    uint32_t* blockHist;   // 256 * numBlocks(n)
+    uint32_t* sortState;   // sort_state_words(n): digit histograms, tile counters, look-back words
     uint32_t* parents;     // 2n (internal n-1 then leaves n)
     uint32_t* flags;       // n-1
     uint32_t* bounds;      // 6 (ordered uints)
 };
 
-size_t sort_block_count(uint32_t n);
+// onesweep radix sort of the Morton codes: keys per tile, and the layout of its state words (zeroed
+// by each build): 4 passes x 256 digit counts, 4 tile counters, then per pass one status word per
+// (tile, digit)
+constexpr uint32_t kSortTileKeys = 2048;
+constexpr uint32_t kSortTileCounters = 4 * 256;
+constexpr uint32_t kSortStatusOffset = kSortTileCounters + 32;
+constexpr size_t sort_tiles(size_t n) { return (n + kSortTileKeys - 1) / kSortTileKeys; }
+constexpr size_t sort_state_words(size_t n) { return kSortStatusOffset + 4 * 256 * sort_tiles(n); }
 cudaError_t lbvh_build(const LbvhBuffers& b, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s);  // topology kept, primBoxes changed
 cudaError_t wide_records(const LbvhBuffers& b, WideNode* out, cudaStream_t s);  // after build / refit
@@ -241,7 +248,7 @@ struct TraceTune {
     int threads = 128, depth = 48, sortKey = RG_SORT_NONE;
 };
 bool tune_supported(const TraceTune& t);
-// scratch of the ray sort (each of the first three: `slots` words; hist: sort_block_count(slots)*256)
+// scratch of the ray sort (each of the first three: `slots` words; hist: 8192 words)
 struct SortScratch {
     uint32_t *keysA, *keysB, *valsA, *valsB, *hist;
 };

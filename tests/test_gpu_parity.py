@@ -44,9 +44,18 @@ def lbvh_equal(g, o):
 
 
 @pytest.mark.parametrize("n,dup", [(1, False), (2, False), (3, False), (100, False), (2049, True), (70000, False),
-                                   (300000, True)])
+                                   (300000, True), (1 << 20, False)])
 def test_lbvh_build_bit_exact(rg, orc, n, dup):
     boxes = random_boxes(n, 7 + n, dup)
+    ctx = rg.Context()
+    lbvh_equal(ctx.lbvh_build_host(boxes), orc.lbvh(boxes))
+
+
+def test_lbvh_sort_lookback_counts_unpublished_tiles(rg, orc, monkeypatch):
+    """Onesweep passes in which every look-back that meets a tile not yet published counts that
+    tile's keys itself (RG_SORT_SPIN_LIMIT=0) sort exactly as the published words do."""
+    monkeypatch.setenv("RG_SORT_SPIN_LIMIT", "0")
+    boxes = random_boxes(300000, 99, True)
     ctx = rg.Context()
     lbvh_equal(ctx.lbvh_build_host(boxes), orc.lbvh(boxes))
 
