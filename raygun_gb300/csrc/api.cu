@@ -100,7 +100,7 @@ struct rg_ctx {
     SceneState* sc = nullptr;
     uint32_t scId = 0;
     // shared sort scratch
-    DevBuf keysA, keysB, valsA, valsB, sortState, bounds;
+    DevBuf keysA, keysB, valsA, valsB, sortState, bounds, sahQueue;
     // images (raytracer.cpp:173-195)
     uint32_t W = 0, H = 0;
     DevBuf base, normal, rough, finalImg, fxaaOut, fb, dbgT, dbgA, dbgB;
@@ -228,8 +228,12 @@ bool range_ok(SceneState& st, uint32_t vOff, uint32_t iOff, uint32_t n, uint32_t
     return true;
 }
 
-// the roughness pass's status word (1 when one of its staged copies never landed)
-int* post_status(rg_ctx* c) { return reinterpret_cast<int*>(c->counters.as<unsigned long long>() + 16); }
+// status word of the device-side waits: 1 when a staged tile copy of the roughness pass never
+// landed, 2 when a task wait of the SAH builder gave up
+int* wait_status(rg_ctx* c) { return reinterpret_cast<int*>(c->counters.as<unsigned long long>() + 16); }
+const char* wait_failure(uint32_t code) {
+    return code == 2 ? "BVH build: a task of the SAH builder was never published" : "roughness pass: a staged tile copy did not complete";
+}
 
 rg_status ensure(rg_ctx* c, DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 16;
@@ -285,6 +289,7 @@ rg_status ensure_sort_scratch(rg_ctx* c, uint32_t n) {
     TRY(ensure(c, c->valsA, 4ull * n));
     TRY(ensure(c, c->valsB, 4ull * n));
     TRY(ensure(c, c->sortState, 4ull * sort_state_words(n)));
+    TRY(ensure(c, c->sahQueue, sah_queue_bytes(std::min(n, kSahBlasMaxPrims))));
     TRY(ensure(c, c->bounds, 64));
     return RG_OK;
 }
@@ -321,6 +326,8 @@ LbvhBuffers buffers(rg_ctx* c, const BvhSet& s) {
     b.parents = s.parents.as<uint32_t>();
     b.flags = s.flags.as<uint32_t>();
     b.bounds = c->bounds.as<uint32_t>();
+    b.sahQueue = c->sahQueue.as<unsigned char>();
+    b.status = wait_status(c);
     return b;
 }
 
@@ -530,7 +537,7 @@ rg_status rg_destroy(rg_ctx* c) {
         if (c->copied[k]) cudaEventDestroy(c->copied[k]);
     }
     if (c->copyStream) cudaStreamDestroy(c->copyStream);
-    DevBuf* bufs[] = {&c->keysA, &c->keysB, &c->valsA, &c->valsB, &c->sortState, &c->bounds, &c->base, &c->normal, &c->rough,
+    DevBuf* bufs[] = {&c->keysA, &c->keysB, &c->valsA, &c->valsB, &c->sortState, &c->bounds, &c->sahQueue, &c->base, &c->normal, &c->rough,
                       &c->finalImg, &c->fxaaOut, &c->fb, &c->dbgT, &c->dbgA, &c->dbgB, &c->counters, &c->tmpA, &c->tmpB, &c->tmpC,
                       &c->tmpD, &c->samples, &c->workCounter, &c->wfPayload, &c->wfMeta, &c->wfFrames, &c->wfQO0, &c->wfQO1,
                       &c->wfQD0, &c->wfQD1, &c->wfQP0, &c->wfQP1, &c->wfHitTUV, &c->wfHitInst, &c->wfCounts, &c->wfOverflow, &c->jobTable,
@@ -755,7 +762,7 @@ rg_status rg_set_resolution(rg_ctx* c, uint32_t w, uint32_t h) {
 static rg_status run_post(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     PostParams pp;
     std::memset(&pp, 0, sizeof(pp));
-    pp.status = post_status(c);
+    pp.status = wait_status(c);
     pp.W = c->W;
     pp.H = c->H;
     pp.base = c->base.as<uint2>();
@@ -864,10 +871,10 @@ rg_status rg_download(rg_ctx* c, float* host) {
     if (!c->haveFrame) return fail(c, RG_ERR_NOT_READY, "no frame rendered");
     TRY(set_device(c));
     CK(cudaMemcpyAsync(host, c->fb.p, 16ull * c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(&c->hostCount[7], post_status(c), 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&c->hostCount[7], wait_status(c), 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     TRY(settle_graph(c));
-    if (c->hostCount[7]) return fail(c, RG_ERR_CUDA, "roughness pass: a staged tile copy did not complete");
+    if (c->hostCount[7]) return fail(c, RG_ERR_CUDA, wait_failure(c->hostCount[7]));
     return RG_OK;
 }
 
@@ -935,11 +942,11 @@ rg_status rg_download_image(rg_ctx* c, int32_t which, float* host) {
 rg_status rg_synchronize(rg_ctx* c) {
     if (!c) return RG_ERR_INVALID_ARG;
     TRY(set_device(c));
-    CK(cudaMemcpyAsync(&c->hostCount[7], post_status(c), 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&c->hostCount[7], wait_status(c), 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaStreamSynchronize(c->copyStream));
     TRY(settle_graph(c));
-    if (c->hostCount[7]) return fail(c, RG_ERR_CUDA, "roughness pass: a staged tile copy did not complete");
+    if (c->hostCount[7]) return fail(c, RG_ERR_CUDA, wait_failure(c->hostCount[7]));
     return RG_OK;
 }
 
@@ -1189,7 +1196,7 @@ cudaError_t enqueue_batch_posts(rg_ctx* c, const JobDesc* jd, const rg_job* jobs
         if (e != cudaSuccess) return e;
         PostParams pp;
         std::memset(&pp, 0, sizeof(pp));
-        pp.status = post_status(c);
+        pp.status = wait_status(c);
         pp.W = d.W;
         pp.H = d.H;
         pp.base = c->bBase.as<uint2>();

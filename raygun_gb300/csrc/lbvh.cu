@@ -438,6 +438,9 @@ __global__ void k_wide_records(const float* __restrict__ primBoxes, const uint32
 // records, refits and traversal are shared.
 constexpr int kSahBins = 16;
 constexpr int kSahWarps = 32;
+constexpr int kSahTaskWarps = 8;               // warps per block of k_sah_tasks
+constexpr uint32_t kSahHandoff = 64;           // tasks of a level from which k_sah_tasks takes over
+constexpr uint32_t kSahWaitLimit = 1u << 22;   // polls of an unpublished task before k_sah_tasks gives up
 
 __device__ __forceinline__ int ord_float(float f) {
     const int i = __float_as_int(f);
@@ -527,16 +530,6 @@ __device__ __forceinline__ void sah_level_grouped(const float* __restrict__ boxe
                 tScale[t][a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
             }
         }
-        if (!median)
-            for (int k = lane; k < 3 * kSahBins; k += 32) {
-                const int a = k / kSahBins, bn = k % kSahBins;
-                bCnt[lw][a][bn] = 0;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    bLo[lw][a][bn][c] = ord_float(INFINITY);
-                    bHi[lw][a][bn][c] = ord_float(-INFINITY);
-                }
-            }
     }
     __syncthreads();
     float tc[3] = {0.0f, 0.0f, 0.0f}, ts[3] = {0.0f, 0.0f, 0.0f};
@@ -550,26 +543,63 @@ __device__ __forceinline__ void sah_level_grouped(const float* __restrict__ boxe
         const float c = 0.5f * (bx[a] + bx[3 + a]);
         return max(0, min((int)((c - tc[a]) * ts[a]), kSahBins - 1));
     };
-    if (has && !median)  // every warp bins its chunk into the leader's bins
+    if (has && !median) {  // every warp bins its chunk into its own bins (no atomics across warps)
+        for (int k = lane; k < 3 * kSahBins; k += 32) {
+            const int a = k / kSahBins, bn = k % kSahBins;
+            bCnt[warp][a][bn] = 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                bLo[warp][a][bn][c] = ord_float(INFINITY);
+                bHi[warp][a][bn][c] = ord_float(-INFINITY);
+            }
+        }
+        __syncwarp();
         for (uint32_t i = cb + lane; i < ce; i += 32) {
             const float* bx = boxes + 6 * (size_t)order[i];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 if (ts[a] <= 0.0f) continue;
                 const int k = bin_of(bx, a);
-                atomicAdd(&bCnt[lw][a][k], 1);
+                atomicAdd(&bCnt[warp][a][k], 1);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    atomicMin(&bLo[lw][a][k][c], ord_float(bx[c]));
-                    atomicMax(&bHi[lw][a][k][c], ord_float(bx[3 + c]));
+                    atomicMin(&bLo[warp][a][k][c], ord_float(bx[c]));
+                    atomicMax(&bHi[warp][a][k][c], ord_float(bx[3 + c]));
                 }
             }
         }
+    }
     __syncthreads();
     if (has && m == 0) {  // the leader picks the split: cheapest surface-area cost, ties to the lowest candidate
         float bestCost = INFINITY;
         int bestCand = -1;
         if (!median) {
+            // the group's bins into the leader's (counts add, bounds are minima and maxima: exact)
+            for (int k = lane; k < 3 * kSahBins; k += 32) {
+                const int a = k / kSahBins, bn = k % kSahBins;
+                int cnt = bCnt[lw][a][bn];
+                int l[3], h[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    l[c] = bLo[lw][a][bn][c];
+                    h[c] = bHi[lw][a][bn][c];
+                }
+                for (uint32_t g = 1; g < G; ++g) {
+                    cnt += bCnt[lw + g][a][bn];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        l[c] = min(l[c], bLo[lw + g][a][bn][c]);
+                        h[c] = max(h[c], bHi[lw + g][a][bn][c]);
+                    }
+                }
+                bCnt[lw][a][bn] = cnt;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    bLo[lw][a][bn][c] = l[c];
+                    bHi[lw][a][bn][c] = h[c];
+                }
+            }
+            __syncwarp();
             for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
                 const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
                 if (ts[a] <= 0.0f) continue;
@@ -664,11 +694,320 @@ __device__ __forceinline__ void sah_level_grouped(const float* __restrict__ boxe
     }
 }
 
+// One node task on one warp: the range's box (written as the node's box) and centroid box, 16 bins
+// per axis in this warp's shared-memory bins, the cheapest of the 45 surface-area splits (ties to
+// the lowest candidate; no usable split or `median`: halve the range), a stable ballot partition of
+// order[b, e) through tmp, then emit(mid) creates the children and writes the node's refs.
+// COHERENT: order[] and tmp[] may have been written by other SMs (the task kernel), so they are read
+// through L2.
+// The same for a task of at most 32 * R primitives, with each lane's primitives (ids and boxes)
+// loaded once into registers: every pass reads them there, and the partition writes order[]
+// directly.  Same bounds, bins, costs and stable partition, so the same split.
+template <int R, bool COHERENT, class Emit>
+__device__ __forceinline__ void sah_task_warp_small(const float* __restrict__ boxes, uint32_t* __restrict__ order,
+                                                    float* __restrict__ nodeBoxes, uint32_t b, uint32_t e, uint32_t node, bool median,
+                                                    int (&wLo)[3][kSahBins][3], int (&wHi)[3][kSahBins][3], int (&wCnt)[3][kSahBins],
+                                                    int lane, Emit&& emit) {
+    uint32_t prim[R];
+    float bx[R][6];
+    bool valid[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const uint32_t i = b + (uint32_t)(32 * j + lane);
+        valid[j] = i < e;
+        prim[j] = valid[j] ? (COHERENT ? __ldcg(order + i) : order[i]) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) bx[j][c] = valid[j] ? boxes[6 * (size_t)prim[j] + c] : 0.0f;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+        if (valid[j])
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fminf(lo[a], bx[j][a]);
+                hi[a] = fmaxf(hi[a], bx[j][3 + a]);
+                const float c = 0.5f * (bx[j][a] + bx[j][3 + a]);
+                clo[a] = fminf(clo[a], c);
+                chi[a] = fmaxf(chi[a], c);
+            }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], off));
+            clo[a] = fminf(clo[a], __shfl_xor_sync(0xFFFFFFFFu, clo[a], off));
+            chi[a] = fmaxf(chi[a], __shfl_xor_sync(0xFFFFFFFFu, chi[a], off));
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            nodeBoxes[6 * (size_t)node + a] = lo[a];
+            nodeBoxes[6 * (size_t)node + 3 + a] = hi[a];
+        }
+    float scale[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ext = chi[a] - clo[a];
+        scale[a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
+    }
+    // bin of primitive j on axis a (a may be a runtime value: selects, not indexing, keep the boxes
+    // in registers)
+    auto bin_of = [&](int j, int a) {
+        const float l = a == 0 ? bx[j][0] : (a == 1 ? bx[j][1] : bx[j][2]);
+        const float h = a == 0 ? bx[j][3] : (a == 1 ? bx[j][4] : bx[j][5]);
+        const float o = a == 0 ? clo[0] : (a == 1 ? clo[1] : clo[2]);
+        const float s = a == 0 ? scale[0] : (a == 1 ? scale[1] : scale[2]);
+        const float c = 0.5f * (l + h);
+        return max(0, min((int)((c - o) * s), kSahBins - 1));
+    };
+    float bestCost = INFINITY;
+    int bestCand = -1;
+    if (!median) {
+        for (int k = lane; k < 3 * kSahBins; k += 32) {
+            const int a = k / kSahBins, bn = k % kSahBins;
+            wCnt[a][bn] = 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                wLo[a][bn][c] = ord_float(INFINITY);
+                wHi[a][bn][c] = ord_float(-INFINITY);
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+            if (valid[j])
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    if (scale[a] <= 0.0f) continue;
+                    const int k = bin_of(j, a);
+                    atomicAdd(&wCnt[a][k], 1);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        atomicMin(&wLo[a][k][c], ord_float(bx[j][c]));
+                        atomicMax(&wHi[a][k][c], ord_float(bx[j][3 + c]));
+                    }
+                }
+        __syncwarp();
+        for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
+            const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
+            if (scale[a] <= 0.0f) continue;
+            float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
+            int nl = 0, nr = 0;
+            for (int k = 0; k < kSahBins; ++k) {
+                const int cnt = wCnt[a][k];
+                if (!cnt) continue;
+                float* X0 = k < sp ? L0 : R0;
+                float* X1 = k < sp ? L1 : R1;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    X0[c] = fminf(X0[c], unord_float(wLo[a][k][c]));
+                    X1[c] = fmaxf(X1[c], unord_float(wHi[a][k][c]));
+                }
+                if (k < sp) nl += cnt;
+                else nr += cnt;
+            }
+            if (!nl || !nr) continue;
+            const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
+            if (cost < bestCost) {
+                bestCost = cost;
+                bestCand = cand;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
+            const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
+            if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
+                bestCost = oc;
+                bestCand = oi;
+            }
+        }
+    }
+    uint32_t mid = b + (e - b) / 2;  // no usable split (coincident centroids): halve the range
+    if (bestCand >= 0) {
+        const int a = bestCand / (kSahBins - 1), sp = bestCand % (kSahBins - 1) + 1;
+        bool isL[R];
+        uint32_t nl = 0;
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            isL[j] = valid[j] && bin_of(j, a) < sp;
+            nl += __popc(__ballot_sync(0xFFFFFFFFu, isL[j]));
+        }
+        uint32_t lb = 0, rb = 0;
+        const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+        for (int j = 0; j < R; ++j) {  // every lane holds its primitives already: write order[] in place
+            const unsigned lm = __ballot_sync(0xFFFFFFFFu, isL[j]), rm = __ballot_sync(0xFFFFFFFFu, valid[j] && !isL[j]);
+            if (isL[j]) order[b + lb + __popc(lm & below)] = prim[j];
+            else if (valid[j]) order[b + nl + rb + __popc(rm & below)] = prim[j];
+            lb += __popc(lm);
+            rb += __popc(rm);
+        }
+        __syncwarp();
+        mid = b + nl;
+    }
+    emit(mid);
+    __syncwarp();
+}
+
+template <bool COHERENT, class Emit>
+__device__ __forceinline__ void sah_task_warp(const float* __restrict__ boxes, uint32_t* __restrict__ order, uint32_t* __restrict__ tmp,
+                                              float* __restrict__ nodeBoxes, uint32_t b, uint32_t e, uint32_t node, bool median,
+                                              int (&wLo)[3][kSahBins][3], int (&wHi)[3][kSahBins][3], int (&wCnt)[3][kSahBins],
+                                              int lane, Emit&& emit) {
+    if (e - b <= 64) {
+        sah_task_warp_small<2, COHERENT>(boxes, order, nodeBoxes, b, e, node, median, wLo, wHi, wCnt, lane, emit);
+        return;
+    }
+    auto ord = [&](uint32_t i) { return COHERENT ? __ldcg(order + i) : order[i]; };
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = b + lane; i < e; i += 32) {
+        const float* bx = boxes + 6 * (size_t)ord(i);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], bx[a]);
+            hi[a] = fmaxf(hi[a], bx[3 + a]);
+            const float c = 0.5f * (bx[a] + bx[3 + a]);
+            clo[a] = fminf(clo[a], c);
+            chi[a] = fmaxf(chi[a], c);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], off));
+            clo[a] = fminf(clo[a], __shfl_xor_sync(0xFFFFFFFFu, clo[a], off));
+            chi[a] = fmaxf(chi[a], __shfl_xor_sync(0xFFFFFFFFu, chi[a], off));
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            nodeBoxes[6 * (size_t)node + a] = lo[a];
+            nodeBoxes[6 * (size_t)node + 3 + a] = hi[a];
+        }
+    float scale[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ext = chi[a] - clo[a];
+        scale[a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
+    }
+    auto bin_of = [&](const float* bx, int a) {
+        const float c = 0.5f * (bx[a] + bx[3 + a]);
+        return max(0, min((int)((c - clo[a]) * scale[a]), kSahBins - 1));
+    };
+    float bestCost = INFINITY;
+    int bestCand = -1;
+    if (!median) {
+        for (int k = lane; k < 3 * kSahBins; k += 32) {
+            const int a = k / kSahBins, bn = k % kSahBins;
+            wCnt[a][bn] = 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                wLo[a][bn][c] = ord_float(INFINITY);
+                wHi[a][bn][c] = ord_float(-INFINITY);
+            }
+        }
+        __syncwarp();
+        for (uint32_t i = b + lane; i < e; i += 32) {
+            const float* bx = boxes + 6 * (size_t)ord(i);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (scale[a] <= 0.0f) continue;
+                const int k = bin_of(bx, a);
+                atomicAdd(&wCnt[a][k], 1);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    atomicMin(&wLo[a][k][c], ord_float(bx[c]));
+                    atomicMax(&wHi[a][k][c], ord_float(bx[3 + c]));
+                }
+            }
+        }
+        __syncwarp();
+        for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
+            const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
+            if (scale[a] <= 0.0f) continue;
+            float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
+            int nl = 0, nr = 0;
+            for (int k = 0; k < kSahBins; ++k) {
+                const int cnt = wCnt[a][k];
+                if (!cnt) continue;
+                float* X0 = k < sp ? L0 : R0;
+                float* X1 = k < sp ? L1 : R1;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    X0[c] = fminf(X0[c], unord_float(wLo[a][k][c]));
+                    X1[c] = fmaxf(X1[c], unord_float(wHi[a][k][c]));
+                }
+                if (k < sp) nl += cnt;
+                else nr += cnt;
+            }
+            if (!nl || !nr) continue;
+            const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
+            if (cost < bestCost) {
+                bestCost = cost;
+                bestCand = cand;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
+            const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
+            if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
+                bestCost = oc;
+                bestCand = oi;
+            }
+        }
+    }
+    uint32_t mid = b + (e - b) / 2;  // no usable split (coincident centroids): halve the range
+    if (bestCand >= 0) {
+        const int a = bestCand / (kSahBins - 1), sp = bestCand % (kSahBins - 1) + 1;
+        uint32_t nl = 0;
+        for (uint32_t i0 = b; i0 < e; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool isL = i < e && bin_of(boxes + 6 * (size_t)ord(i), a) < sp;
+            nl += __popc(__ballot_sync(0xFFFFFFFFu, isL));
+        }
+        uint32_t lb = 0, rb = 0;
+        for (uint32_t i0 = b; i0 < e; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool valid = i < e;
+            const uint32_t prim = valid ? ord(i) : 0u;
+            const bool isL = valid && bin_of(boxes + 6 * (size_t)prim, a) < sp;
+            const unsigned lm = __ballot_sync(0xFFFFFFFFu, isL), rm = __ballot_sync(0xFFFFFFFFu, valid && !isL);
+            const unsigned below = (1u << lane) - 1u;
+            if (isL) tmp[b + lb + __popc(lm & below)] = prim;
+            else if (valid) tmp[b + nl + rb + __popc(rm & below)] = prim;
+            lb += __popc(lm);
+            rb += __popc(rm);
+        }
+        __syncwarp();
+        for (uint32_t i = b + lane; i < e; i += 32) order[i] = COHERENT ? __ldcg(tmp + i) : tmp[i];
+        __syncwarp();
+        mid = b + nl;
+    }
+    emit(mid);
+    __syncwarp();
+}
+
+// The top of the tree: one CTA, level by level (levels with fewer tasks than warps spread each task
+// over a group of warps), until a level has `handoff` tasks or more.  That level's tasks go to the
+// queue Q, whose slots are the node ids from baseCur on, and k_sah_tasks finishes the tree.
 __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __restrict__ boxes, uint32_t n, uint32_t* __restrict__ order,
                                                                  uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
                                                                  uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
                                                                  uint2* __restrict__ tasksA, uint2* __restrict__ tasksB,
-                                                                 uint32_t medianLevel, uint32_t* __restrict__ levelsOut) {
+                                                                 uint32_t medianLevel, uint32_t handoff, SahQueue Q,
+                                                                 uint32_t* __restrict__ levelsOut) {
     __shared__ int bLo[kSahWarps][3][kSahBins][3], bHi[kSahWarps][3][kSahBins][3];
     __shared__ int bCnt[kSahWarps][3][kSahBins];
     __shared__ uint32_t nCur, nNext, baseCur, baseNext, levels;
@@ -680,6 +1019,9 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
     __shared__ uint32_t wLeft[kSahWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) order[i] = i;
+    // every node starts as a valid (leaf 0, leaf 0) node, so a tree left unfinished (a task wait that
+    // gave up) still only refers to nodes and leaves in range
+    for (uint32_t i = threadIdx.x; i + 1 < n; i += blockDim.x) left[i] = right[i] = kLeaf;
     if (threadIdx.x == 0) {
         tasksA[0] = make_uint2(0u, n);  // range [0, n): node 0
         nCur = 1;
@@ -694,6 +1036,19 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
     for (;;) {
         const uint32_t count = nCur;
         if (count == 0) break;
+        if (count >= handoff) {  // the rest of the tree on every SM
+            for (uint32_t t = threadIdx.x; t < count; t += blockDim.x) {
+                const uint2 tk = cur[t];
+                Q.tasks[t] = make_uint4(tk.x, tk.y, baseCur + t, levels);
+                Q.ready[t] = 1u;  // the task kernel starts after this one
+            }
+            if (threadIdx.x == 0) {
+                Q.ctr[1] = count;
+                Q.ctr[2] = baseCur;
+                Q.ctr[3] = n - 1 - baseCur;
+            }
+            break;
+        }
         const bool median = levels >= medianLevel;  // from here on ranges are halved: the depth stays bounded
         if (count < (uint32_t)kSahWarps) {
             sah_level_grouped(boxes, order, tmp, left, right, nodeBoxes, cur, nxt, count, median, baseCur, baseNext, nNext, bLo, bHi,
@@ -702,151 +1057,23 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
         for (uint32_t t = warp; t < count; t += kSahWarps) {
             const uint2 tk = cur[t];
             const uint32_t b = tk.x, e = tk.y, node = baseCur + t;
-            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            for (uint32_t i = b + lane; i < e; i += 32) {
-                const float* bx = boxes + 6 * (size_t)order[i];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    lo[a] = fminf(lo[a], bx[a]);
-                    hi[a] = fmaxf(hi[a], bx[3 + a]);
-                    const float c = 0.5f * (bx[a] + bx[3 + a]);
-                    clo[a] = fminf(clo[a], c);
-                    chi[a] = fmaxf(chi[a], c);
-                }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    lo[a] = fminf(lo[a], __shfl_xor_sync(0xFFFFFFFFu, lo[a], off));
-                    hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xFFFFFFFFu, hi[a], off));
-                    clo[a] = fminf(clo[a], __shfl_xor_sync(0xFFFFFFFFu, clo[a], off));
-                    chi[a] = fmaxf(chi[a], __shfl_xor_sync(0xFFFFFFFFu, chi[a], off));
-                }
-            if (lane == 0)
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    nodeBoxes[6 * (size_t)node + a] = lo[a];
-                    nodeBoxes[6 * (size_t)node + 3 + a] = hi[a];
-                }
-            float scale[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const float ext = chi[a] - clo[a];
-                scale[a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
-            }
-            auto bin_of = [&](const float* bx, int a) {
-                const float c = 0.5f * (bx[a] + bx[3 + a]);
-                return max(0, min((int)((c - clo[a]) * scale[a]), kSahBins - 1));
-            };
-            float bestCost = INFINITY;
-            int bestCand = -1;
-            if (!median) {
-            for (int k = lane; k < 3 * kSahBins; k += 32) {
-                const int a = k / kSahBins, bn = k % kSahBins;
-                bCnt[warp][a][bn] = 0;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    bLo[warp][a][bn][c] = ord_float(INFINITY);
-                    bHi[warp][a][bn][c] = ord_float(-INFINITY);
-                }
-            }
-            __syncwarp();
-            for (uint32_t i = b + lane; i < e; i += 32) {
-                const float* bx = boxes + 6 * (size_t)order[i];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    if (scale[a] <= 0.0f) continue;
-                    const int k = bin_of(bx, a);
-                    atomicAdd(&bCnt[warp][a][k], 1);
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        atomicMin(&bLo[warp][a][k][c], ord_float(bx[c]));
-                        atomicMax(&bHi[warp][a][k][c], ord_float(bx[3 + c]));
-                    }
-                }
-            }
-            __syncwarp();
-            for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
-                const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
-                if (scale[a] <= 0.0f) continue;
-                float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
-                float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
-                int nl = 0, nr = 0;
-                for (int k = 0; k < kSahBins; ++k) {
-                    const int cnt = bCnt[warp][a][k];
-                    if (!cnt) continue;
-                    float* X0 = k < sp ? L0 : R0;
-                    float* X1 = k < sp ? L1 : R1;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        X0[c] = fminf(X0[c], unord_float(bLo[warp][a][k][c]));
-                        X1[c] = fmaxf(X1[c], unord_float(bHi[warp][a][k][c]));
-                    }
-                    if (k < sp) nl += cnt;
-                    else nr += cnt;
-                }
-                if (!nl || !nr) continue;
-                const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
-                if (cost < bestCost) {
-                    bestCost = cost;
-                    bestCand = cand;
-                }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
-                const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
-                if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
-                    bestCost = oc;
-                    bestCand = oi;
-                }
-            }
-            }  // !median
-            uint32_t mid = b + (e - b) / 2;  // no usable split (coincident centroids): halve the range
-            if (bestCand >= 0) {
-                const int a = bestCand / (kSahBins - 1), sp = bestCand % (kSahBins - 1) + 1;
-                uint32_t nl = 0;
-                for (uint32_t i0 = b; i0 < e; i0 += 32) {
-                    const uint32_t i = i0 + lane;
-                    const bool isL = i < e && bin_of(boxes + 6 * (size_t)order[i], a) < sp;
-                    nl += __popc(__ballot_sync(0xFFFFFFFFu, isL));
-                }
-                uint32_t lb = 0, rb = 0;
-                for (uint32_t i0 = b; i0 < e; i0 += 32) {
-                    const uint32_t i = i0 + lane;
-                    const bool valid = i < e;
-                    const uint32_t prim = valid ? order[i] : 0u;
-                    const bool isL = valid && bin_of(boxes + 6 * (size_t)prim, a) < sp;
-                    const unsigned lm = __ballot_sync(0xFFFFFFFFu, isL), rm = __ballot_sync(0xFFFFFFFFu, valid && !isL);
-                    const unsigned below = (1u << lane) - 1u;
-                    if (isL) tmp[b + lb + __popc(lm & below)] = prim;
-                    else if (valid) tmp[b + nl + rb + __popc(rm & below)] = prim;
-                    lb += __popc(lm);
-                    rb += __popc(rm);
-                }
-                __syncwarp();
-                for (uint32_t i = b + lane; i < e; i += 32) order[i] = tmp[i];
-                __syncwarp();
-                mid = b + nl;
-            }
-            if (lane == 0) {
-                const uint32_t rb0[2] = {b, mid}, re0[2] = {mid, e};
-                uint32_t ref[2];
-                for (int c = 0; c < 2; ++c) {
-                    if (re0[c] - rb0[c] == 1) {
-                        ref[c] = kLeaf | rb0[c];
-                    } else {
-                        const uint32_t idx = atomicAdd(&nNext, 1u);
-                        nxt[idx] = make_uint2(rb0[c], re0[c]);
-                        ref[c] = baseNext + idx;
-                    }
-                }
-                left[node] = ref[0];
-                right[node] = ref[1];
-            }
-            __syncwarp();
+            sah_task_warp<false>(boxes, order, tmp, nodeBoxes, b, e, node, median, bLo[warp], bHi[warp], bCnt[warp], lane,
+                                 [&](uint32_t mid) {  // single primitives become leaf refs, the rest next-level tasks
+                                     if (lane != 0) return;
+                                     const uint32_t rb0[2] = {b, mid}, re0[2] = {mid, e};
+                                     uint32_t ref[2];
+                                     for (int c = 0; c < 2; ++c) {
+                                         if (re0[c] - rb0[c] == 1) {
+                                             ref[c] = kLeaf | rb0[c];
+                                         } else {
+                                             const uint32_t idx = atomicAdd(&nNext, 1u);
+                                             nxt[idx] = make_uint2(rb0[c], re0[c]);
+                                             ref[c] = baseNext + idx;
+                                         }
+                                     }
+                                     left[node] = ref[0];
+                                     right[node] = ref[1];
+                                 });
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -862,6 +1089,72 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
         __syncthreads();
     }
     if (threadIdx.x == 0 && levelsOut) *levelsOut = levels;
+}
+
+// The rest of the tree on every SM: a warp claims the next queue slot, waits (bounded) until the
+// slot's task is published, splits it as k_sah_build does, and publishes its children's tasks in
+// the next free slots (node id = first node id of the queue + slot).  Every internal node is one
+// task, so the queue holds exactly n - 1 - (first node id) tasks and a warp whose claim lies beyond
+// that is done.  A slot's task is published by the warp that split its parent, which claimed an
+// earlier slot and runs, so every wait ends; a wait that still runs out sets *status to 2 and
+// leaves that subtree as prepared (valid refs, unset boxes).
+__global__ void __launch_bounds__(kSahTaskWarps * 32, 3) k_sah_tasks(const float* __restrict__ boxes, uint32_t* __restrict__ order,
+                                                                  uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
+                                                                  uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
+                                                                  SahQueue Q, uint32_t medianLevel, uint32_t* __restrict__ levelsOut,
+                                                                  int* __restrict__ status) {
+    __shared__ int bLo[kSahTaskWarps][3][kSahBins][3], bHi[kSahTaskWarps][3][kSahBins][3];
+    __shared__ int bCnt[kSahTaskWarps][3][kSahBins];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t total = Q.ctr[3], base = Q.ctr[2];  // written by k_sah_build
+    uint32_t deepest = 0;
+    for (;;) {
+        uint32_t slot = 0, ok = 1;
+        if (lane == 0) {
+            slot = atomicAdd(Q.ctr, 1u);
+            if (slot < total) {
+                for (uint32_t spins = 0; ld_relaxed(Q.ready + slot) == 0; ++spins) {
+                    if (spins >= kSahWaitLimit) {
+                        ok = 0;
+                        if (status) atomicExch(status, 2);
+                        break;
+                    }
+                    __nanosleep(128);
+                }
+            }
+        }
+        slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+        ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+        if (slot >= total || !ok) break;
+        __threadfence();  // after the publication: the task and its order[] range
+        const uint4 tk = __ldcg(Q.tasks + slot);
+        const uint32_t b = tk.x, e = tk.y, node = tk.z, level = tk.w;
+        deepest = max(deepest, level + 1);
+        sah_task_warp<true>(boxes, order, tmp, nodeBoxes, b, e, node, level >= medianLevel, bLo[warp], bHi[warp], bCnt[warp], lane,
+                            [&](uint32_t mid) {
+                                const uint32_t rb0[2] = {b, mid}, re0[2] = {mid, e};
+                                uint32_t ref[2] = {0u, 0u};
+                                if (lane == 0) {
+                                    for (int c = 0; c < 2; ++c) {
+                                        if (re0[c] - rb0[c] == 1) {
+                                            ref[c] = kLeaf | rb0[c];
+                                        } else {
+                                            const uint32_t q = atomicAdd(Q.ctr + 1, 1u);
+                                            ref[c] = base + q;
+                                            Q.tasks[q] = make_uint4(rb0[c], re0[c], base + q, level + 1);
+                                        }
+                                    }
+                                    left[node] = ref[0];
+                                    right[node] = ref[1];
+                                }
+                                __threadfence();  // every lane's order[] writes and the new tasks, then the publication
+                                __syncwarp();
+                                if (lane == 0)
+                                    for (int c = 0; c < 2; ++c)
+                                        if (!(ref[c] & kLeaf)) st_relaxed(Q.ready + (ref[c] - base), 1u);
+                            });
+    }
+    if (lane == 0 && levelsOut && deepest) atomicMax(levelsOut, deepest);
 }
 
 // parents of a BVH2 in the LBVH layout (internal node i at parents[i], the leaf at sorted position k
@@ -976,13 +1269,37 @@ cudaError_t lbvh_refit(const LbvhBuffers& b, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+static int sah_task_grid() {  // persistent grid of k_sah_tasks (every resident block)
+    static std::atomic<int> grid{0};
+    int g = grid.load(std::memory_order_acquire);
+    if (g) return g;
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sah_tasks, kSahTaskWarps * 32, 0) != cudaSuccess)
+        return 0;
+    g = sms * max(per, 1);
+    grid.store(g, std::memory_order_release);
+    return g;
+}
+
 cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t* levels, cudaStream_t s) {
     if (b.n <= 1) return cudaSuccess;
+    if (!b.sahQueue) return cudaErrorInvalidValue;
+    const int grid = sah_task_grid();
+    if (!grid) return cudaErrorUnknown;
+    SahQueue Q;
+    Q.tasks = reinterpret_cast<uint4*>(b.sahQueue);
+    Q.ready = reinterpret_cast<uint32_t*>(b.sahQueue + 16 * (size_t)b.n);
+    Q.ctr = Q.ready + b.n;
+    cudaError_t e = cudaMemsetAsync(Q.ready, 0, 4 * (size_t)b.n + 32, s);  // ready words and counters
+    if (e != cudaSuccess) return e;
     // scratch: the sort buffers (n words each); at most n / 2 tasks per level, 2 words each
     k_sah_build<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes,
                                               reinterpret_cast<uint2*>(b.valsA), reinterpret_cast<uint2*>(b.valsB), kSahMedianLevel,
-                                              levels);
-    count_launch();
+                                              kSahHandoff, Q, levels);
+    k_sah_tasks<<<grid, kSahTaskWarps * 32, 0, s>>>(b.primBoxes, b.order, b.keysA, b.left, b.right, b.nodeBoxes, Q, kSahMedianLevel,
+                                                     levels, b.status);
+    count_launch(2);
     if (parents) {
         k_parents<<<blocks(b.n - 1, 256), 256, 0, s>>>(b.left, b.right, b.n, b.parents);
         count_launch();

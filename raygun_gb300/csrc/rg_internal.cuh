@@ -136,7 +136,20 @@ struct LbvhBuffers {  // scratch + outputs of one LBVH build, sized by the calle
     uint32_t* parents;     // 2n (internal n-1 then leaves n)
     uint32_t* flags;       // n-1
     uint32_t* bounds;      // 6 (ordered uints)
+    // binned-SAH builds: the task queue of k_sah_tasks (sah_queue_bytes(n), 16-byte aligned) and a
+    // status word set to 2 when one of its waits gave up (nullable)
+    unsigned char* sahQueue = nullptr;
+    int* status = nullptr;
 };
+
+// task queue of the SAH builder's second kernel: n task records (range, node id, level), n ready
+// words, 8 counters (claims, pushes, first node id, tasks in total)
+struct SahQueue {
+    uint4* tasks;
+    uint32_t* ready;
+    uint32_t* ctr;
+};
+constexpr size_t sah_queue_bytes(size_t n) { return 20 * n + 32; }
 
 // onesweep radix sort of the Morton codes: keys per tile, and the layout of its state words (zeroed
 // by each build): 4 passes x 256 digit counts, 4 tile counters, then per pass one status word per
