@@ -478,6 +478,70 @@ def test_deep_sah_blas_bounded_and_traced(rg, orc):
     rt.ctx.close()
 
 
+def multi_chain_scene(chains=64, n_side=30, width=48, height=32):
+    """`chains` copies of the deep chain side by side (chain j at z = 2j).  Each surface-area split
+    peels the outermost triangles of every chain off at once, as a group that is then split along z,
+    so a level holds 64 node tasks from level 6 on -- where the builder's task kernel takes over --
+    while the chains still run past level 32, from which ranges are halved."""
+    xs = 17.0 ** np.arange(n_side)
+    pos, nrm, idx = [], [], []
+    for j in range(chains):
+        z = 2.0 * j
+        for sign in (1.0, -1.0):
+            for x in xs:
+                b = len(pos)
+                pos += [(sign * x, 0.0, z), (sign * x, 0.0, z + 0.5), (sign * x, 0.5, z)]
+                nrm += [(-sign, 0.0, 0.0)] * 3
+                idx.append((b, b + 1, b + 2))
+    mesh = S.Mesh(np.array(pos), np.array(nrm), np.array(idx, np.uint32))
+    mats = S.random_materials(S.Rng(8), 1)
+    ubo = S.make_ubo((0.0, 0.2, 30.0), (1.0, 0.2, 30.0), 90.0, width, height, (-0.4, -1.0, 0.3), 1, 3)
+    return S._finish("multi-chain", [(mesh, np.zeros(len(pos), np.uint32))], mats, S.identity_instance(), ubo, width, height)
+
+
+def tasks_per_level(tree):
+    """Internal nodes per level of a BVH2 in the LBVH layout."""
+    counts, st = {}, [(0, 0)]
+    while st:
+        i, lv = st.pop()
+        counts[lv] = counts.get(lv, 0) + 1
+        for c in (int(tree["left"][i]), int(tree["right"][i])):
+            if not c & 0x80000000:
+                st.append((c, lv + 1))
+    return counts
+
+
+def test_sah_task_kernel_past_the_median_level(rg, orc):
+    """The SAH builder's second kernel (a work queue over every SM, from the first level of 64
+    tasks on) builds the oracle's tree also where it halves ranges (level 32 on), and rays through
+    it hit what the oracle's rays hit."""
+    sc = multi_chain_scene()
+    n = int(sc.meshes["triCount"][0])
+    p = sc.vertices["position"][sc.indices.astype(np.int64)].reshape(n, 3, 3)
+    boxes = np.ascontiguousarray(np.concatenate([p.min(1), p.max(1)], 1), np.float32)
+    ref = orc.sah(boxes)
+    per = tasks_per_level(ref)
+    handoff = min(lv for lv, k in per.items() if k >= 64)
+    assert handoff < 32 and ref["levels"] > 33 and sum(k for lv, k in per.items() if lv >= 32) > 500, (handoff, ref["levels"])
+    rt = rg.Raytracer(sc).prepare()
+    assert orc.same_tree(rt.ctx.bvh(0), ref)
+    o = orc.OracleScene(sc)
+    rng = np.random.RandomState(4)
+    k = 4000
+    rays = np.zeros((k, 8), np.float32)
+    rays[:, 1] = rng.uniform(0.01, 0.2, k)
+    rays[:, 2] = 2.0 * rng.randint(0, 64, k) + rng.uniform(0.01, 0.2, k)  # inside one chain's triangles
+    rays[:, 3], rays[:, 7] = 1e-3, 3e38
+    rays[:, 4] = np.where(np.arange(k) < k // 2, 1.0, -1.0)
+    rays = np.concatenate([rays, camera_rays(sc)])
+    to, io = o.trace(rays)
+    assert (io[:, 0] != 0xFFFFFFFF).mean() > 0.3
+    tg, ig = rt.ctx.trace_rays(rays)
+    assert np.array_equal(ig, io) and np.array_equal(tg, to)
+    assert rt.ctx.stats()["deep_overflows"] == 0
+    rt.ctx.close()
+
+
 def stacked_scene(n=1 << 14, width=48, height=32):
     """n coincident triangles facing the camera.  Their centroids coincide, so the builder halves
     every range: a balanced tree of 14 levels whose boxes every camera ray enters, all at the same
@@ -501,6 +565,10 @@ def test_stack_overflow_is_retraced(rg, orc):
     48-word frame, which does not overflow, bit for bit."""
     sc = stacked_scene()
     rt = rg.Raytracer(sc).prepare()
+    # coincident centroids: every range is halved, on one CTA down to 64 tasks, then on every SM
+    n = int(sc.meshes["triCount"][0])
+    p = sc.vertices["position"][sc.indices.astype(np.int64)].reshape(n, 3, 3)
+    assert orc.same_tree(rt.ctx.bvh(0), orc.sah(np.ascontiguousarray(np.concatenate([p.min(1), p.max(1)], 1), np.float32)))
     ref = rt.render()
     assert rt.ctx.stats()["stack_overflows"] == 0
     o = orc.OracleScene(sc)
