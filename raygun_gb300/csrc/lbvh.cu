@@ -440,6 +440,7 @@ constexpr int kSahBins = 16;
 constexpr int kSahWarps = 32;
 constexpr int kSahTaskWarps = 8;               // warps per block of k_sah_tasks
 constexpr uint32_t kSahHandoff = 64;           // tasks of a level from which k_sah_tasks takes over
+constexpr int kSahParallelLevels = 6;          // levels built by k_sah_level, one launch each
 constexpr uint32_t kSahWaitLimit = 1u << 22;   // polls of an unpublished task before k_sah_tasks gives up
 
 __device__ __forceinline__ int ord_float(float f) {
@@ -999,15 +1000,50 @@ __device__ __forceinline__ void sah_task_warp(const float* __restrict__ boxes, u
     __syncwarp();
 }
 
-// The top of the tree: one CTA, level by level (levels with fewer tasks than warps spread each task
-// over a group of warps), until a level has `handoff` tasks or more.  That level's tasks go to the
-// queue Q, whose slots are the node ids from baseCur on, and k_sah_tasks finishes the tree.
+// The first kSahParallelLevels levels, one launch per level: CTA t of level L splits task t of the
+// level with all 32 of its warps (the grouped routine with one task), so the levels' tasks run on
+// separate SMs.  Level L's tasks are the node ids from base_L = 1 + count_1 + ... + count_(L-1) on
+// (count_0 = 1: the root), listed in tasksA for even L and tasksB for odd L; a child task takes the
+// next slot of level L + 1 from the global counter lvCount[L + 1].  Level 0 also prepares order[]
+// (identity) and the node refs (every node starts as (leaf 0, leaf 0), so a tree left unfinished by
+// a task wait that gave up only refers to nodes and leaves in range).
+__global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_level(const float* __restrict__ boxes, uint32_t n, uint32_t* __restrict__ order,
+                                                                 uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
+                                                                 uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
+                                                                 uint2* __restrict__ tasksA, uint2* __restrict__ tasksB,
+                                                                 uint32_t* __restrict__ lvCount, int level, uint32_t medianLevel) {
+    __shared__ int bLo[kSahWarps][3][kSahBins][3], bHi[kSahWarps][3][kSahBins][3];
+    __shared__ int bCnt[kSahWarps][3][kSahBins];
+    __shared__ float gPart[kSahWarps][12];
+    __shared__ float tClo[kSahWarps][3], tScale[kSahWarps][3];
+    __shared__ int tBest[kSahWarps];
+    __shared__ uint32_t wLeft[kSahWarps];
+    uint2* cur = (level & 1) ? tasksB : tasksA;
+    uint2* nxt = (level & 1) ? tasksA : tasksB;
+    if (level == 0) {
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) order[i] = i;
+        for (uint32_t i = threadIdx.x; i + 1 < n; i += blockDim.x) left[i] = right[i] = kLeaf;
+        if (threadIdx.x == 0) cur[0] = make_uint2(0u, n);
+        __syncthreads();
+    }
+    const uint32_t count = level == 0 ? 1u : lvCount[level];
+    if (blockIdx.x >= count) return;
+    uint32_t base = level == 0 ? 0u : 1u;
+    for (int k = 1; k < level; ++k) base += lvCount[k];
+    sah_level_grouped(boxes, order, tmp, left, right, nodeBoxes, cur + blockIdx.x, nxt, 1u, (uint32_t)level >= medianLevel,
+                      base + blockIdx.x, base + count, lvCount[level + 1], bLo, bHi, bCnt, gPart, tClo, tScale, tBest, wLeft);
+}
+
+// The rest of the top of the tree: one CTA, level by level from level kSahParallelLevels on (levels
+// with fewer tasks than warps spread each task over a group of warps), until a level has `handoff`
+// tasks or more.  That level's tasks go to the queue Q, whose slots are the node ids from baseCur
+// on, and k_sah_tasks finishes the tree.
 __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __restrict__ boxes, uint32_t n, uint32_t* __restrict__ order,
                                                                  uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
                                                                  uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
                                                                  uint2* __restrict__ tasksA, uint2* __restrict__ tasksB,
                                                                  uint32_t medianLevel, uint32_t handoff, SahQueue Q,
-                                                                 uint32_t* __restrict__ levelsOut) {
+                                                                 const uint32_t* __restrict__ lvCount, uint32_t* __restrict__ levelsOut) {
     __shared__ int bLo[kSahWarps][3][kSahBins][3], bHi[kSahWarps][3][kSahBins][3];
     __shared__ int bCnt[kSahWarps][3][kSahBins];
     __shared__ uint32_t nCur, nNext, baseCur, baseNext, levels;
@@ -1018,21 +1054,18 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_build(const float* __
     __shared__ int tBest[kSahWarps];
     __shared__ uint32_t wLeft[kSahWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) order[i] = i;
-    // every node starts as a valid (leaf 0, leaf 0) node, so a tree left unfinished (a task wait that
-    // gave up) still only refers to nodes and leaves in range
-    for (uint32_t i = threadIdx.x; i + 1 < n; i += blockDim.x) left[i] = right[i] = kLeaf;
-    if (threadIdx.x == 0) {
-        tasksA[0] = make_uint2(0u, n);  // range [0, n): node 0
-        nCur = 1;
+    if (threadIdx.x == 0) {  // the state after the level kernels (their counts; level 0: the root)
+        uint32_t base = 1, lv = 1;
+        while (lv < (uint32_t)kSahParallelLevels && lvCount[lv]) base += lvCount[lv++];
+        nCur = lv < (uint32_t)kSahParallelLevels ? 0u : lvCount[lv];
         nNext = 0;
-        baseCur = 0;   // node id of the current level's first task
-        baseNext = 1;  // node id of the next level's first task
-        levels = 0;
+        baseCur = base;          // node id of the current level's first task
+        baseNext = base + nCur;  // node id of the next level's first task
+        levels = lv;
     }
     __syncthreads();
-    uint2* cur = tasksA;
-    uint2* nxt = tasksB;
+    uint2* cur = (kSahParallelLevels & 1) ? tasksB : tasksA;
+    uint2* nxt = (kSahParallelLevels & 1) ? tasksA : tasksB;
     for (;;) {
         const uint32_t count = nCur;
         if (count == 0) break;
@@ -1291,15 +1324,20 @@ cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t* levels, cuda
     Q.tasks = reinterpret_cast<uint4*>(b.sahQueue);
     Q.ready = reinterpret_cast<uint32_t*>(b.sahQueue + 16 * (size_t)b.n);
     Q.ctr = Q.ready + b.n;
-    cudaError_t e = cudaMemsetAsync(Q.ready, 0, 4 * (size_t)b.n + 32, s);  // ready words and counters
+    uint32_t* lvCount = Q.ctr + 8;  // tasks per level of the level kernels
+    cudaError_t e = cudaMemsetAsync(Q.ready, 0, 4 * (size_t)b.n + 64, s);  // ready words and counters
     if (e != cudaSuccess) return e;
     // scratch: the sort buffers (n words each); at most n / 2 tasks per level, 2 words each
-    k_sah_build<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes,
-                                              reinterpret_cast<uint2*>(b.valsA), reinterpret_cast<uint2*>(b.valsB), kSahMedianLevel,
-                                              kSahHandoff, Q, levels);
+    uint2* tasksA = reinterpret_cast<uint2*>(b.valsA);
+    uint2* tasksB = reinterpret_cast<uint2*>(b.valsB);
+    for (int lv = 0; lv < kSahParallelLevels; ++lv)
+        k_sah_level<<<1u << lv, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes, tasksA,
+                                                         tasksB, lvCount, lv, kSahMedianLevel);
+    k_sah_build<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes, tasksA, tasksB,
+                                              kSahMedianLevel, kSahHandoff, Q, lvCount, levels);
     k_sah_tasks<<<grid, kSahTaskWarps * 32, 0, s>>>(b.primBoxes, b.order, b.keysA, b.left, b.right, b.nodeBoxes, Q, kSahMedianLevel,
                                                      levels, b.status);
-    count_launch(2);
+    count_launch(kSahParallelLevels + 2);
     if (parents) {
         k_parents<<<blocks(b.n - 1, 256), 256, 0, s>>>(b.left, b.right, b.n, b.parents);
         count_launch();

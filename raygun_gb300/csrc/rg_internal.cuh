@@ -142,14 +142,15 @@ struct LbvhBuffers {  // scratch + outputs of one LBVH build, sized by the calle
     int* status = nullptr;
 };
 
-// task queue of the SAH builder's second kernel: n task records (range, node id, level), n ready
-// words, 8 counters (claims, pushes, first node id, tasks in total)
+// task queue of the SAH builder's task kernel: n task records (range, node id, level), n ready
+// words, 8 counters (claims, pushes, first node id, tasks in total), 8 per-level task counts of its
+// level kernels
 struct SahQueue {
     uint4* tasks;
     uint32_t* ready;
     uint32_t* ctr;
 };
-constexpr size_t sah_queue_bytes(size_t n) { return 20 * n + 32; }
+constexpr size_t sah_queue_bytes(size_t n) { return 20 * n + 64; }
 
 // onesweep radix sort of the Morton codes: keys per tile, and the layout of its state words (zeroed
 // by each build): 4 passes x 256 digit counts, 4 tile counters, then per pass one status word per
