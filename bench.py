@@ -281,7 +281,8 @@ def run_ours(args):
     rt = rgcuda.Raytracer(sc, device=local).prepare()
     ctx = rt.ctx
     K, W = args.steps, args.warmup
-    total = 2 * (W + K) + 1
+    total = W + K + 1
+    pristine = sc.vertices.copy()  # frame 0's vertices (the animation below moves sc's)
     frames = FrameInputs(sc, total)
     dev = torch.device("cuda", local)
     ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
@@ -374,6 +375,12 @@ def run_ours(args):
     ctx.set_flags(0)
 
     # ---------------- e2e: host buffers through the C ABI ----------------
+    # the same frames as the device-resident loop: back to frame 0's vertices (and BLAS boxes), then
+    # frames 0 .. W + K - 1 again
+    ctx.update_vertices(0, pristine)
+    for b in np.unique(blas_ids):
+        ctx.refit_blas(int(b))
+    f = 0
     for _ in range(W):
         step_host(f)
         f += 1
