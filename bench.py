@@ -543,14 +543,15 @@ def run_batch(args):
     value, ms = replica_throughput(rays, e0.elapsed_time(e1), world, dev)
 
     # ---------------- e2e: job table from host memory, every image read back to pinned host memory ----
-    fb_pin = torch.empty(sum(pixels) * 16, dtype=torch.uint8).pin_memory()
-    fb_host = fb_pin.numpy()
-    offs = np.concatenate([[0], np.cumsum(pixels)]) * 16
+    # two pinned buffers: batch b's images are read back (rg_batch_download_async, every image of the
+    # batch in job order) while batch b + 1 renders
+    fb_pins = [torch.empty(sum(pixels) * 16, dtype=torch.uint8).pin_memory() for _ in range(2)]
+    nstep = [0]
 
     def step_host():
         ctx.render_batch(jobs)
-        for k, sc in enumerate(scenes):
-            ctx.batch_download(k, fb_host[offs[k]:offs[k + 1]].view(np.float32).reshape(sc.height, sc.width, 4))
+        ctx.batch_download_async(fb_pins[nstep[0] % 2].data_ptr())
+        nstep[0] += 1
 
     for _ in range(W):
         step_host()

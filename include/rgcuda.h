@@ -287,6 +287,12 @@ rg_status rg_render_batch(rg_ctx* ctx, const rg_job* jobs, uint32_t n);
 rg_status rg_batch_framebuffer(rg_ctx* ctx, uint32_t job, float** d_rgba);
 /* Job `job`'s image of the last batch to host memory; waits for the batch. */
 rg_status rg_batch_download(rg_ctx* ctx, uint32_t job, float* host_rgba);
+/* Every image of the last batch to host memory without waiting: the images, in job order and
+ * contiguous (sum of width*height*4 floats), are staged on the device (one of the two read-back
+ * slots rg_download_async uses) and copied to host_rgba (pinned memory for an overlapped copy) on the
+ * library's copy stream while later batches render.  host_rgba must stay valid and unread until
+ * rg_synchronize returns. */
+rg_status rg_batch_download_async(rg_ctx* ctx, float* host_rgba);
 rg_status rg_set_batch_tune(rg_ctx* ctx, const rg_batch_tune* tune);
 rg_status rg_get_batch_tune(rg_ctx* ctx, rg_batch_tune* out);
 /* ---- learned roughness filter -------------------------------------------------------------------

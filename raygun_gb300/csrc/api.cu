@@ -1545,6 +1545,25 @@ rg_status rg_autotune_batch(rg_ctx* c, const rg_job* jobs, uint32_t n, uint32_t 
     return RG_OK;
 }
 
+rg_status rg_batch_download_async(rg_ctx* c, float* host) {
+    if (!c || !host) return RG_ERR_INVALID_ARG;
+    if (c->batchOffset.empty()) return fail(c, RG_ERR_NOT_READY, "no batch rendered");
+    TRY(set_device(c));
+    const size_t last = c->batchOffset.size() - 1;
+    const size_t bytes = 16ull * (c->batchOffset[last] + (size_t)c->batchW[last] * c->batchH[last]);
+    const int k = c->readbackSlot;
+    TRY(ensure(c, c->readback[k], bytes));
+    if (c->copyIssued[k]) CK(cudaStreamWaitEvent(c->stream, c->copied[k], 0));  // the slot's previous copy left
+    CK(cudaMemcpyAsync(c->readback[k].p, c->batchFb.p, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaEventRecord(c->staged[k], c->stream));
+    CK(cudaStreamWaitEvent(c->copyStream, c->staged[k], 0));
+    CK(cudaMemcpyAsync(host, c->readback[k].p, bytes, cudaMemcpyDeviceToHost, c->copyStream));
+    CK(cudaEventRecord(c->copied[k], c->copyStream));
+    c->copyIssued[k] = true;
+    c->readbackSlot = k ^ 1;
+    return RG_OK;
+}
+
 rg_status rg_batch_framebuffer(rg_ctx* c, uint32_t job, float** d) {
     if (!c || !d) return RG_ERR_INVALID_ARG;
     if (job >= c->batchOffset.size()) return fail(c, RG_ERR_INVALID_ARG, "no such job in the last batch");

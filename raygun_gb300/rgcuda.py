@@ -36,7 +36,7 @@ EXPORTS = [
     "rg_get_stream", "rg_bvh_info", "rg_instance_inverse", "rg_trace_rays", "rg_post_only", "rg_lbvh_build_host",
     "rg_update_vertices_device", "rg_get_total_stats", "rg_reset_total_stats", "rg_set_flags", "rg_launch_count",
     "rg_lbvh_build_device_noalloc", "rg_scene_create", "rg_scene_select", "rg_scene_destroy", "rg_scene_bytes",
-    "rg_render_batch", "rg_batch_framebuffer", "rg_batch_download", "rg_set_batch_tune", "rg_get_batch_tune",
+    "rg_render_batch", "rg_batch_framebuffer", "rg_batch_download", "rg_batch_download_async", "rg_set_batch_tune", "rg_get_batch_tune",
     "rg_set_batch_slots", "rg_autotune_batch", "rg_get_memory", "rg_filter_create", "rg_filter_destroy",
     "rg_filter_last_error", "rg_filter_get_params", "rg_filter_set_params", "rg_filter_get_grads", "rg_filter_forward",
     "rg_filter_train_step", "rg_filter_input", "rg_filter_target", "rg_set_filter", "rg_set_glossy",
@@ -143,6 +143,7 @@ def load(path: str = LIB_PATH):
         "rg_render_batch": ([P, P, U32], I32),
         "rg_batch_framebuffer": ([P, U32, ctypes.POINTER(P)], I32),
         "rg_batch_download": ([P, U32, P], I32),
+        "rg_batch_download_async": ([P, P], I32),
         "rg_set_batch_tune": ([P, ctypes.POINTER(BatchTune)], I32),
         "rg_get_batch_tune": ([P, ctypes.POINTER(BatchTune)], I32),
         "rg_set_batch_slots": ([P, U32], I32),
@@ -261,6 +262,11 @@ class Context:
 
     def download_to(self, host_ptr: int):
         self._ck(self.L.rg_download(self.h, ctypes.c_void_p(host_ptr)))
+
+    def batch_download_async(self, host_ptr: int):
+        """Queue the read-back of every image of the last batch (job order, contiguous RGBA32F) into
+        host_ptr (valid until synchronize())."""
+        self._ck(self.L.rg_batch_download_async(self.h, ctypes.c_void_p(host_ptr)))
 
     def download_async(self, host_ptr: int):
         """Queue the read-back of the last frame into host_ptr (valid until synchronize())."""

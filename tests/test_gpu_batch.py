@@ -49,6 +49,36 @@ def test_batch_equals_single_renders(rg, batch):
     assert st["stack_overflows"] == 0
 
 
+def test_batch_download_async(rg, batch):
+    """rg_batch_download_async: every image of the last batch, in job order and contiguous, read back
+    on the copy stream while the next batch renders; two batches in flight, each equal to the single
+    renders (the second batch's cameras are the first's moved, so the two differ)."""
+    import torch
+    scenes, singles, _ = batch
+    br = rg.BatchRenderer(scenes)
+    jobs = br.jobs()
+    moved = jobs.copy()
+    for k, sc in enumerate(scenes):
+        moved[k]["ubo"] = S.make_ubo((3.0 + k, 9.0, -30.0), (0, 2, 0), 55.0, sc.width, sc.height, (-0.4, -1.0, 0.3),
+                                     int(sc.ubo["numSamples"][0]), int(sc.ubo["maxRecursions"][0]))[0]
+    sizes = [sc.height * sc.width * 4 for sc in scenes]
+    bufs = [torch.empty(sum(sizes), dtype=torch.float32).pin_memory() for _ in range(2)]
+    br.ctx.render_batch(jobs)
+    br.ctx.batch_download_async(bufs[0].data_ptr())
+    br.ctx.render_batch(moved)
+    br.ctx.batch_download_async(bufs[1].data_ptr())
+    second = [br.ctx.batch_download(k) for k in range(len(moved))]
+    br.ctx.synchronize()
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    for k, sc in enumerate(scenes):
+        a = bufs[0].numpy()[offs[k]:offs[k + 1]].reshape(sc.height, sc.width, 4)
+        b = bufs[1].numpy()[offs[k]:offs[k + 1]].reshape(sc.height, sc.width, 4)
+        assert np.array_equal(a, singles[k]), f"job {k}"
+        assert np.array_equal(b, second[k]), f"job {k}, second batch"
+    assert any(not np.array_equal(x, y) for x, y in zip(second, singles))
+    br.ctx.close()
+
+
 def test_host_loop_equals_graph(rg, batch):
     scenes, singles, stats = batch
     br = rg.BatchRenderer(scenes, flags=rg.RG_FLAG_HOST_LOOP)
