@@ -829,11 +829,12 @@ def run_spheres(args):
     rays = st["primary"] + st["shadow"] + st["secondary"]
     frame_ms = t["rtTotalSum"] / t["frames"]
     value = rays / (t["rtTotalSum"] * 1e-3) / 1e6
-    host = torch.empty(sc.height * sc.width * 4, dtype=torch.float32).pin_memory()
+    # two pinned framebuffers: frame f's read-back overlaps frame f + 1 (rg_download_async)
+    hosts = [torch.empty(sc.height * sc.width * 4, dtype=torch.float32).pin_memory() for _ in range(2)]
     t0 = time.perf_counter()
-    for _ in range(K):
+    for k in range(K):
         rt.do_raytracing()
-        ctx.download_to(host.data_ptr())
+        ctx.download_async(hosts[k % 2].data_ptr())
     ctx.synchronize()
     e2e_ms = (time.perf_counter() - t0) / K * 1e3
     o = oracle.OracleScene(sc)
