@@ -110,7 +110,9 @@ rg_status ensure_activations(rg_filter* f, size_t P, bool training) {
     return RG_OK;
 }
 
-rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W) {
+// training: keep layer 4's own activations (its ReLU mask in the backward pass); inference writes
+// only their sum with the skip, x5
+rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W, bool training) {
     if (!f->packed) TRY_F(refresh_weights(f));
     FilterConvArgs a;
     std::memset(&a, 0, sizeof a);
@@ -134,6 +136,7 @@ rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W) {
         if (l == 3) {
             c.add = f->y1.as<bf>();
             c.ya = f->x5.as<bf>();
+            if (!training) c.y = nullptr;
         }
         FCK(filter_conv(kCin[l], kCout[l], c, f->stream));
         in = outs[l];
@@ -162,7 +165,7 @@ cudaError_t filter_frame(rg_filter* f, const uint2* base, const uint2* normal, c
     cudaError_t e = f->x0.ensure(2 * 16 * P);
     if (e == cudaSuccess && ensure_activations(f, P, false) != RG_OK) e = cudaErrorMemoryAllocation;
     if (e == cudaSuccess) e = filter_gbuffer(base, normal, rough, P, samples, f->x0.p, s);
-    if (e == cudaSuccess && forward(f, f->x0.as<__nv_bfloat16>(), 1, (int)H, (int)W) != RG_OK) e = cudaErrorUnknown;
+    if (e == cudaSuccess && forward(f, f->x0.as<__nv_bfloat16>(), 1, (int)H, (int)W, false) != RG_OK) e = cudaErrorUnknown;
     if (e == cudaSuccess) e = filter_composite(base, f->out.as<float4>(), P, fade, showAlpha, finalImg, s);
     f->stream = saved;
     return e;
@@ -276,7 +279,7 @@ rg_status rg_filter_forward(rg_filter* f, const void* d_input, uint32_t B, uint3
     FCK(cudaSetDevice(f->device));
     const size_t P = (size_t)B * H * W;
     TRY_F(ensure_activations(f, P, false));
-    TRY_F(forward(f, static_cast<const __nv_bfloat16*>(d_input), (int)B, (int)H, (int)W));
+    TRY_F(forward(f, static_cast<const __nv_bfloat16*>(d_input), (int)B, (int)H, (int)W, false));
     FCK(cudaMemcpyAsync(d_out, f->out.p, 16 * P, cudaMemcpyDeviceToDevice, f->stream));
     int st = 0;
     FCK(cudaMemcpyAsync(&st, f->status.p, sizeof(int), cudaMemcpyDeviceToHost, f->stream));
@@ -297,7 +300,7 @@ rg_status rg_filter_train_step(rg_filter* f, const void* d_input, const float* d
     FCK(f->bPartial.ensure(sizeof(float) * biasBlocks * 64));
     FCK(f->lossPartial.ensure(sizeof(float) * lossBlocks));
     const bf* x0 = static_cast<const bf*>(d_input);
-    TRY_F(forward(f, x0, (int)B, (int)H, (int)W));
+    TRY_F(forward(f, x0, (int)B, (int)H, (int)W, true));
     FCK(filter_loss(f->out.as<float4>(), reinterpret_cast<const float4*>(d_target), P, 1.0f / (3.0f * (float)P), f->g5.p,
                     f->lossPartial.as<float>(), lossBlocks, f->stream));
     float* G = f->grads.as<float>();
