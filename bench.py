@@ -75,6 +75,7 @@ def parse():
     ap.add_argument("--filter-weights", default=None, help="filter: load these weights instead of training")
     ap.add_argument("--filter-save", default=None, help="filter: write the trained weights here")
     ap.add_argument("--no-tune", action="store_true", help="batch: skip the autotuner (default launch shape)")
+    ap.add_argument("--batch-slots", type=int, default=0, help="batch: path slots of the round loop (0: the library default)")
     ap.add_argument("--batch-scenes", type=int, default=64, help="batch: scenes per batch (profiling captures only)")
     return ap.parse_args()
 
@@ -501,6 +502,8 @@ def run_batch(args):
     scenes = S.batch_scenes(n=args.batch_scenes)
     br = rgcuda.BatchRenderer(scenes, device=local)
     ctx = br.ctx
+    if args.batch_slots:
+        ctx.set_batch_slots(args.batch_slots)
     jobs = br.jobs()
     K, W = args.steps, args.warmup
     dev = torch.device("cuda", local)
@@ -566,7 +569,9 @@ def run_batch(args):
     e2e_value, ms_e2e = replica_throughput(tot2["primary"] + tot2["shadow"] + tot2["secondary"], dt, world, dev)
     e2e = {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(rgcuda.JOB.itemsize * len(jobs)),
            "d2h_bytes_per_step": int(sum(pixels) * 16), "ms_per_step": ms_e2e / K,
-           "timing": "host wall clock around K batches, each followed by the read-back of every image (synchronous)"}
+           "timing": "host wall clock around K batches; each batch's images are read back to pinned host memory "
+                     "(rg_batch_download_async) while the next batch renders, and the clock stops once the last "
+                     "batch's images are in host memory"}
 
     # ---------------- roofline of the traversal launches (host-polled loop with events) ----------------
     ctx.set_flags(rgcuda.RG_FLAG_COUNT_VISITS)

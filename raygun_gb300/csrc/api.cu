@@ -117,7 +117,7 @@ struct rg_ctx {
     DevBuf bBase, bNormal, bRough, bFinal, bFxaa, batchFb;
     std::vector<size_t> batchOffset;           // per job: first pixel in batchFb
     std::vector<uint32_t> batchW, batchH;
-    uint32_t batchSlots = 1u << 23;            // path slots of the batch loop (path state ~1.6 KB each)
+    uint32_t batchSlots = 1u << 25;            // path slots of the batch loop (path state ~1.6 KB each: 54 GB at most)
     TraceTune tune;
     // graph form of the batch: second stream (loop body capture), instantiated graph and what it
     // was captured for, loop words (device), launch accounting
