@@ -1034,6 +1034,298 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_level(const float* __
                       base + blockIdx.x, base + count, lvCount[level + 1], bLo, bHi, bCnt, gPart, tClo, tScale, tBest, wLeft);
 }
 
+// ---- one task over many CTAs (the top levels of large builds) -------------------------------------
+// For builds of at least kSahSplitMin primitives, the first kSahSplitLevels levels split each task
+// over kSplitCtas CTAs, in five launches per level, because one SM would otherwise bin a whole
+// level's primitives.  CTA (t, m) takes chunk m of task t.
+//   0 bounds: the chunk's box and centroid box          -> part[t][m]
+//   1 bins:   the task's frame from all parts (minima and maxima: every CTA gets the same), the
+//             chunk binned per warp, the warps merged    -> bins[t][m]
+//   2 choose: all CTAs' bins merged (counts add, bounds are minima and maxima: exact), the split
+//             chosen as the one-CTA builder chooses it (every CTA gets the same), the chunk's lefts
+//             counted                                    -> left[t][m]; CTA m = 0: node box, best[t]
+//   3 scatter: the chunk partitioned stably into tmp, its lefts after the lefts of the chunks (and
+//             warps) before it
+//   4 finish: tmp back into order; CTA m = 0 emits the children as k_sah_level does
+// The tree is the one-CTA builder's: same bounds, bins, costs and candidate order, same stable
+// partition.
+constexpr int kSplitCtas = 32;
+constexpr int kSahSplitLevels = 3;
+constexpr uint32_t kSahSplitMin = 32768;
+constexpr int kBinInts = 3 * kSahBins * 7;  // counts, then lo xyz, then hi xyz per (axis, bin)
+
+struct SplitScratch {
+    float* part;  // [4][kSplitCtas][12]
+    int* bins;    // [4][kSplitCtas][kBinInts]
+    uint32_t* left;  // [4][kSplitCtas]
+    int* best;       // [4]
+};
+
+__device__ __forceinline__ int bin_slot_cnt(int a, int bn) { return a * kSahBins + bn; }
+__device__ __forceinline__ int bin_slot_lo(int a, int bn, int c) { return 3 * kSahBins + (a * kSahBins + bn) * 3 + c; }
+__device__ __forceinline__ int bin_slot_hi(int a, int bn, int c) { return 3 * kSahBins + 9 * kSahBins + (a * kSahBins + bn) * 3 + c; }
+
+// the task's frame (box, centroid origin and bin scale) from the parts of all its CTAs
+__device__ __forceinline__ void split_frame(const float* part, float* lo, float* hi, float* clo, float* scale) {
+    float chi[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = clo[a] = INFINITY;
+        hi[a] = chi[a] = -INFINITY;
+    }
+    for (int m = 0; m < kSplitCtas; ++m) {
+        const float* p = part + 12 * m;
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], p[a]);
+            hi[a] = fmaxf(hi[a], p[3 + a]);
+            clo[a] = fminf(clo[a], p[6 + a]);
+            chi[a] = fmaxf(chi[a], p[9 + a]);
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        const float ext = chi[a] - clo[a];
+        scale[a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
+    }
+}
+
+__global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_init(uint32_t n, uint32_t* __restrict__ order, uint32_t* __restrict__ left,
+                                                                uint32_t* __restrict__ right, uint2* __restrict__ tasksA) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        order[i] = i;
+        if (i + 1 < n) left[i] = right[i] = kLeaf;  // every node starts as (leaf 0, leaf 0)
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) tasksA[0] = make_uint2(0u, n);
+}
+
+__global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_split(const float* __restrict__ boxes, uint32_t* __restrict__ order,
+                                                                 uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
+                                                                 uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
+                                                                 uint2* __restrict__ tasksA, uint2* __restrict__ tasksB,
+                                                                 uint32_t* __restrict__ lvCount, SplitScratch X, int level, int phase,
+                                                                 uint32_t medianLevel) {
+    __shared__ int sb[kSahWarps][kBinInts];  // per-warp bins; merged bins in sb[0]
+    __shared__ float red[kSahWarps][12];
+    __shared__ uint32_t wl[kSahWarps];
+    __shared__ int sBest;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t t = blockIdx.x / kSplitCtas, m = blockIdx.x % kSplitCtas;
+    const uint32_t count = level == 0 ? 1u : lvCount[level];
+    if (t >= count) return;
+    uint2* cur = (level & 1) ? tasksB : tasksA;
+    uint2* nxt = (level & 1) ? tasksA : tasksB;
+    uint32_t base = level == 0 ? 0u : 1u;
+    for (int k = 1; k < level; ++k) base += lvCount[k];
+    const uint2 tk = cur[t];
+    const uint32_t b = tk.x, e = tk.y, node = base + t;
+    const uint32_t chunk = (e - b + kSplitCtas - 1) / kSplitCtas;
+    const uint32_t cb = min(e, b + m * chunk), ce = min(e, cb + chunk);
+    float* part = X.part + (size_t)t * kSplitCtas * 12;
+    int* binsT = X.bins + (size_t)t * kSplitCtas * kBinInts;
+    uint32_t* leftT = X.left + (size_t)t * kSplitCtas;
+    const bool median = (uint32_t)level >= medianLevel;
+    if (phase == 0) {  // the chunk's box and centroid box
+        float v[12];
+        for (int a = 0; a < 3; ++a) {
+            v[a] = v[6 + a] = INFINITY;
+            v[3 + a] = v[9 + a] = -INFINITY;
+        }
+        for (uint32_t i = cb + threadIdx.x; i < ce; i += blockDim.x) {
+            const float* bx = boxes + 6 * (size_t)order[i];
+            for (int a = 0; a < 3; ++a) {
+                v[a] = fminf(v[a], bx[a]);
+                v[3 + a] = fmaxf(v[3 + a], bx[3 + a]);
+                const float c = 0.5f * (bx[a] + bx[3 + a]);
+                v[6 + a] = fminf(v[6 + a], c);
+                v[9 + a] = fmaxf(v[9 + a], c);
+            }
+        }
+        for (int off = 16; off > 0; off >>= 1)
+            for (int k = 0; k < 12; ++k) {
+                const float o = __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
+                v[k] = (k % 6) < 3 ? fminf(v[k], o) : fmaxf(v[k], o);
+            }
+        if (lane == 0)
+            for (int k = 0; k < 12; ++k) red[warp][k] = v[k];
+        __syncthreads();
+        if (threadIdx.x < 12) {
+            const int k = threadIdx.x;
+            float r = red[0][k];
+            for (int w = 1; w < kSahWarps; ++w) r = (k % 6) < 3 ? fminf(r, red[w][k]) : fmaxf(r, red[w][k]);
+            part[12 * m + k] = r;
+        }
+        return;
+    }
+    float lo[3], hi[3], clo[3], scale[3];
+    split_frame(part, lo, hi, clo, scale);
+    auto bin_of = [&](const float* bx, int a) {
+        const float c = 0.5f * (bx[a] + bx[3 + a]);
+        return max(0, min((int)((c - clo[a]) * scale[a]), kSahBins - 1));
+    };
+    if (phase == 1) {  // the chunk binned per warp, the warps merged into this CTA's bins
+        if (median) return;
+        for (int k = lane; k < 3 * kSahBins; k += 32) {
+            const int a = k / kSahBins, bn = k % kSahBins;
+            sb[warp][bin_slot_cnt(a, bn)] = 0;
+            for (int c = 0; c < 3; ++c) {
+                sb[warp][bin_slot_lo(a, bn, c)] = ord_float(INFINITY);
+                sb[warp][bin_slot_hi(a, bn, c)] = ord_float(-INFINITY);
+            }
+        }
+        __syncwarp();
+        for (uint32_t i = cb + threadIdx.x; i < ce; i += blockDim.x) {
+            const float* bx = boxes + 6 * (size_t)order[i];
+            for (int a = 0; a < 3; ++a) {
+                if (scale[a] <= 0.0f) continue;
+                const int k = bin_of(bx, a);
+                atomicAdd(&sb[warp][bin_slot_cnt(a, k)], 1);
+                for (int c = 0; c < 3; ++c) {
+                    atomicMin(&sb[warp][bin_slot_lo(a, k, c)], ord_float(bx[c]));
+                    atomicMax(&sb[warp][bin_slot_hi(a, k, c)], ord_float(bx[3 + c]));
+                }
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < kBinInts; k += blockDim.x) {
+            int r = sb[0][k];
+            for (int w = 1; w < kSahWarps; ++w)
+                r = k < 3 * kSahBins ? r + sb[w][k] : (k < 3 * kSahBins + 9 * kSahBins ? min(r, sb[w][k]) : max(r, sb[w][k]));
+            binsT[(size_t)m * kBinInts + k] = r;
+        }
+        return;
+    }
+    if (phase == 2) {  // every CTA's bins merged, the split chosen, the chunk's lefts counted
+        if (!median)
+            for (int k = threadIdx.x; k < kBinInts; k += blockDim.x) {
+                int r = binsT[k];
+                for (int c = 1; c < kSplitCtas; ++c) {
+                    const int o = binsT[(size_t)c * kBinInts + k];
+                    r = k < 3 * kSahBins ? r + o : (k < 3 * kSahBins + 9 * kSahBins ? min(r, o) : max(r, o));
+                }
+                sb[0][k] = r;
+            }
+        __syncthreads();
+        if (warp == 0) {  // cheapest surface-area cost, ties to the lowest candidate
+            float bestCost = INFINITY;
+            int bestCand = -1;
+            if (!median) {
+                for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
+                    const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
+                    if (scale[a] <= 0.0f) continue;
+                    float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                    float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
+                    int nl = 0, nr = 0;
+                    for (int k = 0; k < kSahBins; ++k) {
+                        const int cnt = sb[0][bin_slot_cnt(a, k)];
+                        if (!cnt) continue;
+                        float* X0 = k < sp ? L0 : R0;
+                        float* X1 = k < sp ? L1 : R1;
+                        for (int c = 0; c < 3; ++c) {
+                            X0[c] = fminf(X0[c], unord_float(sb[0][bin_slot_lo(a, k, c)]));
+                            X1[c] = fmaxf(X1[c], unord_float(sb[0][bin_slot_hi(a, k, c)]));
+                        }
+                        if (k < sp) nl += cnt;
+                        else nr += cnt;
+                    }
+                    if (!nl || !nr) continue;
+                    const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
+                    if (cost < bestCost) {
+                        bestCost = cost;
+                        bestCand = cand;
+                    }
+                }
+                for (int off = 16; off > 0; off >>= 1) {
+                    const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
+                    const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
+                    if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
+                        bestCost = oc;
+                        bestCand = oi;
+                    }
+                }
+            }
+            if (lane == 0) sBest = bestCand;
+        }
+        __syncthreads();
+        const int best = sBest;
+        if (m == 0 && threadIdx.x == 0) {
+            X.best[t] = best;
+            for (int a = 0; a < 3; ++a) {
+                nodeBoxes[6 * (size_t)node + a] = lo[a];
+                nodeBoxes[6 * (size_t)node + 3 + a] = hi[a];
+            }
+        }
+        if (best < 0) return;
+        const int sa = best / (kSahBins - 1), sp = best % (kSahBins - 1) + 1;
+        uint32_t nl = 0;
+        for (uint32_t i = cb + threadIdx.x; i < ce; i += blockDim.x) nl += bin_of(boxes + 6 * (size_t)order[i], sa) < sp;
+        for (int off = 16; off > 0; off >>= 1) nl += __shfl_xor_sync(0xFFFFFFFFu, nl, off);
+        if (lane == 0) wl[warp] = nl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t s = 0;
+            for (int w = 0; w < kSahWarps; ++w) s += wl[w];
+            leftT[m] = s;
+        }
+        return;
+    }
+    const int best = X.best[t];
+    if (phase == 3) {  // stable partition of the chunk: warp sub-chunks in order, lanes in order
+        if (best < 0) return;
+        const int sa = best / (kSahBins - 1), sp = best % (kSahBins - 1) + 1;
+        uint32_t nlTotal = 0, before = 0;
+        for (uint32_t c = 0; c < (uint32_t)kSplitCtas; ++c) {
+            const uint32_t x = leftT[c];
+            if (c < m) before += x;
+            nlTotal += x;
+        }
+        const uint32_t sub = (ce - cb + kSahWarps - 1) / kSahWarps;
+        const uint32_t wb = min(ce, cb + warp * sub), we = min(ce, wb + sub);
+        uint32_t nl = 0;
+        for (uint32_t i0 = wb; i0 < we; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            nl += __popc(__ballot_sync(0xFFFFFFFFu, i < we && bin_of(boxes + 6 * (size_t)order[i], sa) < sp));
+        }
+        if (lane == 0) wl[warp] = nl;
+        __syncthreads();
+        uint32_t wBefore = 0;
+        for (int w = 0; w < warp; ++w) wBefore += wl[w];
+        const uint32_t lefts = before + wBefore;  // lefts ahead of this warp's sub-chunk in the task
+        uint32_t lb = b + lefts, rb = b + nlTotal + ((wb - b) - lefts);
+        for (uint32_t i0 = wb; i0 < we; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool valid = i < we;
+            const uint32_t prim = valid ? order[i] : 0u;
+            const bool isL = valid && bin_of(boxes + 6 * (size_t)prim, sa) < sp;
+            const unsigned lm = __ballot_sync(0xFFFFFFFFu, isL), rm = __ballot_sync(0xFFFFFFFFu, valid && !isL);
+            const unsigned below = (1u << lane) - 1u;
+            if (isL) tmp[lb + __popc(lm & below)] = prim;
+            else if (valid) tmp[rb + __popc(rm & below)] = prim;
+            lb += __popc(lm);
+            rb += __popc(rm);
+        }
+        return;
+    }
+    // phase 4: tmp back into order, the children
+    if (best >= 0)
+        for (uint32_t i = cb + threadIdx.x; i < ce; i += blockDim.x) order[i] = tmp[i];
+    if (m == 0 && threadIdx.x == 0) {
+        uint32_t nlTotal = 0;
+        for (uint32_t c = 0; c < (uint32_t)kSplitCtas; ++c) nlTotal += leftT[c];
+        const uint32_t mid = best >= 0 ? b + nlTotal : b + (e - b) / 2;
+        const uint32_t rb0[2] = {b, mid}, re0[2] = {mid, e};
+        uint32_t ref[2];
+        for (int c = 0; c < 2; ++c) {
+            if (re0[c] - rb0[c] == 1) {
+                ref[c] = kLeaf | rb0[c];
+            } else {
+                const uint32_t idx = atomicAdd(&lvCount[level + 1], 1u);
+                nxt[idx] = make_uint2(rb0[c], re0[c]);
+                ref[c] = base + count + idx;
+            }
+        }
+        left[node] = ref[0];
+        right[node] = ref[1];
+    }
+}
+
 // The rest of the top of the tree: one CTA, level by level from level kSahParallelLevels on (levels
 // with fewer tasks than warps spread each task over a group of warps), until a level has `handoff`
 // tasks or more.  That level's tasks go to the queue Q, whose slots are the node ids from baseCur
@@ -1330,14 +1622,31 @@ cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t* levels, cuda
     // scratch: the sort buffers (n words each); at most n / 2 tasks per level, 2 words each
     uint2* tasksA = reinterpret_cast<uint2*>(b.valsA);
     uint2* tasksB = reinterpret_cast<uint2*>(b.valsB);
-    for (int lv = 0; lv < kSahParallelLevels; ++lv)
+    int lv0 = 0;
+    if (b.n >= kSahSplitMin) {  // the first levels with each task over kSplitCtas CTAs
+        SplitScratch X;  // in the queue's task records, which k_sah_build fills only later
+        X.part = reinterpret_cast<float*>(Q.tasks);
+        X.bins = reinterpret_cast<int*>(X.part + 4 * kSplitCtas * 12);
+        X.left = reinterpret_cast<uint32_t*>(X.bins + 4 * kSplitCtas * kBinInts);
+        X.best = reinterpret_cast<int*>(X.left + 4 * kSplitCtas);
+        k_sah_init<<<2 * kSplitCtas, kSahWarps * 32, 0, s>>>(b.n, b.order, b.left, b.right, tasksA);
+        count_launch();
+        for (; lv0 < kSahSplitLevels; ++lv0)
+            for (int ph = 0; ph < 5; ++ph) {
+                k_sah_split<<<(1u << lv0) * kSplitCtas, kSahWarps * 32, 0, s>>>(b.primBoxes, b.order, b.keysA, b.left, b.right,
+                                                                                 b.nodeBoxes, tasksA, tasksB, lvCount, X, lv0, ph,
+                                                                                 kSahMedianLevel);
+                count_launch();
+            }
+    }
+    for (int lv = lv0; lv < kSahParallelLevels; ++lv)
         k_sah_level<<<1u << lv, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes, tasksA,
                                                          tasksB, lvCount, lv, kSahMedianLevel);
     k_sah_build<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes, tasksA, tasksB,
                                               kSahMedianLevel, kSahHandoff, Q, lvCount, levels);
     k_sah_tasks<<<grid, kSahTaskWarps * 32, 0, s>>>(b.primBoxes, b.order, b.keysA, b.left, b.right, b.nodeBoxes, Q, kSahMedianLevel,
                                                      levels, b.status);
-    count_launch(kSahParallelLevels + 2);
+    count_launch(kSahParallelLevels - lv0 + 2);
     if (parents) {
         k_parents<<<blocks(b.n - 1, 256), 256, 0, s>>>(b.left, b.right, b.n, b.parents);
         count_launch();

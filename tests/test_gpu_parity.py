@@ -511,11 +511,13 @@ def tasks_per_level(tree):
     return counts
 
 
-def test_sah_task_kernel_past_the_median_level(rg, orc):
-    """The SAH builder's second kernel (a work queue over every SM, from the first level of 64
-    tasks on) builds the oracle's tree also where it halves ranges (level 32 on), and rays through
-    it hit what the oracle's rays hit."""
-    sc = multi_chain_scene()
+@pytest.mark.parametrize("chains", [64, 640])
+def test_sah_task_kernel_past_the_median_level(rg, orc, chains):
+    """The SAH builder's task kernel (a work queue over every SM, from the first level of 64 tasks
+    on) builds the oracle's tree also where it halves ranges (level 32 on), and rays through it hit
+    what the oracle's rays hit.  640 chains (38,400 triangles) also take the first levels' tasks
+    over many CTAs each (builds of at least 32,768 primitives)."""
+    sc = multi_chain_scene(chains=chains)
     n = int(sc.meshes["triCount"][0])
     p = sc.vertices["position"][sc.indices.astype(np.int64)].reshape(n, 3, 3)
     boxes = np.ascontiguousarray(np.concatenate([p.min(1), p.max(1)], 1), np.float32)
