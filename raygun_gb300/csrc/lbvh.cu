@@ -453,6 +453,51 @@ __device__ __forceinline__ float half_area3(const float* lo, const float* hi) {
     return dx * dy + dy * dz + dz * dx;
 }
 
+// The cheapest of the 3 x 15 surface-area splits of a task's bins (ties to the lowest candidate),
+// reduced over the calling warp (all 32 lanes call it); -1 when no split leaves both sides
+// non-empty.  cnt(a, k), lo(a, k, c), hi(a, k, c) read bin k of axis a (bounds as ordered ints).
+template <class Cnt, class Lo, class Hi>
+__device__ __forceinline__ int sah_best_split(const float* scale, int lane, Cnt cnt, Lo lo, Hi hi) {
+    float bestCost = INFINITY;
+    int bestCand = -1;
+    for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
+        const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
+        if (scale[a] <= 0.0f) continue;
+        float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
+        float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
+        int nl = 0, nr = 0;
+        for (int k = 0; k < kSahBins; ++k) {
+            const int n = cnt(a, k);
+            if (!n) continue;
+            float* X0 = k < sp ? L0 : R0;
+            float* X1 = k < sp ? L1 : R1;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                X0[c] = fminf(X0[c], unord_float(lo(a, k, c)));
+                X1[c] = fmaxf(X1[c], unord_float(hi(a, k, c)));
+            }
+            if (k < sp) nl += n;
+            else nr += n;
+        }
+        if (!nl || !nr) continue;
+        const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
+        if (cost < bestCost) {
+            bestCost = cost;
+            bestCand = cand;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
+        const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
+        if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
+            bestCost = oc;
+            bestCand = oi;
+        }
+    }
+    return bestCand;
+}
+
 // One level with fewer tasks than warps: G warps share a task (G * count <= 32), each taking a
 // contiguous chunk of the task's range.  The same computation as one warp per task -- bounds and bin
 // contents are order-independent minima, maxima and counts, the split is chosen by the same rule, and
@@ -572,7 +617,6 @@ __device__ __forceinline__ void sah_level_grouped(const float* __restrict__ boxe
     }
     __syncthreads();
     if (has && m == 0) {  // the leader picks the split: cheapest surface-area cost, ties to the lowest candidate
-        float bestCost = INFINITY;
         int bestCand = -1;
         if (!median) {
             // the group's bins into the leader's (counts add, bounds are minima and maxima: exact)
@@ -601,41 +645,9 @@ __device__ __forceinline__ void sah_level_grouped(const float* __restrict__ boxe
                 }
             }
             __syncwarp();
-            for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
-                const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
-                if (ts[a] <= 0.0f) continue;
-                float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
-                float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
-                int nl = 0, nr = 0;
-                for (int k = 0; k < kSahBins; ++k) {
-                    const int cnt = bCnt[lw][a][k];
-                    if (!cnt) continue;
-                    float* X0 = k < sp ? L0 : R0;
-                    float* X1 = k < sp ? L1 : R1;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        X0[c] = fminf(X0[c], unord_float(bLo[lw][a][k][c]));
-                        X1[c] = fmaxf(X1[c], unord_float(bHi[lw][a][k][c]));
-                    }
-                    if (k < sp) nl += cnt;
-                    else nr += cnt;
-                }
-                if (!nl || !nr) continue;
-                const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
-                if (cost < bestCost) {
-                    bestCost = cost;
-                    bestCand = cand;
-                }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
-                const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
-                if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
-                    bestCost = oc;
-                    bestCand = oi;
-                }
-            }
+            bestCand = sah_best_split(ts, lane, [&](int a, int k) { return bCnt[lw][a][k]; },
+                                      [&](int a, int k, int c) { return bLo[lw][a][k][c]; },
+                                      [&](int a, int k, int c) { return bHi[lw][a][k][c]; });
         }
         if (lane == 0) tBest[t] = bestCand;
     }
@@ -766,7 +778,6 @@ __device__ __forceinline__ void sah_task_warp_small(const float* __restrict__ bo
         const float c = 0.5f * (l + h);
         return max(0, min((int)((c - o) * s), kSahBins - 1));
     };
-    float bestCost = INFINITY;
     int bestCand = -1;
     if (!median) {
         for (int k = lane; k < 3 * kSahBins; k += 32) {
@@ -794,41 +805,9 @@ __device__ __forceinline__ void sah_task_warp_small(const float* __restrict__ bo
                     }
                 }
         __syncwarp();
-        for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
-            const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
-            if (scale[a] <= 0.0f) continue;
-            float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
-            float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
-            int nl = 0, nr = 0;
-            for (int k = 0; k < kSahBins; ++k) {
-                const int cnt = wCnt[a][k];
-                if (!cnt) continue;
-                float* X0 = k < sp ? L0 : R0;
-                float* X1 = k < sp ? L1 : R1;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    X0[c] = fminf(X0[c], unord_float(wLo[a][k][c]));
-                    X1[c] = fmaxf(X1[c], unord_float(wHi[a][k][c]));
-                }
-                if (k < sp) nl += cnt;
-                else nr += cnt;
-            }
-            if (!nl || !nr) continue;
-            const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
-            if (cost < bestCost) {
-                bestCost = cost;
-                bestCand = cand;
-            }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
-            const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
-            if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
-                bestCost = oc;
-                bestCand = oi;
-            }
-        }
+        bestCand = sah_best_split(scale, lane, [&](int a, int k) { return wCnt[a][k]; },
+                                  [&](int a, int k, int c) { return wLo[a][k][c]; },
+                                  [&](int a, int k, int c) { return wHi[a][k][c]; });
     }
     uint32_t mid = b + (e - b) / 2;  // no usable split (coincident centroids): halve the range
     if (bestCand >= 0) {
@@ -905,7 +884,6 @@ __device__ __forceinline__ void sah_task_warp(const float* __restrict__ boxes, u
         const float c = 0.5f * (bx[a] + bx[3 + a]);
         return max(0, min((int)((c - clo[a]) * scale[a]), kSahBins - 1));
     };
-    float bestCost = INFINITY;
     int bestCand = -1;
     if (!median) {
         for (int k = lane; k < 3 * kSahBins; k += 32) {
@@ -933,41 +911,9 @@ __device__ __forceinline__ void sah_task_warp(const float* __restrict__ boxes, u
             }
         }
         __syncwarp();
-        for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
-            const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
-            if (scale[a] <= 0.0f) continue;
-            float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
-            float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
-            int nl = 0, nr = 0;
-            for (int k = 0; k < kSahBins; ++k) {
-                const int cnt = wCnt[a][k];
-                if (!cnt) continue;
-                float* X0 = k < sp ? L0 : R0;
-                float* X1 = k < sp ? L1 : R1;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    X0[c] = fminf(X0[c], unord_float(wLo[a][k][c]));
-                    X1[c] = fmaxf(X1[c], unord_float(wHi[a][k][c]));
-                }
-                if (k < sp) nl += cnt;
-                else nr += cnt;
-            }
-            if (!nl || !nr) continue;
-            const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
-            if (cost < bestCost) {
-                bestCost = cost;
-                bestCand = cand;
-            }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
-            const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
-            if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
-                bestCost = oc;
-                bestCand = oi;
-            }
-        }
+        bestCand = sah_best_split(scale, lane, [&](int a, int k) { return wCnt[a][k]; },
+                                  [&](int a, int k, int c) { return wLo[a][k][c]; },
+                                  [&](int a, int k, int c) { return wHi[a][k][c]; });
     }
     uint32_t mid = b + (e - b) / 2;  // no usable split (coincident centroids): halve the range
     if (bestCand >= 0) {
@@ -1204,42 +1150,11 @@ __global__ void __launch_bounds__(kSahWarps * 32, 1) k_sah_split(const float* __
             }
         __syncthreads();
         if (warp == 0) {  // cheapest surface-area cost, ties to the lowest candidate
-            float bestCost = INFINITY;
             int bestCand = -1;
             if (!median) {
-                for (int cand = lane; cand < 3 * (kSahBins - 1); cand += 32) {
-                    const int a = cand / (kSahBins - 1), sp = cand % (kSahBins - 1) + 1;
-                    if (scale[a] <= 0.0f) continue;
-                    float L0[3] = {INFINITY, INFINITY, INFINITY}, L1[3] = {-INFINITY, -INFINITY, -INFINITY};
-                    float R0[3] = {INFINITY, INFINITY, INFINITY}, R1[3] = {-INFINITY, -INFINITY, -INFINITY};
-                    int nl = 0, nr = 0;
-                    for (int k = 0; k < kSahBins; ++k) {
-                        const int cnt = sb[0][bin_slot_cnt(a, k)];
-                        if (!cnt) continue;
-                        float* X0 = k < sp ? L0 : R0;
-                        float* X1 = k < sp ? L1 : R1;
-                        for (int c = 0; c < 3; ++c) {
-                            X0[c] = fminf(X0[c], unord_float(sb[0][bin_slot_lo(a, k, c)]));
-                            X1[c] = fmaxf(X1[c], unord_float(sb[0][bin_slot_hi(a, k, c)]));
-                        }
-                        if (k < sp) nl += cnt;
-                        else nr += cnt;
-                    }
-                    if (!nl || !nr) continue;
-                    const float cost = half_area3(L0, L1) * (float)nl + half_area3(R0, R1) * (float)nr;
-                    if (cost < bestCost) {
-                        bestCost = cost;
-                        bestCand = cand;
-                    }
-                }
-                for (int off = 16; off > 0; off >>= 1) {
-                    const float oc = __shfl_xor_sync(0xFFFFFFFFu, bestCost, off);
-                    const int oi = __shfl_xor_sync(0xFFFFFFFFu, bestCand, off);
-                    if (oi >= 0 && (bestCand < 0 || oc < bestCost || (oc == bestCost && oi < bestCand))) {
-                        bestCost = oc;
-                        bestCand = oi;
-                    }
-                }
+                bestCand = sah_best_split(scale, lane, [&](int a, int k) { return sb[0][bin_slot_cnt(a, k)]; },
+                                          [&](int a, int k, int c) { return sb[0][bin_slot_lo(a, k, c)]; },
+                                          [&](int a, int k, int c) { return sb[0][bin_slot_hi(a, k, c)]; });
             }
             if (lane == 0) sBest = bestCand;
         }
