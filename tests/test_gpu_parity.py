@@ -44,7 +44,7 @@ def lbvh_equal(g, o):
 
 
 @pytest.mark.parametrize("n,dup", [(1, False), (2, False), (3, False), (100, False), (2049, True), (70000, False),
-                                   (300000, True), (1 << 20, False)])
+                                   (300000, True), (1 << 20, False), ((1 << 20) + 1, True)])
 def test_lbvh_build_bit_exact(rg, orc, n, dup):
     boxes = random_boxes(n, 7 + n, dup)
     ctx = rg.Context()

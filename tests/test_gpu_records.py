@@ -238,3 +238,25 @@ def test_sah_blas_matches_oracle(rg, orc):
             compared += 1
         assert compared >= 1
         rt.ctx.close()
+
+
+def triangle_soup(n, seed):
+    """n random triangles (side lengths up to ~2) scattered in a 100-unit cube, one mesh."""
+    rng = np.random.RandomState(seed)
+    c = rng.uniform(-50.0, 50.0, (n, 1, 3))
+    pos = (c + rng.uniform(-1.0, 1.0, (n, 3, 3))).reshape(-1, 3)
+    idx = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+    mesh = S.Mesh(pos, np.tile((0.0, 1.0, 0.0), (3 * n, 1)), idx)
+    mats = S.random_materials(S.Rng(seed), 1)
+    ubo = S.make_ubo((0.0, 0.0, -120.0), (0.0, 0.0, 0.0), 60.0, 32, 18, (-0.4, -1.0, 0.3), 1, 2)
+    return S._finish("soup", [(mesh, np.zeros(len(pos), np.uint32))], mats, S.identity_instance(), ubo, 32, 18)
+
+
+@pytest.mark.parametrize("n", [32767, 32768, 100003])
+def test_sah_blas_at_the_split_threshold(rg, orc, n):
+    """Builds just below and at the size from which the first levels split each task over many CTAs
+    (and a ragged larger one) give the oracle's binned-SAH tree."""
+    sc = triangle_soup(n, 17 + n)
+    rt = rg.Raytracer(sc).prepare()
+    assert orc.same_tree(rt.ctx.bvh(0), orc.sah(tri_boxes(sc, 0)))
+    rt.ctx.close()
