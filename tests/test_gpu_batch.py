@@ -267,7 +267,15 @@ def test_batch_errors(rg):
         ctx.set_batch_tune(128, 20, "none")
     with pytest.raises(rg.RgError):
         ctx.scene_destroy(0)  # the selected slot
+    fresh = rg.Context()
+    with pytest.raises(rg.RgError) as e:
+        fresh.batch_download_async(16)  # no batch rendered in this context
+    assert e.value.code == -4
+    fresh.close()
     ctx.render_batch(jobs)
+    with pytest.raises(rg.RgError) as e:
+        ctx.batch_download_async(0)  # null host buffer
+    assert e.value.code == -1
     with pytest.raises(rg.RgError):
         ctx.batch_download(1)
     assert ctx.batch_download(0).shape == (8, 16, 4)
