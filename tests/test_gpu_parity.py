@@ -159,6 +159,22 @@ def test_post_passes_bit_exact(spheres_pair, orc, show_alpha, fade):
     assert np.array_equal(rt.ctx.download_image("pre_fxaa"), dbg[3])
 
 
+@pytest.mark.parametrize("w,h", [(97, 55), (130, 33), (7, 90), (1, 1)])
+def test_post_passes_odd_and_ragged_sizes(rg, orc, w, h):
+    """The roughness pass stages its 64x32 tiles by TMA when the width is even and with plain loads
+    when it is odd; tiles at the right and bottom edges are partial, and FXAA clamps at every edge.
+    The composited frame stays bit-exact with the oracle's post passes."""
+    sc = S.spheres_scene(n_spheres=8, width=w, height=h, num_samples=1, max_recursions=3, seed=21)
+    ob, on, orr, _ = orc.OracleScene(sc).render()
+    rt = rg.Raytracer(sc).prepare()
+    for fx in (False, True):
+        rt.ctx.post_only(sc.ubo, ob, on, orr, fxaa=fx)
+        fin = rt.ctx.download()
+        ref = orc.post(sc.ubo, ob, on, orr, fxaa=fx)
+        assert np.array_equal(fin, ref), f"{w}x{h} fxaa={fx}: {np.mean(fin != ref)} differ"
+    rt.ctx.close()
+
+
 def test_animation_refit_and_tlas_rebuild(rg, orc):
     sc = small_two_level()
     rt = rg.Raytracer(sc, flags=rg.RG_FLAG_TLAS_LBVH | rg.RG_FLAG_BLAS_LBVH).prepare()
