@@ -175,6 +175,25 @@ def test_post_passes_odd_and_ragged_sizes(rg, orc, w, h):
     rt.ctx.close()
 
 
+@pytest.mark.parametrize("w,h,spp", [(97, 55, 2), (31, 9, 3)])
+def test_frame_at_odd_sizes(rg, orc, w, h, spp):
+    """Frames whose sizes are not multiples of the 8x4 work-item tiles (partial tiles in both
+    directions): G-buffers, final image and ray counts against the oracle."""
+    sc = S.spheres_scene(n_spheres=10, width=w, height=h, num_samples=spp, max_recursions=4, seed=23)
+    rt = rg.Raytracer(sc, flags=rg.RG_FLAG_DEBUG_IMAGES).prepare()
+    rt.do_raytracing(fxaa=False)
+    st = rt.ctx.stats()
+    gb = [rt.ctx.download_image(k) for k in ("base", "normal", "rough")]
+    fin = rt.render()
+    ob, on, orr, ost = orc.OracleScene(sc).render()
+    for k in ("primary", "shadow", "secondary", "masked"):
+        assert st[k] == ost[k], (k, st[k], ost[k])
+    for name, g, r in zip(("base", "normal", "rough"), gb, (ob, on, orr)):
+        assert_image_close(g, r, f"{w}x{h} {name}")
+    assert_image_close(fin, orc.post(sc.ubo, ob, on, orr), f"{w}x{h} final")
+    rt.ctx.close()
+
+
 def test_animation_refit_and_tlas_rebuild(rg, orc):
     sc = small_two_level()
     rt = rg.Raytracer(sc, flags=rg.RG_FLAG_TLAS_LBVH | rg.RG_FLAG_BLAS_LBVH).prepare()
