@@ -348,10 +348,13 @@ __global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t*
     uint32_t from = kLeaf | k;
     float cur[6];
     load_box_cg(primBoxes + 6 * (size_t)order[k], cur);
-    while (node != 0xFFFFFFFFu) {
+    // a finished tree has at most 64 levels and in-range parents; the bounds keep a tree that a
+    // failed build left unfinished from sending the climb out of range or round in circles
+    for (int level = 0; node < n - 1u && level < 128; ++level) {  // the root's parent is 0xFFFFFFFF
         if (arrive(&flags[node]) == 0) return;
         const uint32_t L = left[node], R = right[node];
         const uint32_t other = L == from ? R : L;
+        if ((other & kLeaf) ? (other & ~kLeaf) >= n : other >= n - 1u) break;  // in range in a finished tree
         float ob[6];
         if (other & kLeaf) load_box_cg(primBoxes + 6 * (size_t)order[other & ~kLeaf], ob);
         else load_box_cg(nodeBoxes + 6 * (size_t)other, ob);
@@ -1342,7 +1345,7 @@ __global__ void __launch_bounds__(kSahTaskWarps * 32, 3) k_sah_tasks(const float
                                                                   uint32_t* __restrict__ tmp, uint32_t* __restrict__ left,
                                                                   uint32_t* __restrict__ right, float* __restrict__ nodeBoxes,
                                                                   SahQueue Q, uint32_t medianLevel, uint32_t* __restrict__ levelsOut,
-                                                                  int* __restrict__ status) {
+                                                                  int* __restrict__ status, uint32_t waitLimit) {
     __shared__ int bLo[kSahTaskWarps][3][kSahBins][3], bHi[kSahTaskWarps][3][kSahBins][3];
     __shared__ int bCnt[kSahTaskWarps][3][kSahBins];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1354,7 +1357,7 @@ __global__ void __launch_bounds__(kSahTaskWarps * 32, 3) k_sah_tasks(const float
             slot = atomicAdd(Q.ctr, 1u);
             if (slot < total) {
                 for (uint32_t spins = 0; ld_relaxed(Q.ready + slot) == 0; ++spins) {
-                    if (spins >= kSahWaitLimit) {
+                    if (spins >= waitLimit) {
                         ok = 0;
                         if (status) atomicExch(status, 2);
                         break;
@@ -1559,8 +1562,12 @@ cudaError_t sah_build(const LbvhBuffers& b, bool parents, uint32_t* levels, cuda
                                                          tasksB, lvCount, lv, kSahMedianLevel);
     k_sah_build<<<1, kSahWarps * 32, 0, s>>>(b.primBoxes, b.n, b.order, b.keysA, b.left, b.right, b.nodeBoxes, tasksA, tasksB,
                                               kSahMedianLevel, kSahHandoff, Q, lvCount, levels);
+    // polls of an unpublished task before a warp gives up (RG_SAH_WAIT_LIMIT overrides; 0 makes
+    // the first unpublished slot end the wait, which tests use to check the reported status)
+    uint32_t waitLimit = kSahWaitLimit;
+    if (const char* env = getenv("RG_SAH_WAIT_LIMIT")) waitLimit = (uint32_t)strtoul(env, nullptr, 10);
     k_sah_tasks<<<grid, kSahTaskWarps * 32, 0, s>>>(b.primBoxes, b.order, b.keysA, b.left, b.right, b.nodeBoxes, Q, kSahMedianLevel,
-                                                     levels, b.status);
+                                                     levels, b.status, waitLimit);
     count_launch(kSahParallelLevels - lv0 + 2);
     if (parents) {
         k_parents<<<blocks(b.n - 1, 256), 256, 0, s>>>(b.left, b.right, b.n, b.parents);

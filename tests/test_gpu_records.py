@@ -260,3 +260,21 @@ def test_sah_blas_at_the_split_threshold(rg, orc, n):
     rt = rg.Raytracer(sc).prepare()
     assert orc.same_tree(rt.ctx.bvh(0), orc.sah(tri_boxes(sc, 0)))
     rt.ctx.close()
+
+
+def test_sah_task_wait_that_gives_up_is_reported(rg, monkeypatch):
+    """Every wait of the SAH task kernel is bounded.  With the bound at zero polls
+    (RG_SAH_WAIT_LIMIT=0) a warp that claims a slot whose task is not published yet gives up at
+    once: that part of the tree stays as prepared (in-range refs only), and the context reports it
+    at the next rg_synchronize as RG_ERR_CUDA naming the builder.  Nothing faults, and a refit of
+    the unfinished tree stays in range."""
+    monkeypatch.setenv("RG_SAH_WAIT_LIMIT", "0")
+    sc = triangle_soup(100003, 5)
+    rt = rg.Raytracer(sc)
+    rt.setup_model_buffers()
+    rt.setup_bottom_level_as()
+    rt.ctx.refit_blas(rt.blas_ids[0])
+    with pytest.raises(rg.RgError) as e:
+        rt.ctx.synchronize()
+    assert e.value.code == -2 and "SAH" in str(e.value), str(e.value)
+    rt.ctx.close()
