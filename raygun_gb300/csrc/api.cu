@@ -231,6 +231,13 @@ bool range_ok(SceneState& st, uint32_t vOff, uint32_t iOff, uint32_t n, uint32_t
 // status word of the device-side waits: 1 when a staged tile copy of the roughness pass never
 // landed, 2 when a task wait of the SAH builder gave up
 int* wait_status(rg_ctx* c) { return reinterpret_cast<int*>(c->counters.as<unsigned long long>() + 16); }
+// polls of a staged tile copy before the roughness pass gives up (RG_POST_WAIT_LIMIT overrides; 0
+// makes the pass give up on its first copy, which tests use to check the reported status -- the
+// pass still waits, with the full bound, for that copy to land before it returns)
+uint32_t post_wait_limit() {
+    const char* env = getenv("RG_POST_WAIT_LIMIT");
+    return env ? (uint32_t)strtoul(env, nullptr, 10) : (1u << 24);
+}
 const char* wait_failure(uint32_t code) {
     return code == 2 ? "BVH build: a task of the SAH builder was never published" : "roughness pass: a staged tile copy did not complete";
 }
@@ -763,6 +770,7 @@ static rg_status run_post(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     PostParams pp;
     std::memset(&pp, 0, sizeof(pp));
     pp.status = wait_status(c);
+    pp.waitLimit = post_wait_limit();
     pp.W = c->W;
     pp.H = c->H;
     pp.base = c->base.as<uint2>();
@@ -1197,6 +1205,7 @@ cudaError_t enqueue_batch_posts(rg_ctx* c, const JobDesc* jd, const rg_job* jobs
         PostParams pp;
         std::memset(&pp, 0, sizeof(pp));
         pp.status = wait_status(c);
+        pp.waitLimit = post_wait_limit();
         pp.W = d.W;
         pp.H = d.H;
         pp.base = c->bBase.as<uint2>();

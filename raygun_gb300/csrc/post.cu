@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kPostThreads, 1) k_rough_post(const __grid_con
         const int st = k & 1;
         const int x0 = (tile % tilesX) * TW, y0 = (tile / tilesX) * TH;
         if (tma) {
-            const bool ok = mbar_wait(&S.mbar[st], (uint32_t)(k >> 1) & 1u, P.status);
+            const bool ok = mbar_wait(&S.mbar[st], (uint32_t)(k >> 1) & 1u, P.status, P.waitLimit);
             if (__syncthreads_or(!ok)) {  // the copy did not land: wait once more (bounded) for it, then give up
                 if (threadIdx.x == 0) mbar_wait(&S.mbar[st], (uint32_t)(k >> 1) & 1u, nullptr);
                 __syncthreads();

@@ -340,6 +340,7 @@ struct PostParams {
     int showAlpha;
     int fxaa;
     int* status;           // nullable: set to 1 when a staged copy of the roughness pass never landed
+    uint32_t waitLimit;    // polls of a staged copy before the pass gives up (see post_wait_limit)
 };
 cudaError_t launch_rough_post(const PostParams& p, cudaStream_t s);
 cudaError_t launch_fxaa(const PostParams& p, cudaStream_t s);

@@ -20,10 +20,11 @@ __device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
 }
-// bounded wait on phase `phase`; false (and *status set) when it did not complete
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, int* status) {
+// bounded wait on phase `phase` (at most `limit` polls); false (and *status set) when it did not
+// complete
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, int* status, uint32_t limit = 1u << 24) {
     uint32_t done = 0;
-    for (int spin = 0; spin < (1 << 24) && !done; ++spin) {
+    for (uint32_t spin = 0; spin < limit && !done; ++spin) {
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)

@@ -282,6 +282,20 @@ def test_errors_are_status_codes(rg):
         ctx.render(u)
 
 
+def test_roughness_copy_wait_that_gives_up_is_reported(rg, monkeypatch):
+    """The roughness pass's waits for its TMA-staged tiles are bounded.  With the first wait's bound
+    at zero polls (RG_POST_WAIT_LIMIT=0) the pass gives up on its first tile, still waits (with the
+    full bound) for that copy to land, and returns; rg_download then reports RG_ERR_CUDA naming the
+    pass.  Nothing faults or hangs."""
+    monkeypatch.setenv("RG_POST_WAIT_LIMIT", "0")
+    sc = S.spheres_scene(n_spheres=6, width=96, height=54, num_samples=1, max_recursions=2, seed=2)  # even width: TMA
+    rt = rg.Raytracer(sc).prepare()
+    with pytest.raises(rg.RgError) as e:
+        rt.render()
+    assert e.value.code == -2 and "roughness" in str(e.value), str(e.value)
+    rt.ctx.close()
+
+
 def test_malformed_scene_rejected_on_host(rg, orc):
     """Index, vertex and material references that leave the uploaded buffers are rejected on the host
     with RG_ERR_INVALID_ARG before any kernel reads through them (the reference relied on Vulkan's
