@@ -221,8 +221,9 @@ rg_status rg_download_image(rg_ctx* ctx, int32_t which, float* host_rgba);
 rg_status rg_synchronize(rg_ctx* ctx);  /* waits for the render stream and for rg_download_async copies */
 /* rg_download and rg_synchronize also read the context's device-wait status: every device-side wait
  * of this library is bounded, and one that gave up (a staged tile copy of the roughness pass that
- * never landed, or a task of the SAH BVH builder that was never published) makes them return
- * RG_ERR_CUDA, with rg_last_error naming which.  No such wait ends this way in a correct run. */
+ * never landed, a task of the SAH BVH builder that was never published, or a copy or tensor-core
+ * wait of the learned filter in the frame) makes them return RG_ERR_CUDA, with rg_last_error
+ * naming which.  No such wait ends this way in a correct run. */
 /* Replaces Profiler (raygun/profiler.cpp:55-105): GPU ranges of the last frame. */
 rg_status rg_get_timings(rg_ctx* ctx, rg_timings* out);
 rg_status rg_get_stats(rg_ctx* ctx, rg_stats* out);

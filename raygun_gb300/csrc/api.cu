@@ -229,7 +229,7 @@ bool range_ok(SceneState& st, uint32_t vOff, uint32_t iOff, uint32_t n, uint32_t
 }
 
 // status word of the device-side waits: 1 when a staged tile copy of the roughness pass never
-// landed, 2 when a task wait of the SAH builder gave up
+// landed, 2 when a task wait of the SAH builder gave up, 3 when a wait of the learned filter did
 int* wait_status(rg_ctx* c) { return reinterpret_cast<int*>(c->counters.as<unsigned long long>() + 16); }
 // polls of a staged tile copy before the roughness pass gives up (RG_POST_WAIT_LIMIT overrides; 0
 // makes the pass give up on its first copy, which tests use to check the reported status -- the
@@ -239,7 +239,9 @@ uint32_t post_wait_limit() {
     return env ? (uint32_t)strtoul(env, nullptr, 10) : (1u << 24);
 }
 const char* wait_failure(uint32_t code) {
-    return code == 2 ? "BVH build: a task of the SAH builder was never published" : "roughness pass: a staged tile copy did not complete";
+    if (code == 2) return "BVH build: a task of the SAH builder was never published";
+    if (code == 3) return "learned filter: a copy or tensor-core completion wait gave up";
+    return "roughness pass: a staged tile copy did not complete";
 }
 
 rg_status ensure(rg_ctx* c, DevBuf& b, size_t bytes) {
@@ -791,7 +793,7 @@ static rg_status run_post(rg_ctx* c, const rg_ubo* ubo, int32_t fxaa) {
     TRY(cur_events(c, &fe));
     CK(cudaEventRecord(fe->ev[EV_POST0], c->stream));
     if (c->filter)  // the learned filter in place of the roughness passes, then the same FXAA
-        CK(filter_frame(c->filter, pp.base, pp.normal, pp.rough, c->W, c->H, (float)c->lastSamples, pp.fade, pp.showAlpha, pp.finalImg,
+        CK(filter_frame(c->filter, pp.base, pp.normal, pp.rough, c->W, c->H, (float)c->lastSamples, pp.fade, pp.showAlpha, pp.finalImg, wait_status(c),
                         c->stream));
     else
         CK(launch_rough_post(pp, c->stream));
@@ -1218,7 +1220,7 @@ cudaError_t enqueue_batch_posts(rg_ctx* c, const JobDesc* jd, const rg_job* jobs
         pp.showAlpha = d.ubo.showAlpha ? 1 : 0;
         pp.fxaa = (jobs[j].options & RG_JOB_FXAA) ? 1 : 0;
         if (jobs[j].options & RG_JOB_FILTER)  // the learned filter in place of the roughness passes
-            e = filter_frame(c->filter, pp.base, pp.normal, pp.rough, d.W, d.H, (float)d.S, pp.fade, pp.showAlpha, pp.finalImg,
+            e = filter_frame(c->filter, pp.base, pp.normal, pp.rough, d.W, d.H, (float)d.S, pp.fade, pp.showAlpha, pp.finalImg, wait_status(c),
                              c->stream);
         else
             e = launch_rough_post(pp, c->stream);

@@ -173,7 +173,7 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* mbar, uint32_t phas
         if ((spin & 255) == 255 && *abort) return false;
     }
     *abort = 1;
-    if (status) atomicExch(status, 1);
+    if (status) atomicExch(status, 3);  // 3: a wait of the learned filter gave up
     return false;
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(128, 1) k_filter_dw(const bf16* __restrict__ x
             umma_commit(&mbar);
         }
         first = false;
-        ok = __syncthreads_and(mbar_wait(&mbar, phase, status)) != 0;  // also: the next tile overwrites the operands
+        ok = __syncthreads_and(mbar_wait(&mbar, phase, status, 1u << 24, 3)) != 0;  // also: the next tile overwrites the operands
         phase ^= 1u;
         tc_fence_after();
     }

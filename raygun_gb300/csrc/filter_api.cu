@@ -112,14 +112,15 @@ rg_status ensure_activations(rg_filter* f, size_t P, bool training) {
 
 // training: keep layer 4's own activations (its ReLU mask in the backward pass); inference writes
 // only their sum with the skip, x5
-rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W, bool training) {
+// status: where a wait that gives up is reported (nullptr: the filter's own status word)
+rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W, bool training, int* status = nullptr) {
     if (!f->packed) TRY_F(refresh_weights(f));
     FilterConvArgs a;
     std::memset(&a, 0, sizeof a);
     a.B = B;
     a.H = H;
     a.W = W;
-    a.status = f->status.as<int>();
+    a.status = status ? status : f->status.as<int>();
     using bf = __nv_bfloat16;
     const bf* w[kL];
     for (int l = 0; l < kL; ++l) w[l] = f->wf[l].as<bf>();
@@ -156,7 +157,7 @@ rg_status forward(rg_filter* f, const __nv_bfloat16* x0, int B, int H, int W, bo
 namespace rg {
 
 cudaError_t filter_frame(rg_filter* f, const uint2* base, const uint2* normal, const uint2* rough, uint32_t W, uint32_t H, float samples,
-                         const float fade[4], int showAlpha, uint2* finalImg, cudaStream_t s) {
+                         const float fade[4], int showAlpha, uint2* finalImg, int* status, cudaStream_t s) {
     const size_t P = (size_t)W * H;
     cudaError_t e0 = cudaStreamSynchronize(f->stream);  // parameter updates issued on the filter's stream
     if (e0 != cudaSuccess) return e0;
@@ -165,7 +166,7 @@ cudaError_t filter_frame(rg_filter* f, const uint2* base, const uint2* normal, c
     cudaError_t e = f->x0.ensure(2 * 16 * P);
     if (e == cudaSuccess && ensure_activations(f, P, false) != RG_OK) e = cudaErrorMemoryAllocation;
     if (e == cudaSuccess) e = filter_gbuffer(base, normal, rough, P, samples, f->x0.p, s);
-    if (e == cudaSuccess && forward(f, f->x0.as<__nv_bfloat16>(), 1, (int)H, (int)W, false) != RG_OK) e = cudaErrorUnknown;
+    if (e == cudaSuccess && forward(f, f->x0.as<__nv_bfloat16>(), 1, (int)H, (int)W, false, status) != RG_OK) e = cudaErrorUnknown;
     if (e == cudaSuccess) e = filter_composite(base, f->out.as<float4>(), P, fade, showAlpha, finalImg, s);
     f->stream = saved;
     return e;

@@ -319,9 +319,10 @@ cudaError_t filter_composite(const uint2* base, const float4* pred, size_t P, co
                              cudaStream_t s);
 cudaError_t filter_target(const uint2* rough, size_t P, float4* out, cudaStream_t s);
 cudaError_t filter_bias_pad(const float* b, int cReal, int c, float* out, cudaStream_t s);
-// the filter on one frame (G-buffers -> input -> network -> composite into finalImg); filter_api.cu
+// the filter on one frame (G-buffers -> input -> network -> composite into finalImg); filter_api.cu.
+// status: the rendering context's device-wait status word (3 when a wait of the filter gave up)
 cudaError_t filter_frame(rg_filter* f, const uint2* base, const uint2* normal, const uint2* rough, uint32_t W, uint32_t H, float samples,
-                         const float fade[4], int showAlpha, uint2* finalImg, cudaStream_t s);
+                         const float fade[4], int showAlpha, uint2* finalImg, int* status, cudaStream_t s);
 const float4* filter_prediction(const rg_filter* f);  // [P] of the last frame: RGB, w unused
 
 struct PostParams {

@@ -20,9 +20,9 @@ __device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
 }
-// bounded wait on phase `phase` (at most `limit` polls); false (and *status set) when it did not
-// complete
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, int* status, uint32_t limit = 1u << 24) {
+// bounded wait on phase `phase` (at most `limit` polls); false (and *status set to `code`) when it
+// did not complete
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, int* status, uint32_t limit = 1u << 24, int code = 1) {
     uint32_t done = 0;
     for (uint32_t spin = 0; spin < limit && !done; ++spin) {
         asm volatile(
@@ -31,7 +31,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, int* s
             : "r"(smem_u32(mbar)), "r"(phase)
             : "memory");
     }
-    if (!done && status) atomicExch(status, 1);
+    if (!done && status) atomicExch(status, code);
     return done != 0;
 }
 // orders this thread's earlier generic-proxy shared-memory accesses before later async-proxy ones
