@@ -21,6 +21,7 @@
 // integer n -> repeated multiply; a zero direction (refract at total internal reflection) -> no
 // traversal, miss shader; clamp/min/max treat a NaN operand as absent (fminf/fmaxf).
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -1968,7 +1969,11 @@ cudaError_t capture_trace_batch(const TraceParams& p0, const TraceTune& tune, co
         trace<<<gTrace, tune.threads, 0, s2>>>(p, q);
         k_wf_shade<true><<<gShade, 128, 0, s2>>>(p, q);
     }
-    k_batch_continue<<<1, 1, 0, s2>>>(h, p.wf.counts, p.workCounter, p.totalWork, (uint32_t)RG_TAIL_RAYS, 50000u, loopWords);
+    // body runs before the loop stops with its limit flag set (RG_BATCH_LOOP_LIMIT overrides, read
+    // when the graph is captured; tests use a small limit to check the reported error)
+    uint32_t maxIter = 50000u;
+    if (const char* env = getenv("RG_BATCH_LOOP_LIMIT")) maxIter = (uint32_t)strtoul(env, nullptr, 10);
+    k_batch_continue<<<1, 1, 0, s2>>>(h, p.wf.counts, p.workCounter, p.totalWork, (uint32_t)RG_TAIL_RAYS, maxIter, loopWords);
     cudaGraph_t captured = nullptr;
     e = cudaStreamEndCapture(s2, &captured);
     if (e != cudaSuccess) return e;

@@ -279,3 +279,23 @@ def test_batch_errors(rg):
     with pytest.raises(rg.RgError):
         ctx.batch_download(1)
     assert ctx.batch_download(0).shape == (8, 16, 4)
+
+
+def test_batch_loop_limit_is_reported(rg, batch, monkeypatch):
+    """The device-side round loop of the batch graph stops at an iteration limit and leaves a sticky
+    flag, which the host reports as RG_ERR_CUDA at the next read-back.  Forced here with a limit of
+    one body run (RG_BATCH_LOOP_LIMIT, read when the graph is captured): nothing faults or hangs,
+    and a new context renders the batch correctly."""
+    scenes, singles, _ = batch
+    monkeypatch.setenv("RG_BATCH_LOOP_LIMIT", "1")
+    br = rg.BatchRenderer(scenes)
+    br.ctx.set_batch_slots(1024)  # a small pool: the batch needs many more than two rounds
+    br.ctx.render_batch(br.jobs())
+    with pytest.raises(rg.RgError) as e:
+        br.ctx.batch_download(0)
+    assert e.value.code == -2 and "iteration limit" in str(e.value), str(e.value)
+    br.ctx.close()
+    monkeypatch.delenv("RG_BATCH_LOOP_LIMIT")
+    br = rg.BatchRenderer(scenes)
+    assert all(np.array_equal(a, b) for a, b in zip(br.render(), singles))
+    br.ctx.close()
