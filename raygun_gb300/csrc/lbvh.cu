@@ -335,10 +335,12 @@ __device__ __forceinline__ uint32_t arrive(uint32_t* flag) {  // release my box,
     return old;
 }
 
-// one thread per leaf climbs towards the root; at each node the first arrival stops and the second,
-// which then sees the first's box (release / acquire on the node's arrival counter), writes the
-// union.  The climbing thread keeps the box of the child it comes from in registers and loads only
-// its sibling's.
+// one thread per leaf climbs towards the root and writes each node's box as the union of its
+// children's.  The climbing thread keeps the box of the child it comes from in registers and loads
+// only its sibling's.  A leaf sibling's box is input data, so a node with a leaf child needs no
+// arrival: the thread from its inner child (or, for two leaves, from its left leaf) goes on and the
+// other stops at once.  A node with two inner children takes the arrival counter: the first
+// arrival stops, the second (which then sees the first's box: release / acquire) goes on.
 __global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t* __restrict__ order, uint32_t n,
                             const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
                             const uint32_t* __restrict__ parents, uint32_t* flags, float* nodeBoxes) {
@@ -346,15 +348,21 @@ __global__ void k_bottom_up(const float* __restrict__ primBoxes, const uint32_t*
     if (k >= n) return;
     uint32_t node = parents[(n - 1) + k];
     uint32_t from = kLeaf | k;
-    float cur[6];
-    load_box_cg(primBoxes + 6 * (size_t)order[k], cur);
+    float cur[6];  // loaded once this thread knows that it goes on from its leaf
     // a finished tree has at most 64 levels and in-range parents; the bounds keep a tree that a
     // failed build left unfinished from sending the climb out of range or round in circles
     for (int level = 0; node < n - 1u && level < 128; ++level) {  // the root's parent is 0xFFFFFFFF
-        if (arrive(&flags[node]) == 0) return;
         const uint32_t L = left[node], R = right[node];
         const uint32_t other = L == from ? R : L;
         if ((other & kLeaf) ? (other & ~kLeaf) >= n : other >= n - 1u) break;  // in range in a finished tree
+        if (other & kLeaf) {
+            if ((from & kLeaf) && L != from) return;  // two leaves: the left one goes on
+        } else if (from & kLeaf) {
+            return;  // the thread from the inner child goes on
+        } else if (arrive(&flags[node]) == 0) {
+            return;  // two inner children: the second arrival goes on
+        }
+        if (level == 0) load_box_cg(primBoxes + 6 * (size_t)order[k], cur);
         float ob[6];
         if (other & kLeaf) load_box_cg(primBoxes + 6 * (size_t)order[other & ~kLeaf], ob);
         else load_box_cg(nodeBoxes + 6 * (size_t)other, ob);
