@@ -459,8 +459,9 @@ def run_ours(args):
                  "stack_overflows": sst["stack_overflows"],
                  "rays_def": "GENERIC reflection + refraction rays at the hits of 3840x2160 pixel-centre camera rays "
                              "(the 4-spp frame's primary-ray count), materials as uploaded",
-                 "kernel": "rg_trace_rays_device: queue fill + one k_wf_trace launch + hit read-out, CUDA events on the "
-                           "library stream, L2 flushed before each launch"}
+                 "kernel": "rg_trace_rays_device: one k_wf_trace launch in its query form (rays read from the caller's "
+                           "buffer, hits written into the caller's buffers), CUDA events on the library stream, L2 "
+                           "flushed before each launch"}
 
     out = {
         "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": K, "warmup": W,

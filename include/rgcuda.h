@@ -375,8 +375,10 @@ rg_status rg_instance_inverse(rg_ctx* ctx, float* out);
  * statistics: rg_get_stats afterwards reports this call's stack_overflows / deep_overflows. */
 rg_status rg_trace_rays(rg_ctx* ctx, const float* rays, uint32_t n, float* hit_tuv, uint32_t* hit_ids);
 /* The same closest hits from and into device memory, asynchronous on the context's stream, traced by
- * one launch of the frame loop's traversal kernel (the rays fill its ray queue; no shading follows).
- * The hits equal rg_trace_rays'.  Like the reference's traceRayEXT of a batch of rays with no
+ * one launch of the frame loop's traversal kernel, which reads the rays where they are (d_rays
+ * 16-byte aligned, else RG_ERR_INVALID_ARG) and writes the hits straight into d_hit_tuv / d_hit_ids;
+ * no shading follows.  Stack depth as rg_trace_rays' (48 with RG_FLAG_COUNT_VISITS); rays that
+ * overflow it are traced again with the deep stack.  The hits equal rg_trace_rays'.  Like the reference's traceRayEXT of a batch of rays with no
  * shading (closesthit.rchit:215,232,244 issue such rays), it is how incoherent secondary-ray
  * throughput is measured.  Resets the per-frame statistics (stack_overflows; nodes / tris with
  * RG_FLAG_COUNT_VISITS). */

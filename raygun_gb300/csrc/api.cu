@@ -1139,18 +1139,13 @@ rg_status rg_trace_rays(rg_ctx* c, const float* rays, uint32_t n, float* tuv, ui
 
 rg_status rg_trace_rays_device(rg_ctx* c, const float* d_rays, uint32_t n, float* d_tuv, uint32_t* d_ids) {
     if (!c || (n && (!d_rays || !d_tuv || !d_ids))) return RG_ERR_INVALID_ARG;
+    if (reinterpret_cast<uintptr_t>(d_rays) & 15u) return fail(c, RG_ERR_INVALID_ARG, "trace_rays_device: rays must be 16-byte aligned");
     if (!c->sc->tlasReady) return fail(c, RG_ERR_NOT_READY, "no TLAS");
     if (!n) return RG_OK;
     TRY(set_device(c));
-    // the queue, hit records and overflow list of the frame loop, sized for n rays (no path state)
-    const size_t Q = n;
-    TRY(ensure(c, c->wfQO0, 16 * Q));
-    TRY(ensure(c, c->wfQO1, 16));
-    TRY(ensure(c, c->wfQD0, 16 * Q));
-    TRY(ensure(c, c->wfQD1, 16));
-    TRY(ensure(c, c->wfHitTUV, 16 * Q));
-    TRY(ensure(c, c->wfHitInst, 4 * Q));
-    TRY(ensure(c, c->wfOverflow, 4 * Q));
+    // the traversal kernel reads the rays and writes the hits in the caller's buffers; of the frame
+    // loop's state it uses the counters and the overflow list (rays re-traced with the deep stack)
+    TRY(ensure(c, c->wfOverflow, 4ull * n));
     if (!c->wfCounts.p) {
         TRY(ensure(c, c->wfCounts, 32));
         CK(cudaMemsetAsync(c->wfCounts.p, 0, 32, c->stream));
@@ -1160,16 +1155,10 @@ rg_status rg_trace_rays_device(rg_ctx* c, const float* d_rays, uint32_t n, float
     tp.scene = scene_of(*c->sc);
     tp.counters = c->counters.as<unsigned long long>();
     tp.countVisits = (c->flags & RG_FLAG_COUNT_VISITS) ? 1 : 0;
-    tp.wf.qO[0] = c->wfQO0.as<float4>();
-    tp.wf.qO[1] = c->wfQO1.as<float4>();
-    tp.wf.qD[0] = c->wfQD0.as<float4>();
-    tp.wf.qD[1] = c->wfQD1.as<float4>();
-    tp.wf.hitTUV = c->wfHitTUV.as<float4>();
-    tp.wf.hitInst = c->wfHitInst.as<uint32_t>();
     tp.wf.counts = c->wfCounts.as<uint32_t>();
     tp.wf.overflow = c->wfOverflow.as<uint32_t>();
     CK(cudaMemsetAsync(c->counters.p, 0, 64, c->stream));
-    CK(launch_trace_queue(tp, d_rays, n, d_tuv, d_ids, c->stream));
+    CK(launch_trace_queue(tp, d_rays, n, d_tuv, d_ids, c->tune.depth, c->stream));
     return RG_OK;
 }
 

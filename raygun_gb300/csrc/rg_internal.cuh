@@ -241,6 +241,13 @@ struct TraceParams {
     // frame loop: the first (trace, shade) round computes the camera rays and initial payloads of
     // work items 0 .. W*H*S-1 (8x4-tile order) itself instead of reading a raygen queue
     int firstRound;
+    // ray query (rg_trace_rays_device): queryCount rays read from the caller's buffer (origin, tmin,
+    // direction, tmax: two float4 per ray) and hits written in rg_trace_rays' layout, so the query
+    // needs neither a queue copy before the traversal nor a read-out pass after it
+    const float4* queryRays;
+    float* queryTuv;
+    uint32_t* queryIds;
+    uint32_t queryCount;
 };
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s);
 // Work items of the frame loop: W x H pixels padded to whole 8 x 4 tiles, times S samples.  The first
@@ -281,9 +288,12 @@ int batch_graph_kernels(const TraceTune& tune, int* perBody);
 // raygen.rgen:36-38 for one job of a batch: average its samples into RGBA16F G-buffers
 cudaError_t launch_resolve_job(const float4* samples, const JobDesc& hostJob, uint2* base, uint2* normal, uint2* rough,
                                cudaStream_t s);
-// closest hits of n rays (8 floats each, device memory) by one round of the frame loop's traversal
-// kernel (k_wf_trace): rays into queue 0 of p.wf, one launch, hit records out in rg_trace_rays' layout
-cudaError_t launch_trace_queue(const TraceParams& p, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s);
+// closest hits of n rays (8 floats each, device memory, 16-byte aligned) by one launch of the frame
+// loop's traversal kernel (k_wf_trace in its query form): the kernel takes the rays straight from
+// `rays` and writes the hits in rg_trace_rays' layout; stack of `depth` (16, 24, 32 or 48) entries,
+// 48 when p.countVisits
+cudaError_t launch_trace_queue(const TraceParams& p, const float* rays, uint32_t n, float* tuv, uint32_t* ids, int depth,
+                               cudaStream_t s);
 // closest hits of n rays with a traversal stack of `depth` (16, 24, 32 or 48) entries
 cudaError_t launch_trace_rays(const DevScene& sc, const float* rays, uint32_t n, float* tuv, uint32_t* ids,
                               unsigned long long* counters, int depth, cudaStream_t s);

@@ -1210,12 +1210,32 @@ __global__ void __launch_bounds__(256) k_wfb_raygen(const TraceParams P) {
 // at 128 threads x 48 words that is 27,648 B, and 7 blocks (plus the 1 KB the driver reserves per
 // block) fill the 196 KB shared-memory carve-out exactly.  One more byte per block moves the SM to
 // the 228 KB carve-out and halves the L1 left for BVH records (measured: trace stage +5 %).
-template <bool COUNT, bool BATCH, int THREADS, int DEPTH>
+// a finished ray's hit: the frame loop's hit record (t, u, v, primitive; instance or 0xFFFFFFFF), or
+// for a ray query rg_trace_rays' layout in the caller's buffers (t, u, v and (instance, primitive);
+// zeros and 0xFFFFFFFF for a miss)
+template <bool QUERY>
+__device__ __forceinline__ void put_hit(const TraceParams& P, uint32_t slot, const Hit& h, bool hit) {
+    if (QUERY) {
+        float* t = P.queryTuv + 3 * (size_t)slot;
+        uint32_t* id = P.queryIds + 2 * (size_t)slot;
+        t[0] = hit ? h.t : 0.0f;
+        t[1] = hit ? h.u : 0.0f;
+        t[2] = hit ? h.v : 0.0f;
+        id[0] = hit ? h.inst : 0xFFFFFFFFu;
+        id[1] = hit ? h.prim : 0xFFFFFFFFu;
+    } else {
+        P.wf.hitTUV[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+        P.wf.hitInst[slot] = hit ? h.inst : 0xFFFFFFFFu;
+    }
+}
+
+// QUERY: the ray-query form (rg_trace_rays_device), rays and hits in the caller's buffers
+template <bool COUNT, bool BATCH, int THREADS, int DEPTH, bool QUERY = false>
 __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k_wf_trace(const __grid_constant__ TraceParams P, int q) {
     RG_DECLARE_SMEM_STACK(stk, THREADS, DEPTH);
     const WavefrontBuffers& wf = P.wf;
-    const bool first = !BATCH && P.firstRound;
-    const uint32_t count = first ? frame_work_total(P) : *(volatile uint32_t*)(wf.counts + q);
+    const bool first = !BATCH && !QUERY && P.firstRound;
+    const uint32_t count = QUERY ? P.queryCount : first ? frame_work_total(P) : *(volatile uint32_t*)(wf.counts + q);
     if (blockIdx.x == 0 && threadIdx.x == 0) wf.counts[q ^ 1] = 0;  // the shade kernel appends there next
     const unsigned lane = threadIdx.x & 31;
     const unsigned ltmask = (1u << lane) - 1u;
@@ -1233,8 +1253,7 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
             vc.overflow++;                                                                   \
             wf.overflow[atomicAdd(wf.counts + 3, 1u)] = slot;                                \
         }                                                                                    \
-        wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));       \
-        wf.hitInst[slot] = T.h.hit ? T.h.inst : 0xFFFFFFFFu;                                 \
+        put_hit<QUERY>(P, slot, T.h, T.h.hit);                                               \
     } while (0)
     bool exhausted = false;
     for (;;) {
@@ -1266,12 +1285,10 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
                     } else {
                         slot = P.perm ? P.perm[k] : k;
                         if (BATCH) scp = &P.jobs[P.slotJob[wf.qPath[q][slot]]].scene;
-                        const float4 o = wf.qO[q][slot], d = wf.qD[q][slot];
+                        const float4 o = QUERY ? P.queryRays[2 * (size_t)slot] : wf.qO[q][slot];
+                        const float4 d = QUERY ? P.queryRays[2 * (size_t)slot + 1] : wf.qD[q][slot];
                         trav_begin(T, RG_SC, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, stk);
-                        if (!T.active) {  // zero direction or the scene box missed
-                            wf.hitTUV[slot] = make_float4(T.h.t, T.h.u, T.h.v, __uint_as_float(T.h.prim));
-                            wf.hitInst[slot] = 0xFFFFFFFFu;
-                        }
+                        if (!T.active) put_hit<QUERY>(P, slot, T.h, false);  // zero direction or the scene box missed
                     }
                 }
             }
@@ -1346,6 +1363,9 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
             frame_work_item(P, s, path, p0, r0);
             o = make_float4(r0.o.x, r0.o.y, r0.o.z, r0.tmin);
             d = make_float4(r0.d.x, r0.d.y, r0.d.z, r0.tmax);
+        } else if (QUERY) {
+            o = P.queryRays[2 * (size_t)s];
+            d = P.queryRays[2 * (size_t)s + 1];
         } else {
             o = __ldcg(&wf.qO[q][s]);
             d = __ldcg(&wf.qD[q][s]);
@@ -1353,8 +1373,7 @@ __global__ void __launch_bounds__(THREADS, (RG_WF_MIN_BLOCKS * 128) / THREADS) k
         }
         Hit h;
         retrace_deep(sc, o, d, &h, P.counters);
-        wf.hitTUV[s] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-        wf.hitInst[s] = h.hit ? h.inst : 0xFFFFFFFFu;
+        put_hit<QUERY>(P, s, h, h.hit);
     }
     if (threadIdx.x == 0) {
         wf.counts[3] = 0;
@@ -1665,33 +1684,6 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(const __grid_const
     }
 }
 
-// rays (origin + tmin, direction + tmax: two float4 each) into queue 0 for one traversal round
-__global__ void k_rays_to_queue(const float4* __restrict__ rays, uint32_t n, const WavefrontBuffers wf) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        wf.counts[0] = n;
-        wf.counts[2] = 0;  // the trace kernel's fetch counter
-    }
-    if (i >= n) return;
-    wf.qO[0][i] = rays[2 * (size_t)i];
-    wf.qD[0][i] = rays[2 * (size_t)i + 1];
-}
-
-// hit records of that round in rg_trace_rays' layout: t, u, v and (instance, primitive), zeros and
-// 0xFFFFFFFF for a miss
-__global__ void k_queue_hits(uint32_t n, const WavefrontBuffers wf, float* __restrict__ tuv, uint32_t* __restrict__ ids) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 h = wf.hitTUV[i];
-    const uint32_t inst = wf.hitInst[i];
-    const bool hit = inst != 0xFFFFFFFFu;
-    tuv[3 * (size_t)i] = hit ? h.x : 0.0f;
-    tuv[3 * (size_t)i + 1] = hit ? h.y : 0.0f;
-    tuv[3 * (size_t)i + 2] = hit ? h.z : 0.0f;
-    ids[2 * (size_t)i] = inst;
-    ids[2 * (size_t)i + 1] = hit ? __float_as_uint(h.w) : 0xFFFFFFFFu;
-}
-
 }  // namespace
 
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t s) {
@@ -1767,18 +1759,39 @@ bool tune_supported(const TraceTune& t) {
     return trace_kernel(true, false, t.threads, t.depth) != nullptr && t.sortKey >= RG_SORT_NONE && t.sortKey <= RG_SORT_MORTON;
 }
 
-cudaError_t launch_trace_queue(const TraceParams& p, const float* rays, uint32_t n, float* tuv, uint32_t* ids, cudaStream_t s) {
+// the query form of the traversal kernel for a stack depth (visit counting: the default depth only)
+static TraceKernel query_kernel(bool count, int depth) {
+    if (count) return k_wf_trace<true, false, kTraceThreads, kTraversalStack, true>;
+    switch (depth) {
+        case 16: return k_wf_trace<false, false, kTraceThreads, 16, true>;
+        case 24: return k_wf_trace<false, false, kTraceThreads, 24, true>;
+        case 32: return k_wf_trace<false, false, kTraceThreads, 32, true>;
+        case 48: return k_wf_trace<false, false, kTraceThreads, 48, true>;
+        default: return nullptr;
+    }
+}
+
+cudaError_t launch_trace_queue(const TraceParams& p, const float* rays, uint32_t n, float* tuv, uint32_t* ids, int depth,
+                               cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const TraceKernel trace = trace_kernel(false, p.countVisits ? 1 : 0, kTraceThreads, kTraversalStack);
+    if (reinterpret_cast<uintptr_t>(rays) & 15u) return cudaErrorInvalidValue;  // read as float4
+    const TraceKernel trace = query_kernel(p.countVisits != 0, depth);
+    if (!trace) return cudaErrorInvalidValue;
     const int g = grid_of((const void*)trace, kTraceThreads);
     if (!g) return cudaErrorUnknown;
     TraceParams q = p;
     q.firstRound = 0;
     q.perm = nullptr;
-    k_rays_to_queue<<<(n + 255) / 256, 256, 0, s>>>(reinterpret_cast<const float4*>(rays), n, q.wf);
+    q.queryRays = reinterpret_cast<const float4*>(rays);
+    q.queryTuv = tuv;
+    q.queryIds = ids;
+    q.queryCount = n;
+    // the fetch counter, the overflow-list length and the finished-block count (the kernel's last
+    // block clears the latter two again)
+    cudaError_t e = cudaMemsetAsync(q.wf.counts + 2, 0, 3 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
     trace<<<g, kTraceThreads, 0, s>>>(q, 0);
-    k_queue_hits<<<(n + 255) / 256, 256, 0, s>>>(n, q.wf, tuv, ids);
-    count_launch(3);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -612,8 +612,10 @@ def stacked_scene(n=1 << 14, width=48, height=32):
 def test_stack_overflow_is_retraced(rg, orc):
     """With a 16-word traversal stack (rg_set_batch_tune) every ray through the stacked scene
     overflows it; each is traced again with the deep stack, so the hits still equal the oracle's,
-    and the batch frame (the wavefront trace kernel, re-traced by its last block) equals rg_render's
-    48-word frame, which does not overflow, bit for bit."""
+    from rg_trace_rays and from the wavefront trace kernel's query form (rg_trace_rays_device,
+    re-traced by its last block), and the batch frame (the same kernel) equals rg_render's 48-word
+    frame, which does not overflow, bit for bit."""
+    import torch
     sc = stacked_scene()
     rt = rg.Raytracer(sc).prepare()
     # coincident centroids: every range is halved, on one CTA down to 64 tasks, then on every SM
@@ -626,6 +628,7 @@ def test_stack_overflow_is_retraced(rg, orc):
     rays = camera_rays(sc)
     to, io = o.trace(rays)
     assert (io[:, 0] != 0xFFFFFFFF).mean() > 0.9
+    d_rays = torch.from_numpy(np.ascontiguousarray(rays, np.float32)).cuda()
     for depth in (48, 16):
         rt.ctx.set_batch_tune(128, depth, "none")
         tg, ig = rt.ctx.trace_rays(rays)
@@ -633,6 +636,18 @@ def test_stack_overflow_is_retraced(rg, orc):
         assert np.array_equal(ig, io) and np.array_equal(tg, to), depth
         assert st["deep_overflows"] == 0
         assert (st["stack_overflows"] > 0) == (depth == 16), (depth, st)
+        d_tuv = torch.full((len(rays), 3), -1.0, device="cuda")
+        d_ids = torch.zeros((len(rays), 2), dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        rt.ctx.trace_rays_device(d_rays.data_ptr(), len(rays), d_tuv.data_ptr(), d_ids.data_ptr())
+        rt.ctx.synchronize()
+        st = rt.ctx.stats()
+        assert np.array_equal(d_ids.cpu().numpy().view(np.uint32), io) and np.array_equal(d_tuv.cpu().numpy(), to), depth
+        assert st["deep_overflows"] == 0
+        assert (st["stack_overflows"] > 0) == (depth == 16), (depth, st)
+    # the query form reads the rays as float4: a pointer off the 16-byte grid is turned away on the host
+    with pytest.raises(rg.RgError, match="aligned"):
+        rt.ctx.trace_rays_device(d_rays.data_ptr() + 4, len(rays) - 1, d_tuv.data_ptr(), d_ids.data_ptr())
     rt.ctx.close()
     for flags in (0, rg.RG_FLAG_HOST_LOOP):
         br = rg.BatchRenderer([sc], flags=flags)
