@@ -153,6 +153,30 @@ def test_closest_hit_degenerate_directions(rg, scene_pair):
     assert (ig[:12000, 0] != 0xFFFFFFFF).sum() > 100
 
 
+@pytest.mark.parametrize("n", [1, 33, None])
+def test_device_query_degenerate_and_ragged(rg, scene_pair, n):
+    """rg_trace_rays_device (the traversal kernel's query form: rays read and hits written in the
+    caller's buffers) on degenerate directions, zero directions and ragged counts (one ray, a partial
+    warp, every ray) gives the oracle's hits bit for bit, misses as zeros and 0xFFFFFFFF."""
+    import torch
+    sc, rt, o = scene_pair
+    rays = np.concatenate([degenerate_rays(sc, 6000, 17), camera_rays(sc, stride=4)])
+    rays = np.concatenate([rays, rays[:7] * np.array([1, 1, 1, 1, 0, 0, 0, 1], np.float32)])  # zero directions
+    rays = np.ascontiguousarray(rays[::-1] if n is None else rays[-n:], np.float32)
+    to, io = o.trace(rays)
+    d_rays = torch.from_numpy(rays).cuda()
+    d_tuv = torch.full((len(rays), 3), -1.0, device="cuda")
+    d_ids = torch.zeros((len(rays), 2), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    rt.ctx.trace_rays_device(d_rays.data_ptr(), len(rays), d_tuv.data_ptr(), d_ids.data_ptr())
+    rt.ctx.synchronize()
+    ig, tg = d_ids.cpu().numpy().view(np.uint32), d_tuv.cpu().numpy()
+    assert np.array_equal(ig, io) and np.array_equal(tg, to)
+    assert (ig[-1 if n else 0, 0] == 0xFFFFFFFF) and (tg[-1 if n else 0] == 0).all()  # a zero direction misses
+    if n is None:
+        assert (ig[:, 0] != 0xFFFFFFFF).sum() > 100
+
+
 def test_records_follow_refit(rg, orc):
     """After BLAS refits and a TLAS rebuild the records carry the moved boxes, and hits still match
     the oracle."""
