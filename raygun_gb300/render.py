@@ -3,6 +3,8 @@
     python -m raygun_gb300.render [--res WxH] [--spp S] [--frames N] [--blas-lbvh] [--tlas-lbvh]
                                   [--learned-filter] [--out frame.npy]
     python -m raygun_gb300.render --lbvh-boxes N [--frames K]   (K LBVH builds over N seeded boxes)
+    python -m raygun_gb300.render --secondary K [--res WxH]      (K closest-hit queries of the scene's
+        first-bounce reflection / refraction rays at 2W x 2H pixel-centre camera rays)
 
 Builds the scene, renders N frames through the library (RenderSystem::render without a window),
 prints the rays of the last frame and optionally saves its RGBA32F framebuffer.  No timing: this is
@@ -28,6 +30,8 @@ def main(argv=None):
     ap.add_argument("--tlas-lbvh", action="store_true", help="the TLAS as an LBVH instead of binned SAH")
     ap.add_argument("--learned-filter", action="store_true", help="the learned roughness filter (committed weights)")
     ap.add_argument("--lbvh-boxes", type=int, default=0, help="instead of frames: LBVH builds over this many seeded boxes")
+    ap.add_argument("--secondary", type=int, default=0,
+                    help="instead of frames: this many rg_trace_rays_device queries of the first-bounce secondary rays")
     ap.add_argument("--out", default=None)
     args = ap.parse_args(argv)
     if args.lbvh_boxes:
@@ -45,6 +49,22 @@ def main(argv=None):
     sc = S.instanced_scene(width=w, height=h, num_samples=args.spp)
     flags = (rgcuda.RG_FLAG_BLAS_LBVH if args.blas_lbvh else 0) | (rgcuda.RG_FLAG_TLAS_LBVH if args.tlas_lbvh else 0)
     rt = rgcuda.Raytracer(sc, flags=flags).prepare()
+    if args.secondary:
+        import torch
+        from .rays import first_bounce_secondary
+        dev = torch.device("cuda", 0)
+        rays = first_bounce_secondary(rt.ctx, sc, sc.instances, dev, 2 * w, 2 * h)
+        tuv = torch.empty(len(rays), 3, device=dev)
+        ids = torch.empty(len(rays), 2, dtype=torch.int32, device=dev)
+        torch.cuda.synchronize(dev)
+        for _ in range(args.secondary):
+            rt.ctx.trace_rays_device(rays.data_ptr(), len(rays), tuv.data_ptr(), ids.data_ptr())
+        rt.ctx.synchronize()
+        hits = int((ids[:, 0] != -1).sum())
+        print(json.dumps({"width": 2 * w, "height": 2 * h, "secondary_rays": len(rays), "queries": args.secondary,
+                          "hits": hits, "stack_overflows": rt.ctx.stats()["stack_overflows"]}))
+        rt.ctx.close()
+        return
     flt = None
     if args.learned_filter:
         from . import filter_train
