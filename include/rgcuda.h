@@ -405,7 +405,7 @@ rg_status rg_measure_l2(int32_t device, uint64_t working_set_bytes, int32_t reps
  * rg_lbvh_build_host, but every pointer is a caller-owned DEVICE buffer (d_boxes: n x 6 floats;
  * d_morton, d_order: n; d_left, d_right: n-1; d_nodeboxes: (n-1) x 6 floats) and the work is queued
  * on `stream` (a cudaStream_t, NULL = legacy default stream) without waiting for it.  Scratch memory
- * is one fixed file-scope device array (about 1.8 MiB) that each GPU loading this library holds until
+ * is one fixed file-scope device array (about 1.9 MiB) that each GPU loading this library holds until
  * exit.  n > RG_LBVH_NOALLOC_MAX_PRIMS returns RG_ERR_TOO_LARGE.  All calls share that array: calls
  * whose GPU work overlaps (e.g. on two unsynchronised streams) race.  The first call on a device
  * looks up the array's device address with that device current; make it before any stream
