@@ -43,7 +43,8 @@ def first_bounce_secondary(ctx, sc, instances, dev, width, height):
     n = len(cam)
     tuv = torch.empty(n, 3, device=dev)
     ids = torch.empty(n, 2, dtype=torch.int32, device=dev)
-    torch.cuda.synchronize(dev)
+    if torch.device(dev).type == "cuda":
+        torch.cuda.synchronize(dev)
     ctx.trace_rays_device(cam.data_ptr(), n, tuv.data_ptr(), ids.data_ptr())
     ctx.synchronize()
     inst_id = ids[:, 0].to(torch.int64) & 0xFFFFFFFF
